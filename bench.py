@@ -1,0 +1,306 @@
+#!/usr/bin/env python3
+"""BSSN right-hand-side throughput on GB300 (grid points x vars / s).
+
+Workload (default): the uneven 20,000-block batch — 14,000 x 13^3,
+4,000 x 19^3, 1,600 x 31^3, 400 x 61^3 padded blocks (eleOrder 6, 3-point
+pad), levels 4-10 on [-32,32]^3, 24 FP64 fields of seeded Brill-Lindquist
+data + 1e-6 noise; one step = one bssnRHS evaluation (6th-order
+derivatives, algebra, KO sigma = 0.1) over all blocks in ONE persistent
+launch.  Units = interior points x 24 variables per step.
+
+Arms:
+  --impl ours (default)   the CUDA library through its C ABI.  `value`:
+                          device-resident fields; `e2e`: host arrays through
+                          dgb_bssn_rhs_host (H2D + compute + D2H timed).
+  --impl reference        the reference's CPU path on the host cores: the
+                          oracle port (C restatement of BSSN_GR/src/rhs.cpp
+                          bssnrhs with OpenMP over blocks, as
+                          BSSN_GR/src/rhsTestBed.cpp runs it), each step a
+                          bounded, stratified sample of the same workload.
+Multi-GPU (torchrun): replicas — every rank runs the whole batch on its own
+GPU with no collective on the data path; max time over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "dendro-5.01_gb300")
+METRIC = ("BSSN RK4 grid-pts×vars/s on 1 GB300 (FP64 vs mixed), % roofline, vs host CPU")
+# Algorithmic FP64 operations per interior point per RHS, 6th order with
+# the reference binding (centred advective, 7-point KO): 8,223.
+FLOP_PER_POINT = 8223.0
+SEED2 = 20261203 + 2
+SEED1 = 20261203 + 1
+
+
+def load_dgb():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("dgb", os.path.join(PKG, "dgb.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def workload(dgb, name):
+    if name == "uneven20k":
+        return dgb.synth_blocks(2, SEED2), SEED2, 0.1
+    if name == "uniform512":
+        return dgb.synth_blocks(1), SEED1, 0.1
+    raise SystemExit(f"unknown workload {name}")
+
+
+def interior_points(blocks):
+    return sum((b.sz[0] - 6) * (b.sz[1] - 6) * (b.sz[2] - 6) for b in blocks)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(blocks, fraction):
+    """Stratified block sample: every k-th block of each size class."""
+    by = {}
+    for i, b in enumerate(blocks):
+        by.setdefault(tuple(b.sz), []).append(i)
+    idx = []
+    for s, lst in sorted(by.items()):
+        k = max(1, int(round(1.0 / fraction)))
+        idx.extend(lst[::k])
+    return sorted(idx)
+
+
+def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1):
+    """Times the oracle port of the reference CPU path on all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from workloads import repack
+    ora = oracle_py.Oracle()
+    cores = os.cpu_count() or 1
+    prm = dgb.params_vector(dgb.default_params(sigma))
+    # calibrate on a small sample, then size the sample to ~target_s
+    frac = 1.0 / 400
+    times = []
+    for attempt in range(3):
+        idx = cpu_sample(blocks, frac)
+        sub = repack(dgb, blocks, idx)
+        u = [np.zeros(dgb.unzipped_size(sub)) for _ in range(24)]
+        dgb.synth_fill_host(sub, u, seed, 1e-6)
+        r = [np.zeros_like(u[0]) for _ in range(24)]
+        t0 = time.perf_counter()
+        assert ora.bssnrhs_blocks(r, u, sub, prm, cores) == 0
+        dt = time.perf_counter() - t0
+        if dt > 0.25 * target_s or frac >= 1.0:
+            break
+        frac = min(1.0, frac * max(2.0, min(50.0, target_s / max(dt, 1e-3))))
+    pts = interior_points(sub)
+    vals = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        assert ora.bssnrhs_blocks(r, u, sub, prm, cores) == 0
+        vals.append(pts * 24 / (time.perf_counter() - t0))
+    return {"value": float(np.median(vals)), "unit": "grid-pts*vars/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{len(sub)} of {len(blocks)} blocks (stratified by size, "
+                      f"{pts} interior points), FP64, OpenMP over blocks"}, vals
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="uneven20k", choices=["uneven20k", "uniform512"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--autotune", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dgb = load_dgb()
+    blocks, seed, sigma = workload(dgb, args.workload)
+    npts = interior_points(blocks)
+    units = npts * 24
+    wl = {"workload": f"{args.workload}: {len(blocks)} padded blocks "
+                      "(14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)" if args.workload == "uneven20k"
+          else f"{args.workload}: 512 blocks 13^3, dx 0.05",
+          "interior_points": npts, "vars": 24, "fd_order": 6, "ko_sigma": sigma,
+          "step": "one bssnRHS (+KO) over all blocks, one persistent launch",
+          "l2": "inputs (37.8 GB of fields) larger than L2" if args.workload == "uneven20k"
+          else "inputs larger than L2 not guaranteed (small workload)",
+          "precision": args.precision}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        base, vals = run_cpu_baseline(dgb, blocks, seed, sigma, steps=args.steps + args.warmup)
+        v = float(np.median(vals[args.warmup:])) if len(vals) > args.warmup else base["value"]
+        ms = units / v * 1e3
+        print(json.dumps({"metric": METRIC, "value": v, "unit": "grid-pts*vars/s", "n_gpus": 1,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64", "data": "synthetic", "config": wl, "impl": "reference",
+                          "cpu_baseline": dict(base, value=v),
+                          "e2e": {"value": v, "unit": "grid-pts*vars/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dgb.init(local)
+    prec = dgb.PREC_MIXED if args.precision == "mixed" else dgb.PREC_FP64
+    plan = dgb.Plan(blocks, dgb.default_params(sigma))
+    n = plan.unzipped
+    du = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(24)]
+    dr = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(24)]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    plan.synth_fill_device([t.data_ptr() for t in du], seed, 1e-6, sh)
+    up = [t.data_ptr() for t in du]
+    rp = [t.data_ptr() for t in dr]
+    if args.autotune:
+        plan.autotune(rp, up, prec, sh)
+    for _ in range(args.warmup):
+        plan.rhs_device(rp, up, prec, sh)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.rhs_device(rp, up, prec, sh)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    value = units * world / (ms * 1e-3)
+
+    fp64_gflops, _ = dgb.measure_fp64_peak()
+    achieved = npts * FLOP_PER_POINT / (ms * 1e-3) / 1e9
+    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
+            "frac": achieved / fp64_gflops, "traffic": None,
+            "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
+            "flop_per_point": FLOP_PER_POINT,
+            "hbm_gbs_algorithmic": 24 * 8 * (n + npts) / (ms * 1e-3) / 1e9}
+    traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_file):
+        try:
+            tj = json.load(open(traffic_file))
+            key = f"{args.workload}:{args.precision}"
+            if key in tj:
+                roof["traffic"] = tj[key]["bytes_per_launch"]
+        except (ValueError, KeyError):
+            pass
+
+    e2e = None
+    if not args.no_e2e:
+        del du, dr
+        torch.cuda.empty_cache()
+        hu = [np.empty(n) for _ in range(24)]
+        dgb.synth_fill_host(blocks, hu, seed, 1e-6)
+        hr = [np.zeros(n) for _ in range(24)]
+        plan.rhs_host(hr, hu, prec)  # warm-up: allocates the plan's staging
+        t0 = time.perf_counter()
+        for _ in range(max(1, min(args.steps, 3))):
+            plan.rhs_host(hr, hu, prec)
+        e2e_s = (time.perf_counter() - t0) / max(1, min(args.steps, 3))
+        e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
+               "h2d_bytes_per_step": 2 * 24 * n * 8, "d2h_bytes_per_step": 24 * n * 8,
+               "ms_per_step": e2e_s * 1e3,
+               "path": "dgb_bssn_rhs_host (reference calling convention, pageable host arrays)"}
+        del hu, hr
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu, _ = run_cpu_baseline(dgb, blocks, seed, sigma)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "grid-pts*vars/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64" if prec == dgb.PREC_FP64 else "f64 (FP32 stencils/KO)",
+               "data": "synthetic (seeded Brill-Lindquist + 1e-6 noise)",
+               "config": dict(wl, tile=plan.tile(prec)),
+               "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+               "gpu_launches": args.steps, "impl": "ours"}
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,443 @@
+// C ABI of the library: device set-up, plans, the RHS entry points (device
+// and host arrays), the RK4 stage update and the synthetic fill.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "dgb_internal.h"
+#include "synth.cuh"
+
+namespace dgb {
+
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+
+static int g_device = -1;
+static int g_nsm = 0;
+
+#define DGB_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+            return DGB_ERR_CUDA;                                                             \
+        }                                                                                    \
+    } while (0)
+
+}  // namespace dgb
+
+using namespace dgb;
+
+struct dgb_plan {
+    int device = -1;
+    int nsm = 0;
+    std::vector<dgb_block_desc> blocks;
+    dgb_bssn_params prm{};
+    uint64_t unzipped = 0, interior = 0;
+    DevBlock *d_blocks = nullptr;
+    uint64_t *d_first = nullptr;  // first padded point of each block (synthetic fill)
+    // work items per tile variant (built lazily)
+    std::vector<WorkItem *> d_items;
+    std::vector<uint32_t> nitems;
+    int variant[2] = {0, 0};  // chosen tile variant per precision
+    unsigned int *d_queue = nullptr;
+    double *d_scratch = nullptr;
+    size_t scratch_doubles = 0;
+    int ctas_per_sm = 1;
+    // device copies for the host-array entry point
+    double *d_u = nullptr, *d_rhs = nullptr;
+};
+
+namespace {
+
+bool interior_block(const dgb_block_desc &b) { return b.sz[0] >= 7 && b.sz[1] >= 7 && b.sz[2] >= 7; }
+
+// Split interior extent m into the fewest tiles of size <= t, as even as possible.
+void split_extent(int m, int t, std::vector<std::pair<int, int>> &out)
+{
+    out.clear();
+    const int nt = (m + t - 1) / t;
+    const int base = m / nt, rem = m % nt;
+    int o = 0;
+    for (int q = 0; q < nt; q++) {
+        const int e = base + (q < rem ? 1 : 0);
+        out.push_back({o, e});
+        o += e;
+    }
+}
+
+dgb_status build_items(dgb_plan *p, int variant)
+{
+    if (p->d_items[variant]) return DGB_OK;
+    const TileShape t = kTileShapes[variant];
+    std::vector<WorkItem> items;
+    std::vector<std::pair<int, int>> sx, sy, sz;
+    for (size_t b = 0; b < p->blocks.size(); b++) {
+        const dgb_block_desc &d = p->blocks[b];
+        split_extent((int)d.sz[0] - 6, t.tx, sx);
+        split_extent((int)d.sz[1] - 6, t.ty, sy);
+        split_extent((int)d.sz[2] - 6, t.tz, sz);
+        for (auto &kz : sz)
+            for (auto &jy : sy)
+                for (auto &ix : sx) {
+                    WorkItem w;
+                    w.blk = (uint32_t)b;
+                    w.o[0] = (uint16_t)ix.first; w.o[1] = (uint16_t)jy.first; w.o[2] = (uint16_t)kz.first;
+                    w.e[0] = (uint16_t)ix.second; w.e[1] = (uint16_t)jy.second; w.e[2] = (uint16_t)kz.second;
+                    items.push_back(w);
+                }
+    }
+    // largest tiles first (longest-processing-time order for the queue)
+    std::stable_sort(items.begin(), items.end(), [](const WorkItem &a, const WorkItem &b) {
+        return a.e[0] * a.e[1] * a.e[2] > b.e[0] * b.e[1] * b.e[2];
+    });
+    WorkItem *d = nullptr;
+    if (!items.empty()) {
+        DGB_CUDA(cudaMalloc(&d, items.size() * sizeof(WorkItem)));
+        DGB_CUDA(cudaMemcpy(d, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+    }
+    p->d_items[variant] = d;
+    p->nitems[variant] = (uint32_t)items.size();
+    return DGB_OK;
+}
+
+RhsParams rhs_params(const dgb_bssn_params &q)
+{
+    RhsParams r;
+    r.l1 = q.lambda[0]; r.l2 = q.lambda[1]; r.l3 = q.lambda[2]; r.l4 = q.lambda[3];
+    r.lf0 = q.lambda_f[0]; r.lf1 = q.lambda_f[1];
+    r.eta_const = q.eta_const; r.eta_r0 = q.eta_r0; r.eta_exp = q.eta_damping_exp;
+    r.sigma = q.ko_sigma;
+    return r;
+}
+
+dgb_status run_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int precision,
+                   int variant, cudaStream_t st)
+{
+    if (precision != DGB_PREC_FP64 && precision != DGB_PREC_MIXED) {
+        set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
+        return DGB_ERR_INVALID;
+    }
+    dgb_status s = build_items(p, variant);
+    if (s != DGB_OK) return s;
+    if (p->nitems[variant] == 0) return DGB_OK;
+    DGB_CUDA(rhs_configure(variant, precision));
+    RhsArgs a;
+    for (int v = 0; v < NV; v++) {
+        a.u[v] = u[v];
+        a.rhs[v] = rhs[v];
+    }
+    a.blocks = p->d_blocks;
+    a.items = p->d_items[variant];
+    a.nitems = p->nitems[variant];
+    a.queue = p->d_queue;
+    a.scratch = p->d_scratch;
+    a.prm = rhs_params(p->prm);
+    const int grid = p->nsm * p->ctas_per_sm;
+    DGB_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned int), st));
+    DGB_CUDA(rhs_launch(variant, precision, a, grid, st));
+    return DGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dgb_version(void) { return 1; }
+
+const char *dgb_last_error(void) { return g_err.c_str(); }
+
+dgb_status dgb_init(int device)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        set_error("no CUDA device");
+        return DGB_ERR_NOT_INIT;
+    }
+    if (device < 0 || device >= n) {
+        set_error("device index out of range");
+        return DGB_ERR_INVALID;
+    }
+    DGB_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    DGB_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major * 10 + prop.minor < 100) {
+        set_error("this library is built for sm_103a (GB300)");
+        return DGB_ERR_UNSUPPORTED;
+    }
+    g_device = device;
+    g_nsm = prop.multiProcessorCount;
+    return DGB_OK;
+}
+
+dgb_status dgb_plan_create(const dgb_block_desc *blocks, size_t nblk, const dgb_bssn_params *prm,
+                           dgb_plan **plan)
+{
+    if (!plan || !prm || (!blocks && nblk)) {
+        set_error("dgb_plan_create: null argument");
+        return DGB_ERR_INVALID;
+    }
+    *plan = nullptr;
+    if (g_device < 0) {
+        set_error("dgb_init not called");
+        return DGB_ERR_NOT_INIT;
+    }
+    if (nblk > 0xFFFFFFFFull) {
+        set_error("too many blocks");
+        return DGB_ERR_INVALID;
+    }
+    dgb_plan *p = new dgb_plan();
+    p->device = g_device;
+    p->nsm = g_nsm;
+    p->prm = *prm;
+    p->blocks.assign(blocks, blocks + nblk);
+    std::vector<DevBlock> db(nblk);
+    std::vector<uint64_t> first(nblk);
+    for (size_t b = 0; b < nblk; b++) {
+        const dgb_block_desc &d = blocks[b];
+        if (!interior_block(d) || d.sz[0] > 4096 || d.sz[1] > 4096 || d.sz[2] > 4096) {
+            set_error("block " + std::to_string(b) + ": each side must be in [7, 4096]");
+            delete p;
+            return DGB_ERR_INVALID;
+        }
+        if (d.bflag != 0) {
+            set_error("block " + std::to_string(b) +
+                      ": domain-boundary blocks (bflag != 0) are not supported by this build");
+            delete p;
+            return DGB_ERR_UNSUPPORTED;
+        }
+        if ((d.sz[0] - 6) > 65535 || (d.sz[1] - 6) > 65535) { delete p; return DGB_ERR_INVALID; }
+        const uint64_t n = (uint64_t)d.sz[0] * d.sz[1] * d.sz[2];
+        p->unzipped = std::max(p->unzipped, d.offset + n);
+        p->interior += (uint64_t)(d.sz[0] - 6) * (d.sz[1] - 6) * (d.sz[2] - 6);
+        db[b].offset = d.offset;
+        for (int a = 0; a < 3; a++) {
+            db[b].sz[a] = d.sz[a];
+            db[b].pmin[a] = d.ptmin[a];
+            db[b].h[a] = (d.ptmax[a] - d.ptmin[a]) / (double)(d.sz[a] - 1);
+            if (!(db[b].h[a] > 0.0) || !std::isfinite(db[b].h[a])) {
+                set_error("block " + std::to_string(b) + ": ptmax must exceed ptmin");
+                delete p;
+                return DGB_ERR_INVALID;
+            }
+        }
+        db[b].pad_ = 0;
+        first[b] = d.offset;
+    }
+    p->d_items.assign(kNumTileShapes, nullptr);
+    p->nitems.assign(kNumTileShapes, 0);
+    p->ctas_per_sm = 1;
+    size_t maxslot = 0;
+    for (int v = 0; v < kNumTileShapes; v++) maxslot = std::max(maxslot, rhs_scratch_per_cta(v));
+    p->scratch_doubles = maxslot * (size_t)p->nsm * p->ctas_per_sm;
+    cudaError_t e = cudaSuccess;
+    if (nblk) {
+        e = cudaMalloc(&p->d_blocks, nblk * sizeof(DevBlock));
+        if (e == cudaSuccess) e = cudaMemcpy(p->d_blocks, db.data(), nblk * sizeof(DevBlock), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMalloc(&p->d_first, nblk * sizeof(uint64_t));
+        if (e == cudaSuccess) e = cudaMemcpy(p->d_first, first.data(), nblk * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_queue, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_scratch, p->scratch_doubles * sizeof(double));
+    if (e != cudaSuccess) {
+        set_error(std::string("dgb_plan_create: ") + cudaGetErrorString(e));
+        dgb_plan_destroy(p);
+        return DGB_ERR_ALLOC;
+    }
+    *plan = p;
+    return DGB_OK;
+}
+
+dgb_status dgb_plan_destroy(dgb_plan *p)
+{
+    if (!p) return DGB_OK;
+    cudaFree(p->d_blocks);
+    cudaFree(p->d_first);
+    for (auto d : p->d_items) cudaFree(d);
+    cudaFree(p->d_queue);
+    cudaFree(p->d_scratch);
+    cudaFree(p->d_u);
+    cudaFree(p->d_rhs);
+    delete p;
+    return DGB_OK;
+}
+
+uint64_t dgb_plan_unzipped_size(const dgb_plan *p) { return p ? p->unzipped : 0; }
+uint64_t dgb_plan_interior_points(const dgb_plan *p) { return p ? p->interior : 0; }
+
+dgb_status dgb_plan_tile(const dgb_plan *p, int precision, uint32_t *tile3)
+{
+    if (!p || !tile3) return DGB_ERR_INVALID;
+    const TileShape t = kTileShapes[p->variant[precision == DGB_PREC_MIXED ? 1 : 0]];
+    tile3[0] = t.tx; tile3[1] = t.ty; tile3[2] = t.tz;
+    return DGB_OK;
+}
+
+int dgb_num_tile_variants(void) { return kNumTileShapes; }
+
+dgb_status dgb_plan_set_tile_variant(dgb_plan *p, int precision, int variant)
+{
+    if (!p || variant < 0 || variant >= kNumTileShapes) {
+        set_error("dgb_plan_set_tile_variant: bad plan or variant");
+        return DGB_ERR_INVALID;
+    }
+    p->variant[precision == DGB_PREC_MIXED ? 1 : 0] = variant;
+    return DGB_OK;
+}
+
+dgb_status dgb_bssn_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int precision,
+                        void *stream)
+{
+    if (!p || !rhs || !u) {
+        set_error("dgb_bssn_rhs: null argument");
+        return DGB_ERR_INVALID;
+    }
+    for (int v = 0; v < NV; v++)
+        if (!rhs[v] || !u[v]) {
+            set_error("dgb_bssn_rhs: null field pointer");
+            return DGB_ERR_INVALID;
+        }
+    const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
+    return run_rhs(p, rhs, u, precision, p->variant[prec], (cudaStream_t)stream);
+}
+
+dgb_status dgb_plan_autotune(dgb_plan *p, double *const *rhs, const double *const *u,
+                             int precision, void *stream)
+{
+    if (!p || !rhs || !u) return DGB_ERR_INVALID;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
+    cudaEvent_t e0, e1;
+    DGB_CUDA(cudaEventCreate(&e0));
+    DGB_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bestv = p->variant[prec];
+    for (int v = 0; v < kNumTileShapes; v++) {
+        dgb_status s = run_rhs(p, rhs, u, precision, v, st);  // warm-up
+        if (s != DGB_OK) return s;
+        DGB_CUDA(cudaEventRecord(e0, st));
+        s = run_rhs(p, rhs, u, precision, v, st);
+        if (s != DGB_OK) return s;
+        DGB_CUDA(cudaEventRecord(e1, st));
+        DGB_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        DGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            bestv = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p->variant[prec] = bestv;
+    return DGB_OK;
+}
+
+dgb_status dgb_bssn_rhs_host(dgb_plan *p, double *const *rhs, const double *const *u, int precision)
+{
+    if (!p || !rhs || !u) {
+        set_error("dgb_bssn_rhs_host: null argument");
+        return DGB_ERR_INVALID;
+    }
+    const size_t n = p->unzipped;
+    if (n == 0) return DGB_OK;
+    if (!p->d_u) {
+        cudaError_t e = cudaMalloc(&p->d_u, (size_t)NV * n * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&p->d_rhs, (size_t)NV * n * sizeof(double));
+        if (e != cudaSuccess) {
+            cudaFree(p->d_u);
+            p->d_u = nullptr;
+            set_error(std::string("dgb_bssn_rhs_host: ") + cudaGetErrorString(e));
+            return DGB_ERR_ALLOC;
+        }
+    }
+    double *du[NV], *dr[NV];
+    for (int v = 0; v < NV; v++) {
+        du[v] = p->d_u + (size_t)v * n;
+        dr[v] = p->d_rhs + (size_t)v * n;
+        DGB_CUDA(cudaMemcpyAsync(du[v], u[v], n * sizeof(double), cudaMemcpyHostToDevice, 0));
+        // the reference leaves the padding of rhs untouched: carry it through
+        DGB_CUDA(cudaMemcpyAsync(dr[v], rhs[v], n * sizeof(double), cudaMemcpyHostToDevice, 0));
+    }
+    const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
+    dgb_status s = run_rhs(p, dr, du, precision, p->variant[prec], 0);
+    if (s != DGB_OK) return s;
+    for (int v = 0; v < NV; v++)
+        DGB_CUDA(cudaMemcpyAsync(rhs[v], dr[v], n * sizeof(double), cudaMemcpyDeviceToHost, 0));
+    DGB_CUDA(cudaStreamSynchronize(0));
+    return DGB_OK;
+}
+
+dgb_status dgb_bssnrhs_block_host(double *const *rhs, const double *const *u, uint64_t offset,
+                                  const double *ptmin, const double *ptmax, const uint32_t *sz,
+                                  uint32_t bflag, const dgb_bssn_params *prm, int precision)
+{
+    if (!rhs || !u || !ptmin || !ptmax || !sz || !prm) {
+        set_error("dgb_bssnrhs_block_host: null argument");
+        return DGB_ERR_INVALID;
+    }
+    dgb_block_desc d;
+    memset(&d, 0, sizeof d);
+    d.offset = 0;
+    for (int a = 0; a < 3; a++) {
+        d.sz[a] = sz[a];
+        d.ptmin[a] = ptmin[a];
+        d.ptmax[a] = ptmax[a];
+    }
+    d.bflag = bflag;
+    dgb_plan *p = nullptr;
+    dgb_status s = dgb_plan_create(&d, 1, prm, &p);
+    if (s != DGB_OK) return s;
+    const double *uo[NV];
+    double *ro[NV];
+    for (int v = 0; v < NV; v++) {
+        uo[v] = u[v] + offset;
+        ro[v] = rhs[v] + offset;
+    }
+    s = dgb_bssn_rhs_host(p, ro, uo, precision);
+    dgb_plan_destroy(p);
+    return s;
+}
+
+dgb_status dgb_rk4_stage(int stage, double *const *dst, const double *const *prev,
+                         const double *const *k, uint64_t nnodes, double dt, double chi_floor,
+                         void *stream)
+{
+    if (stage < 0 || stage > 3 || !dst || !prev || !k) {
+        set_error("dgb_rk4_stage: bad argument");
+        return DGB_ERR_INVALID;
+    }
+    if (nnodes == 0) return DGB_OK;
+    static unsigned int *d_status = nullptr;
+    if (!d_status) DGB_CUDA(cudaMalloc(&d_status, sizeof(unsigned int)));
+    cudaStream_t st = (cudaStream_t)stream;
+    DGB_CUDA(cudaMemsetAsync(d_status, 0, sizeof(unsigned int), st));
+    DGB_CUDA(rk4_launch(stage, dst, prev, k, nnodes, dt, chi_floor, d_status, st));
+    unsigned int h = 0;
+    DGB_CUDA(cudaMemcpyAsync(&h, d_status, sizeof h, cudaMemcpyDeviceToHost, st));
+    DGB_CUDA(cudaStreamSynchronize(st));
+    if (h & 1u) {
+        set_error("dgb_rk4_stage: det(gt) <= 0 at some node (the reference exits here)");
+        return DGB_ERR_CONSTRAINT;
+    }
+    return DGB_OK;
+}
+
+dgb_status dgb_synth_fill_device(dgb_plan *p, double *const *u, uint64_t seed, double noise,
+                                 void *stream)
+{
+    if (!p || !u) return DGB_ERR_INVALID;
+    if (p->blocks.empty()) return DGB_OK;
+    DGB_CUDA(synth_fill_launch(p->d_blocks, (uint32_t)p->blocks.size(), p->d_first, p->unzipped, u,
+                               seed, noise, (cudaStream_t)stream));
+    return DGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,77 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/dendro_gb300.h"
+
+namespace dgb {
+
+constexpr int NV = DGB_NUM_VARS;
+
+// Per-block data the kernels read (built once per plan).
+struct DevBlock {
+    uint64_t offset;
+    uint32_t sz[3];
+    uint32_t pad_;
+    double pmin[3];
+    double h[3];
+};
+
+// One unit of the persistent work queue: a rectangular tile of a block's
+// interior.  o = tile origin in interior coordinates (padded index - 3),
+// e = tile extents.
+struct WorkItem {
+    uint32_t blk;
+    uint16_t o[3];
+    uint16_t e[3];
+};
+
+// Runtime constants of the RHS (bssn:: globals).
+struct RhsParams {
+    double l1, l2, l3, l4, lf0, lf1;
+    double eta_const, eta_r0, eta_exp, sigma;
+};
+
+struct RhsArgs {
+    const double *u[NV];
+    double *rhs[NV];
+    const DevBlock *blocks;
+    const WorkItem *items;
+    uint32_t nitems;
+    unsigned int *queue;   // work-queue head, zeroed before each launch
+    double *scratch;       // per-CTA derivative workspace
+    RhsParams prm;
+};
+
+// Tile schedule: one compiled kernel variant per max tile shape.
+struct TileShape {
+    int tx, ty, tz;
+};
+
+// Compiled variants (index into kTileShapes).
+extern const TileShape kTileShapes[];
+extern const int kNumTileShapes;
+
+size_t rhs_smem_bytes(int variant, int precision);
+int rhs_threads(int variant);
+size_t rhs_scratch_per_cta(int variant);  // doubles
+cudaError_t rhs_launch(int variant, int precision, const RhsArgs &args, int grid,
+                       cudaStream_t stream);
+cudaError_t rhs_configure(int variant, int precision);
+int rhs_max_ctas_per_sm(int variant, int precision);
+
+cudaError_t rk4_launch(int stage, double *const *dst, const double *const *prev,
+                       const double *const *k, uint64_t nnodes, double dt, double chi_floor,
+                       unsigned int *status, cudaStream_t stream);
+
+cudaError_t synth_fill_launch(const DevBlock *blocks, uint32_t nblk, const uint64_t *first_pt,
+                              uint64_t total, double *const *u, uint64_t seed, double noise,
+                              cudaStream_t stream);
+
+void set_error(const std::string &msg);
+
+}  // namespace dgb

@@ -1,0 +1,148 @@
+/*
+ * dendro_gb300.h — C ABI of the GB300 (sm_103a) BSSN per-step hot path.
+ *
+ * Plain pointers and sizes only.  Every entry point returns a dgb_status and
+ * never aborts; dgb_last_error() gives the message of the last failure on
+ * the calling thread.  A plan is not thread-safe; distinct plans on distinct
+ * streams are independent.
+ *
+ * Field layout (identical to the reference's unzipped vectors): 24 separate
+ * arrays, one per evolved variable in the order of bssn::VAR
+ * (BSSN_GR/include/grDef.h:31): alpha, chi, K, Gt0..2, beta0..2, B0..2,
+ * gt00,01,02,11,12,22, At00,01,02,11,12,22.  Block b occupies
+ * [offset_b, offset_b + sz0*sz1*sz2) of each array, x fastest
+ * (IDX(i,j,k) = i + sz0*(j + sz1*k), BSSN_GR/include/rhs.h:21).
+ */
+#ifndef DENDRO_GB300_H
+#define DENDRO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DGB_NUM_VARS 24
+
+typedef enum {
+    DGB_OK = 0,
+    DGB_ERR_INVALID = 1,     /* bad argument, size or block descriptor */
+    DGB_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    DGB_ERR_ALLOC = 3,       /* device or pinned allocation failed */
+    DGB_ERR_NOT_INIT = 4,    /* dgb_init not called / no device */
+    DGB_ERR_TIMEOUT = 5,     /* a bounded device wait expired */
+    DGB_ERR_NONFINITE = 6,   /* NaN/Inf found by a checking entry point */
+    DGB_ERR_CONSTRAINT = 7,  /* det(gt) <= 0 in the RK constraint step */
+    DGB_ERR_UNSUPPORTED = 8  /* valid request this build does not implement */
+} dgb_status;
+
+enum { DGB_PREC_FP64 = 0, DGB_PREC_MIXED = 1 };
+
+/* One padded octant block; what bssnRHS derives per block from ot::Block
+ * (BSSN_GR/src/rhs.cpp:45-62): getOffset(), getAllocationSz{X,Y,Z}(),
+ * getBlkNodeFlag(), ptmin = corner - 3dx, ptmax = corner + 3dx. */
+typedef struct {
+    uint64_t offset;
+    uint32_t sz[3];
+    uint32_t bflag;
+    double ptmin[3];
+    double ptmax[3];
+} dgb_block_desc;
+
+/* The bssn:: globals the RHS and the RK update read
+ * (BSSN_GR/include/parameters.h; defaults BSSN_GR/src/parameters.cpp). */
+typedef struct {
+    double lambda[4];        /* BSSN_LAMBDA (integers in the reference) */
+    double lambda_f[2];      /* BSSN_LAMBDA_F */
+    double eta_const;        /* ETA_CONST */
+    double eta_r0;           /* ETA_R0 */
+    double eta_damping_exp;  /* ETA_DAMPING_EXP */
+    double ko_sigma;         /* KO_DISS_SIGMA */
+    double chi_floor;        /* CHI_FLOOR */
+} dgb_bssn_params;
+
+typedef struct dgb_plan dgb_plan;
+
+/* Library / device set-up.  Replaces the CUDA context set-up the reference
+ * does inside cuda::computeRHS (BSSN_GR/cuda_gr/src/rhs_cuda.cu:12-133). */
+dgb_status dgb_init(int device);
+const char *dgb_last_error(void);
+int dgb_version(void);
+
+/* Block list -> device plan (descriptors, work items, tile schedule,
+ * workspace).  Replaces the per-call block partitioning and workspace
+ * allocation of cuda::computeRHS (rhs_cuda.cu:35-133). */
+dgb_status dgb_plan_create(const dgb_block_desc *blocks, size_t nblk,
+                           const dgb_bssn_params *prm, dgb_plan **plan);
+dgb_status dgb_plan_destroy(dgb_plan *plan);
+/* Number of padded points sum_b sz0*sz1*sz2 (length of each field array). */
+uint64_t dgb_plan_unzipped_size(const dgb_plan *plan);
+uint64_t dgb_plan_interior_points(const dgb_plan *plan);
+
+/* bssnRHS over all blocks of the plan, DEVICE pointers, on `stream`
+ * (a cudaStream_t, 0 = legacy default).  Replaces
+ * void bssnRHS(double**, const double**, const ot::Block*, unsigned)
+ * (BSSN_GR/include/rhs.h:45, BSSN_GR/src/rhs.cpp:9-76).  Writes only the
+ * interior points of each block of rhs[v]; padding is left untouched.
+ * precision: DGB_PREC_FP64 (drop-in) or DGB_PREC_MIXED (FP32 stencils/KO). */
+dgb_status dgb_bssn_rhs(dgb_plan *plan, double *const *rhs, const double *const *u,
+                        int precision, void *stream);
+
+/* Same call with HOST arrays (the reference's calling convention): copies the
+ * fields in, computes, copies the interior of rhs out, synchronously. */
+dgb_status dgb_bssn_rhs_host(dgb_plan *plan, double *const *rhs, const double *const *u,
+                             int precision);
+
+/* One block, host arrays: replaces bssnrhs(double**, const double**,
+ * const unsigned& offset, const double* ptmin, const double* ptmax,
+ * const unsigned* sz, const unsigned& bflag) (BSSN_GR/include/rhs.h:47-50,
+ * BSSN_GR/src/rhs.cpp:86-392). */
+dgb_status dgb_bssnrhs_block_host(double *const *rhs, const double *const *u,
+                                  uint64_t offset, const double *ptmin, const double *ptmax,
+                                  const uint32_t *sz, uint32_t bflag,
+                                  const dgb_bssn_params *prm, int precision);
+
+/* Autotuner: times the candidate tile schedules for each block-size class of
+ * the plan on device buffers and keeps the fastest.  Optional. */
+dgb_status dgb_plan_autotune(dgb_plan *plan, double *const *rhs, const double *const *u,
+                             int precision, void *stream);
+/* Current maximum tile extents (out: tx,ty,tz) of the schedule chosen for
+ * `precision`; every block is cut into the fewest tiles within them. */
+dgb_status dgb_plan_tile(const dgb_plan *plan, int precision, uint32_t *tile3);
+/* Compiled tile schedules: count, and explicit choice (bypasses autotune). */
+int dgb_num_tile_variants(void);
+dgb_status dgb_plan_set_tile_variant(dgb_plan *plan, int precision, int variant);
+
+/* RK4 stage update on zipped (CG) vectors with the per-node constraint
+ * closure, device pointers.  stage 0..2: dst = prev + U[s+1] dt k[s];
+ * stage 3: dst = prev + sum_s C[s] dt k[s]; then enforce_bssn_constraints.
+ * k is 4 x 24 pointers (only k[0..stage] are read).  Replaces the node loops
+ * of RK_BSSN::performSingleIteration (BSSN_GR/src/rkBSSN.cpp:895-905,
+ * 996-1011) and enforce_bssn_constraints (BSSN_GR/src/bssn_constraints.cpp). */
+dgb_status dgb_rk4_stage(int stage, double *const *dst, const double *const *prev,
+                         const double *const *k, uint64_t nnodes, double dt,
+                         double chi_floor, void *stream);
+
+/* Seeded synthetic Brill-Lindquist + U(-1,1)*noise fields at every padded
+ * point of every block (host or device memory).  Host and device fill give
+ * identical bits. */
+dgb_status dgb_synth_fill_host(const dgb_block_desc *blocks, size_t nblk,
+                               double *const *u, uint64_t seed, double noise, int nthreads);
+dgb_status dgb_synth_fill_device(dgb_plan *plan, double *const *u, uint64_t seed,
+                                 double noise, void *stream);
+/* Synthetic block lists.  which = 1: 512 uniform 13^3 blocks, dx = 0.05,
+ * tiled 8x8x8 over [-1.2,1.2]^3; which = 2: 20,000 blocks, 70/20/8/2 % of
+ * 13^3/19^3/31^3/61^3, levels 4-10 on [-32,32]^3.  Pass blocks == NULL to
+ * get the count. */
+dgb_status dgb_synth_blocks(int which, uint64_t seed, dgb_block_desc *blocks, size_t *nblk);
+
+/* Measured FP64 FMA throughput of the current device (GFLOP/s, 2 per FMA)
+ * and the probe kernel's time: the roofline denominator of the FP64-bound
+ * RHS.  No reference counterpart (measurement support). */
+dgb_status dgb_measure_fp64_peak(double *gflops, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DENDRO_GB300_H */

@@ -1,0 +1,498 @@
+/*
+ * ORACLE — test infrastructure only.  A plain-C restatement of the
+ * reference's per-block BSSN hot path, used by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker
+ * and CPU timing arm.  Never linked into, or called by, the product library.
+ *
+ * Parity pin: tests/test_oracle.py compares every function here with the
+ * reference's own code compiled from its sources (oracle/Makefile.ref,
+ * machines that hold the reference tree) and with the golden vectors in
+ * tests/golden/ that the same reference build produced.
+ *
+ * What follows which reference lines:
+ *   stencils      QuadGrav/src/derivs.cpp:2141-2953 (deriv64_*, centred
+ *                 "advective" = deriv64), BSSN_GR/src/derivs.cpp:914-1410
+ *                 (ko_deriv42_*), with the reference loop ranges; only the
+ *                 bflag == 0 (interior-block) branch.
+ *   rhs driver    BSSN_GR/src/rhs.cpp:86-392 (bssnrhs: h = (pmax-pmin)/(n-1),
+ *                 derivative staging per BSSN_GR/scripts/bssnrhs_derivs.h,
+ *                 eta(r) at rhs.cpp:219-223, KO accumulate at :336-373).
+ *   point algebra the BSSN system of CodeGen/bssn.py:36-96 with the tensor
+ *                 helpers of CodeGen/dendro.py (lie :211, trace_free :317,
+ *                 DiDj :160, laplacian :259, sqr :305, up_up :188,
+ *                 christoffels :368-440, compute_ricci :443-527), written as
+ *                 explicit index loops (the reference emits the same system
+ *                 as 970 CSE temporaries, BSSN_GR/src/
+ *                 bssneqs_eta_const_standard_gauge.cpp), with eta const
+ *                 (B_rhs = Gt_rhs - eta B + ...).
+ *   RK4 stage     BSSN_GR/src/rkBSSN.cpp:895-905 and :996-1011, tableau
+ *                 BSSN_GR/include/rkBSSN.h:55-58.
+ *   constraints   BSSN_GR/src/bssn_constraints.cpp:12-172.
+ *
+ * Parameter vector prm[] (doubles): lambda[0..3], lambda_f[0..1], eta_const,
+ * eta_r0, eta_damping_exp, ko_sigma.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NV 24
+enum { A_ = 0, CHI_, K_, GT0_, GT1_, GT2_, BETA0_, BETA1_, BETA2_, B0_, B1_, B2_,
+       SGT0_, SGT1_, SGT2_, SGT3_, SGT4_, SGT5_, SAT0_, SAT1_, SAT2_, SAT3_, SAT4_, SAT5_ };
+
+static const int SYM[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+
+#define IX(i, j, k) ((i) + nx * ((j) + ny * (k)))
+
+/* ---------------- stencils (QuadGrav/src/derivs.cpp) ---------------- */
+/* First derivative, 6th order, along a stride s; the reference evaluates the
+ * six taps left to right and scales by (1/h)/60 (derivs.cpp:2144-2170). */
+static inline double d1_6(const double *u, long s, double c60)
+{
+    return (-1.0 * u[-3 * s] + 9.0 * u[-2 * s] - 45.0 * u[-s] + 45.0 * u[s]
+            - 9.0 * u[2 * s] + 1.0 * u[3 * s]) * c60;
+}
+static inline double d2_6(const double *u, long s, double c180)
+{
+    return (2.0 * u[-3 * s] - 27.0 * u[-2 * s] + 270.0 * u[-s] - 490.0 * u[0]
+            + 270.0 * u[s] - 27.0 * u[2 * s] + 2.0 * u[3 * s]) * c180;
+}
+static inline double ko_4(const double *u, long s, double pre)
+{
+    return pre * (-u[-3 * s] + 6.0 * u[-2 * s] - 15.0 * u[-s] + 20.0 * u[0]
+                  - 15.0 * u[s] + 6.0 * u[2 * s] - u[3 * s]);
+}
+
+/* dir 0: i in [3,nx-3), j,k full (derivs.cpp:2151-2156)
+ * dir 1: i,j in [3,n-3), k full;  dir 2: interior.  Values outside the
+ * computed range are left untouched, as in the reference. */
+void orc_deriv64(int dir, double *D, const double *u, double h, const unsigned *sz)
+{
+    const int nx = sz[0], ny = sz[1], nz = sz[2];
+    const double c60 = (1.0 / h) / 60.0;
+    const int jb = dir == 0 ? 0 : 3, je = dir == 0 ? ny : ny - 3;
+    const int kb = dir == 2 ? 3 : 0, ke = dir == 2 ? nz - 3 : nz;
+    const long s = dir == 0 ? 1 : dir == 1 ? nx : (long)nx * ny;
+    for (int k = kb; k < ke; k++)
+        for (int j = jb; j < je; j++)
+            for (int i = 3; i < nx - 3; i++) D[IX(i, j, k)] = d1_6(&u[IX(i, j, k)], s, c60);
+}
+
+void orc_deriv64_2(int dir, double *D, const double *u, double h, const unsigned *sz)
+{
+    const int nx = sz[0], ny = sz[1], nz = sz[2];
+    const double c180 = (1.0 / (h * h)) / 180.0;
+    const long s = dir == 0 ? 1 : dir == 1 ? nx : (long)nx * ny;
+    for (int k = 3; k < nz - 3; k++)
+        for (int j = 3; j < ny - 3; j++)
+            for (int i = 3; i < nx - 3; i++) D[IX(i, j, k)] = d2_6(&u[IX(i, j, k)], s, c180);
+}
+
+void orc_ko42(int dir, double *D, const double *u, double h, const unsigned *sz)
+{
+    const int nx = sz[0], ny = sz[1], nz = sz[2];
+    const double pre = -1.0 / 64.0 / h;
+    const long s = dir == 0 ? 1 : dir == 1 ? nx : (long)nx * ny;
+    for (int k = 3; k < nz - 3; k++)
+        for (int j = 3; j < ny - 3; j++)
+            for (int i = 3; i < nx - 3; i++) D[IX(i, j, k)] = ko_4(&u[IX(i, j, k)], s, pre);
+}
+
+/* ---------------- point algebra (CodeGen/bssn.py, dendro.py) ---------------- */
+typedef struct {
+    double a, chi, K, Gt[3], b[3], B[3], gt[3][3], At[3][3];
+    double da[3], dchi[3], dK[3], dGt[3][3], db[3][3], dB[3][3];  /* [component][dir] */
+    double dgt[3][3][3], dAt[3][3][3];                           /* [i][j][dir] */
+    double ddgt[3][3][3][3], ddchi[3][3], dda[3][3], ddb[3][3][3]; /* [..][l][m] */
+} orc_point;
+
+/* out[] in variable order (grDef.h:31). */
+void orc_bssn_point(const orc_point *P, const double *prm, double eta, double *out)
+{
+    const double l1 = prm[0], l2 = prm[1], l3 = prm[2], l4 = prm[3];
+    const double lf0 = prm[4], lf1 = prm[5];
+    const double a = P->a, chi = P->chi, K = P->K;
+    double g[3][3], ig[3][3];
+    memcpy(g, P->gt, sizeof g);
+
+    /* inverse conformal metric: adjugate over determinant (dendro.py:351) */
+    const double det = g[0][0] * (g[1][1] * g[2][2] - g[1][2] * g[1][2])
+                     - g[0][1] * g[0][1] * g[2][2] + 2.0 * g[0][1] * g[0][2] * g[1][2]
+                     - g[0][2] * g[0][2] * g[1][1];
+    ig[0][0] = (g[1][1] * g[2][2] - g[1][2] * g[1][2]) / det;
+    ig[0][1] = (g[0][2] * g[1][2] - g[0][1] * g[2][2]) / det;
+    ig[0][2] = (g[0][1] * g[1][2] - g[0][2] * g[1][1]) / det;
+    ig[1][1] = (g[0][0] * g[2][2] - g[0][2] * g[0][2]) / det;
+    ig[1][2] = (g[0][1] * g[0][2] - g[0][0] * g[1][2]) / det;
+    ig[2][2] = (g[0][0] * g[1][1] - g[0][1] * g[0][1]) / det;
+    ig[1][0] = ig[0][1]; ig[2][0] = ig[0][2]; ig[2][1] = ig[1][2];
+
+    /* Christoffels (dendro.py:368-440) */
+    double C1[3][3][3], C2[3][3][3], C3[3][3][3], igdchi[3], CalGt[3];
+    for (int k = 0; k < 3; k++)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+                C1[k][i][j] = 0.5 * (P->dgt[k][i][j] + P->dgt[k][j][i] - P->dgt[i][j][k]);
+    for (int k = 0; k < 3; k++)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double s = 0.0;
+                for (int l = 0; l < 3; l++) s += ig[k][l] * C1[l][i][j];
+                C2[k][i][j] = s;
+            }
+    for (int i = 0; i < 3; i++) {
+        double s = 0.0;
+        for (int m = 0; m < 3; m++) s += ig[i][m] * P->dchi[m];
+        igdchi[i] = s;
+    }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++)
+                C3[i][j][k] = C2[i][j][k] - 0.5 / chi * ((i == j ? P->dchi[k] : 0.0)
+                              + (i == k ? P->dchi[j] : 0.0) - g[j][k] * igdchi[i]);
+    for (int i = 0; i < 3; i++) {
+        double s = 0.0;
+        for (int k = 0; k < 3; k++)
+            for (int l = 0; l < 3; l++) s += ig[k][l] * C2[i][k][l];
+        CalGt[i] = s;
+    }
+
+    /* Ricci tensor (dendro.py:443-527) */
+    double R[3][3];
+    double trchi = 0.0, CalGtdchi = 0.0;
+    for (int k = 0; k < 3; k++)
+        for (int l = 0; l < 3; l++)
+            trchi += ig[k][l] * (P->ddchi[k][l] - 3.0 / (2.0 * chi) * P->dchi[k] * P->dchi[l]);
+    for (int m = 0; m < 3; m++) CalGtdchi += CalGt[m] * P->dchi[m];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double t1 = 0.0, t2 = 0.0, t3 = 0.0, t4 = 0.0;
+            for (int l = 0; l < 3; l++)
+                for (int m = 0; m < 3; m++) t1 += ig[l][m] * P->ddgt[i][j][l][m];
+            for (int k = 0; k < 3; k++)
+                t2 += g[k][i] * P->dGt[k][j] + g[k][j] * P->dGt[k][i];
+            for (int k = 0; k < 3; k++) t3 += CalGt[k] * (C1[i][j][k] + C1[j][i][k]);
+            for (int k = 0; k < 3; k++)
+                for (int l = 0; l < 3; l++)
+                    for (int m = 0; m < 3; m++)
+                        t4 += ig[l][m] * (C2[k][l][i] * C1[j][k][m] + C2[k][l][j] * C1[i][k][m]
+                                          + C2[k][i][m] * C1[k][l][j]);
+            const double Rt = -0.5 * t1 + 0.5 * t2 + 0.5 * t3 + t4;
+            double c2d = 0.0;
+            for (int k = 0; k < 3; k++) c2d += C2[k][j][i] * P->dchi[k];
+            const double xR = 1.0 / (2.0 * chi) * (P->ddchi[i][j] - c2d)
+                            - 1.0 / (4.0 * chi * chi) * P->dchi[i] * P->dchi[j];
+            const double Rphi = xR + 1.0 / (2.0 * chi) * g[i][j] * (trchi - CalGtdchi);
+            R[i][j] = Rt + Rphi;
+        }
+
+    /* second covariant derivative of the lapse (dendro.py:160) */
+    double DDa[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double s = 0.0;
+            for (int l = 0; l < 3; l++) s += C3[l][i][j] * P->da[l];
+            DDa[i][j] = P->dda[i][j] - s;
+        }
+
+    double divb = 0.0;
+    for (int k = 0; k < 3; k++) divb += P->db[k][k];
+
+    /* lapse, shift (bssn.py:65-72) */
+    double adva = 0.0;
+    for (int i = 0; i < 3; i++) adva += P->b[i] * P->da[i];
+    const double a_rhs = l1 * adva - 2.0 * a * K;
+    double b_rhs[3];
+    for (int i = 0; i < 3; i++) {
+        double s = 0.0;
+        for (int j = 0; j < 3; j++) s += P->b[j] * P->db[i][j];
+        b_rhs[i] = 3.0 / 4.0 * (lf0 + lf1 * a) * P->B[i] + l2 * s;
+    }
+
+    /* Lie derivatives of weight -2/3 (dendro.py:211) */
+    const double w = -2.0 / 3.0;
+    double gt_rhs[3][3], At_rhs[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double sg = 0.0, sa = 0.0;
+            for (int k = 0; k < 3; k++) {
+                sg += P->b[k] * P->dgt[i][j][k] + g[i][k] * P->db[k][j] + g[k][j] * P->db[k][i]
+                    + w * g[i][j] * P->db[k][k];
+                sa += P->b[k] * P->dAt[i][j][k] + P->At[i][k] * P->db[k][j]
+                    + P->At[k][j] * P->db[k][i] + w * P->At[i][j] * P->db[k][k];
+            }
+            gt_rhs[i][j] = sg - 2.0 * a * P->At[i][j];
+            At_rhs[i][j] = sa;
+        }
+    double advchi = 0.0;
+    for (int i = 0; i < 3; i++) advchi += P->b[i] * P->dchi[i];
+    const double chi_rhs = advchi + w * chi * divb + 2.0 / 3.0 * (chi * a * K);
+
+    /* At: chi * TF(a R - DiDj a) + a (K At - 2 At_ik At^k_j)  (bssn.py:78-80) */
+    double X[3][3], trX = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) X[i][j] = a * R[i][j] - DDa[i][j];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) trX += ig[i][j] * X[i][j];
+    double AUd[3][3]; /* At^k_j = ig^kl At_lj */
+    for (int k = 0; k < 3; k++)
+        for (int j = 0; j < 3; j++) {
+            double s = 0.0;
+            for (int l = 0; l < 3; l++) s += ig[k][l] * P->At[l][j];
+            AUd[k][j] = s;
+        }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double AA = 0.0;
+            for (int k = 0; k < 3; k++) AA += P->At[i][k] * AUd[k][j];
+            At_rhs[i][j] += chi * (X[i][j] - g[i][j] * trX / 3.0)
+                          + a * (K * P->At[i][j] - 2.0 * AA);
+        }
+
+    /* K (bssn.py:82) */
+    double AUU[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double s = 0.0;
+            for (int k = 0; k < 3; k++)
+                for (int l = 0; l < 3; l++) s += ig[i][k] * ig[j][l] * P->At[k][l];
+            AUU[i][j] = s;
+        }
+    double lap = 0.0, sqrA = 0.0, advK = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            lap += chi * ig[i][j] * DDa[i][j];
+            sqrA += P->At[i][j] * AUU[i][j];
+        }
+    for (int i = 0; i < 3; i++) advK += P->b[i] * P->dK[i];
+    const double K_rhs = advK - lap + a * (K * K / 3.0 + sqrA);
+
+    /* Gt, B (bssn.py:86-104) */
+    double Gt_rhs[3], B_rhs[3];
+    for (int i = 0; i < 3; i++) {
+        double s = 0.0;
+        for (int j = 0; j < 3; j++) s += P->b[j] * P->dGt[i][j];
+        for (int j = 0; j < 3; j++) s -= CalGt[j] * P->db[i][j];
+        s += 2.0 / 3.0 * CalGt[i] * divb;
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++)
+                s += ig[j][k] * P->ddb[i][j][k] + ig[i][j] * P->ddb[k][j][k] / 3.0;
+        for (int j = 0; j < 3; j++) s -= 2.0 * AUU[i][j] * P->da[j];
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++) s += 2.0 * a * C2[i][j][k] * AUU[j][k];
+        for (int j = 0; j < 3; j++)
+            s -= a * (3.0 / chi * AUU[i][j] * P->dchi[j] + 4.0 / 3.0 * ig[i][j] * P->dK[j]);
+        Gt_rhs[i] = s;
+    }
+    for (int i = 0; i < 3; i++) {
+        double sB = 0.0, sG = 0.0;
+        for (int j = 0; j < 3; j++) {
+            sB += P->b[j] * P->dB[i][j];
+            sG += P->b[j] * P->dGt[i][j];
+        }
+        B_rhs[i] = Gt_rhs[i] - eta * P->B[i] + l3 * sB - l4 * sG;
+    }
+
+    out[A_] = a_rhs; out[CHI_] = chi_rhs; out[K_] = K_rhs;
+    for (int i = 0; i < 3; i++) {
+        out[GT0_ + i] = Gt_rhs[i];
+        out[BETA0_ + i] = b_rhs[i];
+        out[B0_ + i] = B_rhs[i];
+    }
+    for (int i = 0; i < 3; i++)
+        for (int j = i; j < 3; j++) {
+            out[SGT0_ + SYM[i][j]] = gt_rhs[i][j];
+            out[SAT0_ + SYM[i][j]] = At_rhs[i][j];
+        }
+}
+
+/* ---------------- per-block driver (BSSN_GR/src/rhs.cpp:86-392) ---------------- */
+/* 11 fields carry second derivatives (BSSN_GR/scripts/bssnrhs_derivs.h). */
+static const int HAS_D2[NV] = {1, 1, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0,
+                               1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0};
+
+/* Returns 0 on success, -1 for a domain-boundary block, -2 on allocation
+ * failure.  Writes only interior points of each rhs[v] + offset. */
+int orc_bssnrhs(double **rhs, const double **uz, unsigned long offset,
+                const double *pmin, const double *pmax, const unsigned *sz,
+                unsigned bflag, const double *prm)
+{
+    if (bflag != 0) return -1;
+    const int nx = sz[0], ny = sz[1], nz = sz[2];
+    const size_t n = (size_t)nx * ny * nz;
+    const double h[3] = {(pmax[0] - pmin[0]) / (nx - 1), (pmax[1] - pmin[1]) / (ny - 1),
+                         (pmax[2] - pmin[2]) / (nz - 1)};
+    /* grad[v][d] and, for HAS_D2 fields, grad2[v][0..5] = xx,xy,xz,yy,yz,zz */
+    double *grad[NV][3], *grad2[NV][6];
+    double *pool = (double *)malloc(sizeof(double) * n * (NV * 3 + 11 * 6));
+    if (!pool) return -2;
+    double *p = pool;
+    for (int v = 0; v < NV; v++) {
+        for (int d = 0; d < 3; d++) { grad[v][d] = p; p += n; }
+        for (int q = 0; q < 6; q++) grad2[v][q] = NULL;
+        if (HAS_D2[v]) for (int q = 0; q < 6; q++) { grad2[v][q] = p; p += n; }
+    }
+    for (int v = 0; v < NV; v++) {
+        const double *u = uz[v] + offset;
+        for (int d = 0; d < 3; d++) orc_deriv64(d, grad[v][d], u, h[d], sz);
+        if (HAS_D2[v]) {
+            orc_deriv64_2(0, grad2[v][0], u, h[0], sz);
+            orc_deriv64_2(1, grad2[v][3], u, h[1], sz);
+            orc_deriv64_2(2, grad2[v][5], u, h[2], sz);
+            orc_deriv64(1, grad2[v][1], grad[v][0], h[1], sz); /* d_y(d_x u) */
+            orc_deriv64(2, grad2[v][2], grad[v][0], h[2], sz); /* d_z(d_x u) */
+            orc_deriv64(2, grad2[v][4], grad[v][1], h[2], sz); /* d_z(d_y u) */
+        }
+    }
+    static const int Q[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+    const double eta_const = prm[6], eta_r0 = prm[7], eta_exp = prm[8];
+    for (int k = 3; k < nz - 3; k++) {
+        const double z = pmin[2] + k * h[2];
+        for (int j = 3; j < ny - 3; j++) {
+            const double y = pmin[1] + j * h[1];
+            for (int i = 3; i < nx - 3; i++) {
+                const double x = pmin[0] + i * h[0];
+                const size_t pp = IX(i, j, k);
+                const double r = sqrt(x * x + y * y + z * z);
+                double eta = eta_const;
+                if (r >= eta_r0) eta *= pow(eta_r0 / r, eta_exp);
+                orc_point P;
+#define F(v) (uz[v][offset + pp])
+                P.a = F(A_); P.chi = F(CHI_); P.K = F(K_);
+                for (int c = 0; c < 3; c++) {
+                    P.Gt[c] = F(GT0_ + c); P.b[c] = F(BETA0_ + c); P.B[c] = F(B0_ + c);
+                }
+                for (int a2 = 0; a2 < 3; a2++)
+                    for (int b2 = 0; b2 < 3; b2++) {
+                        P.gt[a2][b2] = F(SGT0_ + SYM[a2][b2]);
+                        P.At[a2][b2] = F(SAT0_ + SYM[a2][b2]);
+                    }
+#undef F
+                for (int d = 0; d < 3; d++) {
+                    P.da[d] = grad[A_][d][pp]; P.dchi[d] = grad[CHI_][d][pp];
+                    P.dK[d] = grad[K_][d][pp];
+                    for (int c = 0; c < 3; c++) {
+                        P.dGt[c][d] = grad[GT0_ + c][d][pp];
+                        P.db[c][d] = grad[BETA0_ + c][d][pp];
+                        P.dB[c][d] = grad[B0_ + c][d][pp];
+                    }
+                    for (int a2 = 0; a2 < 3; a2++)
+                        for (int b2 = 0; b2 < 3; b2++) {
+                            P.dgt[a2][b2][d] = grad[SGT0_ + SYM[a2][b2]][d][pp];
+                            P.dAt[a2][b2][d] = grad[SAT0_ + SYM[a2][b2]][d][pp];
+                        }
+                }
+                for (int l = 0; l < 3; l++)
+                    for (int m = 0; m < 3; m++) {
+                        const int q = Q[l][m];
+                        P.ddchi[l][m] = grad2[CHI_][q][pp];
+                        P.dda[l][m] = grad2[A_][q][pp];
+                        for (int c = 0; c < 3; c++) P.ddb[c][l][m] = grad2[BETA0_ + c][q][pp];
+                        for (int a2 = 0; a2 < 3; a2++)
+                            for (int b2 = 0; b2 < 3; b2++)
+                                P.ddgt[a2][b2][l][m] = grad2[SGT0_ + SYM[a2][b2]][q][pp];
+                    }
+                double out[NV];
+                orc_bssn_point(&P, prm, eta, out);
+                for (int v = 0; v < NV; v++) rhs[v][offset + pp] = out[v];
+            }
+        }
+    }
+    /* KO dissipation reuses the first-derivative scratch (bssnrhs_ko_derivs.h) */
+    const double sigma = prm[9];
+    for (int v = 0; v < NV; v++) {
+        const double *u = uz[v] + offset;
+        for (int d = 0; d < 3; d++) orc_ko42(d, grad[v][d], u, h[d], sz);
+        double *o = rhs[v] + offset;
+        for (int k = 3; k < nz - 3; k++)
+            for (int j = 3; j < ny - 3; j++)
+                for (int i = 3; i < nx - 3; i++) {
+                    const size_t pp = IX(i, j, k);
+                    o[pp] += sigma * (grad[v][0][pp] + grad[v][1][pp] + grad[v][2][pp]);
+                }
+    }
+    free(pool);
+    return 0;
+}
+
+/* bssnRHS over a block list (BSSN_GR/src/rhs.cpp:9-76), OpenMP over blocks
+ * as the reference test bed does (BSSN_GR/src/rhsTestBed.cpp:181-215).
+ * blk[] rows: offset, sz0, sz1, sz2, bflag (as doubles are avoided: ulong). */
+int orc_bssnrhs_blocks(double **rhs, const double **uz, long nblk,
+                       const unsigned long *offsets, const unsigned *sizes /*3 per block*/,
+                       const unsigned *bflags, const double *pmins, const double *pmaxs,
+                       const double *prm, int nthreads)
+{
+    int err = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic) reduction(|:err)
+#endif
+    for (long b = 0; b < nblk; b++)
+        err |= -orc_bssnrhs(rhs, uz, offsets[b], pmins + 3 * b, pmaxs + 3 * b,
+                            sizes + 3 * b, bflags[b], prm);
+    (void)nthreads;
+    return -err;
+}
+
+/* ---------------- RK4 stage update + constraints ---------------- */
+/* BSSN_GR/src/bssn_constraints.cpp:12-172 on one node of SoA vectors. */
+void orc_enforce_bssn_constraints(double **v, size_t node, double chi_floor)
+{
+    const double one_third = 1.0 / 3.0;
+    double g[3][3], A[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            g[i][j] = v[SGT0_ + SYM[i][j]][node];
+            A[i][j] = v[SAT0_ + SYM[i][j]][node];
+        }
+    double det = g[0][0] * (g[1][1] * g[2][2] - g[1][2] * g[1][2]) - g[0][1] * g[0][1] * g[2][2]
+               + 2.0 * g[0][1] * g[0][2] * g[1][2] - g[0][2] * g[0][2] * g[1][1];
+    const double s = 1.0 / pow(det, one_third);
+    for (int j = 0; j < 3; j++)
+        for (int i = 0; i < 3; i++) g[i][j] *= s;
+    det = g[0][0] * (g[1][1] * g[2][2] - g[1][2] * g[1][2]) - g[0][1] * g[0][1] * g[2][2]
+        + 2.0 * g[0][1] * g[0][2] * g[1][2] - g[0][2] * g[0][2] * g[1][1];
+    const double idet = 1.0 / det;
+    double gu[3][3];
+    gu[0][0] = idet * (g[1][1] * g[2][2] - g[1][2] * g[1][2]);
+    gu[0][1] = idet * (-g[0][1] * g[2][2] + g[0][2] * g[1][2]);
+    gu[0][2] = idet * (g[0][1] * g[1][2] - g[0][2] * g[1][1]);
+    gu[1][1] = idet * (g[0][0] * g[2][2] - g[0][2] * g[0][2]);
+    gu[1][2] = idet * (-g[0][0] * g[1][2] + g[0][1] * g[0][2]);
+    gu[2][2] = idet * (g[0][0] * g[1][1] - g[0][1] * g[0][1]);
+    const double tr3 = one_third * (A[0][0] * gu[0][0] + A[1][1] * gu[1][1] + A[2][2] * gu[2][2]
+                                    + 2.0 * (A[0][1] * gu[0][1] + A[0][2] * gu[0][2] + A[1][2] * gu[1][2]));
+    for (int i = 0; i < 3; i++)
+        for (int j = i; j < 3; j++) {
+            v[SAT0_ + SYM[i][j]][node] = A[i][j] - tr3 * g[i][j];
+            v[SGT0_ + SYM[i][j]][node] = g[i][j];
+        }
+    if (v[CHI_][node] < chi_floor) v[CHI_][node] = chi_floor;
+    v[A_][node] = (v[A_][node] < chi_floor) ? chi_floor : v[A_][node]; /* std::max */
+}
+
+/* Stage s in 0..2: im = prev + U[s+1] dt k_s, then enforce (rkBSSN.cpp:895-905).
+ * Final (s == 3): var = prev + sum_s C[s] dt k_s in stage order, then enforce
+ * (rkBSSN.cpp:996-1011).  k[s][v] are the zipped stage vectors. */
+void orc_rk4_stage(int s, double **dst, const double **prev, const double ***k,
+                   size_t nnodes, double dt, double chi_floor)
+{
+    static const double RK4_C[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+    static const double RK4_U[4] = {0.0, 1.0 / 2.0, 1.0 / 2.0, 1.0};
+    for (size_t node = 0; node < nnodes; node++) {
+        for (int v = 0; v < NV; v++) {
+            double x = prev[v][node];
+            if (s < 3) {
+                x += RK4_U[s + 1] * dt * k[s][v][node];
+            } else {
+                for (int q = 0; q < 4; q++) x += RK4_C[q] * dt * k[q][v][node];
+            }
+            dst[v][node] = x;
+        }
+        orc_enforce_bssn_constraints(dst, node, chi_floor);
+    }
+}
