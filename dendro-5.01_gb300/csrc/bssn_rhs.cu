@@ -51,21 +51,41 @@ __constant__ int8_t c_d2index[NV] = {0, 1, -1, -1, -1, -1, 2, 3, 4, -1, -1, -1,
                                      5, 6, 7, 8, 9, 10, -1, -1, -1, -1, -1, -1};
 
 // ---------------------------------------------------------------- FP64 stencils
-// Same taps and coefficients as the reference; nvcc contracts to FMA.
+// The reference's rounding sequence, operation by operation: every tap is a
+// rounded product added left to right, then one rounded scale
+// (QuadGrav/src/derivs.cpp:2164-2170, :2592-2598; BSSN_GR/src/derivs.cpp:963-971).
+// Explicit _rn intrinsics keep nvcc from contracting to FMA: an FMA rounds
+// once where the reference rounds twice, and on fields of size ~1 whose
+// right-hand side is ~1e-6 that difference alone reaches 1e-11 normwise.
+// Multiplications by -1, 1 are exact and are not issued.
 __device__ __forceinline__ double d1_64(const double *u, int s, double c60)
 {
-    return (-1.0 * u[-3 * s] + 9.0 * u[-2 * s] - 45.0 * u[-s] + 45.0 * u[s] - 9.0 * u[2 * s]
-            + 1.0 * u[3 * s]) * c60;
+    double t = __dadd_rn(-u[-3 * s], __dmul_rn(9.0, u[-2 * s]));
+    t = __dsub_rn(t, __dmul_rn(45.0, u[-s]));
+    t = __dadd_rn(t, __dmul_rn(45.0, u[s]));
+    t = __dsub_rn(t, __dmul_rn(9.0, u[2 * s]));
+    t = __dadd_rn(t, u[3 * s]);
+    return __dmul_rn(t, c60);
 }
 __device__ __forceinline__ double d2_64(const double *u, int s, double c180)
 {
-    return (2.0 * u[-3 * s] - 27.0 * u[-2 * s] + 270.0 * u[-s] - 490.0 * u[0] + 270.0 * u[s]
-            - 27.0 * u[2 * s] + 2.0 * u[3 * s]) * c180;
+    double t = __dsub_rn(__dmul_rn(2.0, u[-3 * s]), __dmul_rn(27.0, u[-2 * s]));
+    t = __dadd_rn(t, __dmul_rn(270.0, u[-s]));
+    t = __dsub_rn(t, __dmul_rn(490.0, u[0]));
+    t = __dadd_rn(t, __dmul_rn(270.0, u[s]));
+    t = __dsub_rn(t, __dmul_rn(27.0, u[2 * s]));
+    t = __dadd_rn(t, __dmul_rn(2.0, u[3 * s]));
+    return __dmul_rn(t, c180);
 }
 __device__ __forceinline__ double ko_64(const double *u, int s, double pre)
 {
-    return pre * (-u[-3 * s] + 6.0 * u[-2 * s] - 15.0 * u[-s] + 20.0 * u[0] - 15.0 * u[s]
-                  + 6.0 * u[2 * s] - u[3 * s]);
+    double t = __dadd_rn(-u[-3 * s], __dmul_rn(6.0, u[-2 * s]));
+    t = __dsub_rn(t, __dmul_rn(15.0, u[-s]));
+    t = __dadd_rn(t, __dmul_rn(20.0, u[0]));
+    t = __dsub_rn(t, __dmul_rn(15.0, u[s]));
+    t = __dadd_rn(t, __dmul_rn(6.0, u[2 * s]));
+    t = __dsub_rn(t, u[3 * s]);
+    return __dmul_rn(pre, t);
 }
 
 // ---------------------------------------------------------------- FP32 split stencils
@@ -163,9 +183,11 @@ struct AlgIOw {
     double sigma;
     __device__ __forceinline__ double u(int v) const { return __ldg(uu[v] + gi); }
     __device__ __forceinline__ double d(int s) const { return S[(size_t)s * pmax + p]; }
+    // rhs += sigma * (kx + ky + kz) with the reference's two roundings
+    // (BSSN_GR/src/rhs.cpp:336-373); the KO sum is stored pre-added.
     __device__ __forceinline__ void out(int v, double x) const
     {
-        rr[v][gi] = x + sigma * S[(size_t)(DGB_NUM_DERIV + v) * pmax + p];
+        rr[v][gi] = __dadd_rn(x, __dmul_rn(sigma, S[(size_t)(DGB_NUM_DERIV + v) * pmax + p]));
     }
 };
 
