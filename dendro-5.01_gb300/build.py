@@ -14,6 +14,8 @@ LIB = os.path.join(HERE, "libdendro_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xptxas", "-v", "--expt-relaxed-constexpr"]
+# extra nvcc flags for build experiments, e.g. DGB_NVCC_EXTRA="-DDGB_RHS_MIN_CTAS=1"
+NVCC_FLAGS += os.environ.get("DGB_NVCC_EXTRA", "").split()
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-fopenmp", "-ffp-contract=off",
              "-Wall", "-Wno-unused-function"]
 

@@ -36,6 +36,7 @@
 
 #include "bssn_algebra.cuh"
 #include "dgb_internal.h"
+#include "exact_mul.cuh"
 
 namespace dgb {
 
@@ -45,6 +46,11 @@ const int kNumTileShapes = sizeof(kTileShapes) / sizeof(kTileShapes[0]);
 namespace {
 
 constexpr int kThreads = 256;
+#ifndef DGB_RHS_MIN_CTAS
+#define DGB_RHS_MIN_CTAS 2
+#endif
+// CTAs per SM the register budget is sized for (255 registers at 1, 128 at 2)
+constexpr int kMinBlocks = DGB_RHS_MIN_CTAS;
 
 // fields with second derivatives, VAR order -> D2 index (or -1)
 __constant__ int8_t c_d2index[NV] = {0, 1, -1, -1, -1, -1, 2, 3, 4, -1, -1, -1,
@@ -57,33 +63,35 @@ __constant__ int8_t c_d2index[NV] = {0, 1, -1, -1, -1, -1, 2, 3, 4, -1, -1, -1,
 // Explicit _rn intrinsics keep nvcc from contracting to FMA: an FMA rounds
 // once where the reference rounds twice, and on fields of size ~1 whose
 // right-hand side is ~1e-6 that difference alone reaches 1e-11 normwise.
-// Multiplications by -1, 1 are exact and are not issued.
+// Multiplications by -1, 1 are exact and are not issued; the tap products
+// by the integer coefficients are formed on the integer pipes, bit-identical
+// to DMUL (exact_mul.cuh), which leaves the FP64 pipe the adds and the scale.
 __device__ __forceinline__ double d1_64(const double *u, int s, double c60)
 {
-    double t = __dadd_rn(-u[-3 * s], __dmul_rn(9.0, u[-2 * s]));
-    t = __dsub_rn(t, __dmul_rn(45.0, u[-s]));
-    t = __dadd_rn(t, __dmul_rn(45.0, u[s]));
-    t = __dsub_rn(t, __dmul_rn(9.0, u[2 * s]));
+    double t = __dadd_rn(-u[-3 * s], dgb_mul_const<9>(u[-2 * s]));
+    t = __dsub_rn(t, dgb_mul_const<45>(u[-s]));
+    t = __dadd_rn(t, dgb_mul_const<45>(u[s]));
+    t = __dsub_rn(t, dgb_mul_const<9>(u[2 * s]));
     t = __dadd_rn(t, u[3 * s]);
     return __dmul_rn(t, c60);
 }
 __device__ __forceinline__ double d2_64(const double *u, int s, double c180)
 {
-    double t = __dsub_rn(__dmul_rn(2.0, u[-3 * s]), __dmul_rn(27.0, u[-2 * s]));
-    t = __dadd_rn(t, __dmul_rn(270.0, u[-s]));
-    t = __dsub_rn(t, __dmul_rn(490.0, u[0]));
-    t = __dadd_rn(t, __dmul_rn(270.0, u[s]));
-    t = __dsub_rn(t, __dmul_rn(27.0, u[2 * s]));
-    t = __dadd_rn(t, __dmul_rn(2.0, u[3 * s]));
+    double t = __dsub_rn(dgb_mul2(u[-3 * s]), dgb_mul_const<27>(u[-2 * s]));
+    t = __dadd_rn(t, dgb_mul_const<270>(u[-s]));
+    t = __dsub_rn(t, dgb_mul_const<490>(u[0]));
+    t = __dadd_rn(t, dgb_mul_const<270>(u[s]));
+    t = __dsub_rn(t, dgb_mul_const<27>(u[2 * s]));
+    t = __dadd_rn(t, dgb_mul2(u[3 * s]));
     return __dmul_rn(t, c180);
 }
 __device__ __forceinline__ double ko_64(const double *u, int s, double pre)
 {
-    double t = __dadd_rn(-u[-3 * s], __dmul_rn(6.0, u[-2 * s]));
-    t = __dsub_rn(t, __dmul_rn(15.0, u[-s]));
-    t = __dadd_rn(t, __dmul_rn(20.0, u[0]));
-    t = __dsub_rn(t, __dmul_rn(15.0, u[s]));
-    t = __dadd_rn(t, __dmul_rn(6.0, u[2 * s]));
+    double t = __dadd_rn(-u[-3 * s], dgb_mul_const<6>(u[-2 * s]));
+    t = __dsub_rn(t, dgb_mul_const<15>(u[-s]));
+    t = __dadd_rn(t, dgb_mul_const<20>(u[0]));
+    t = __dsub_rn(t, dgb_mul_const<15>(u[s]));
+    t = __dadd_rn(t, dgb_mul_const<6>(u[2 * s]));
     t = __dsub_rn(t, u[3 * s]);
     return __dmul_rn(pre, t);
 }
@@ -215,7 +223,7 @@ struct Smem {
 };
 
 template <int TX, int TY, int TZ, bool MIXED>
-__global__ void __launch_bounds__(kThreads, 1) rhs_kernel(const RhsArgs args)
+__global__ void __launch_bounds__(kThreads, kMinBlocks) rhs_kernel(const RhsArgs args)
 {
     using G = Geo<TX, TY, TZ>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -514,6 +522,7 @@ cudaError_t rhs_configure(int variant, int precision)
 int rhs_max_ctas_per_sm(int variant, int precision)
 {
     const bool mixed = precision == DGB_PREC_MIXED;
+    if (rhs_configure(variant, precision) != cudaSuccess) return 0;
     DGB_DISPATCH(variant, mixed, occupancy_variant)
     return 0;
 }

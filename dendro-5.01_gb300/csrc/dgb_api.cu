@@ -50,7 +50,7 @@ struct dgb_plan {
     unsigned int *d_queue = nullptr;
     double *d_scratch = nullptr;
     size_t scratch_doubles = 0;
-    int ctas_per_sm = 1;
+    int occupancy[8][2] = {};  // resident CTAs per SM per (variant, precision)
     // device copies for the host-array entry point
     double *d_u = nullptr, *d_rhs = nullptr;
 };
@@ -140,7 +140,7 @@ dgb_status run_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int 
     a.queue = p->d_queue;
     a.scratch = p->d_scratch;
     a.prm = rhs_params(p->prm);
-    const int grid = p->nsm * p->ctas_per_sm;
+    const int grid = p->nsm * p->occupancy[variant][precision == DGB_PREC_MIXED ? 1 : 0];
     DGB_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned int), st));
     DGB_CUDA(rhs_launch(variant, precision, a, grid, st));
     return DGB_OK;
@@ -233,10 +233,15 @@ dgb_status dgb_plan_create(const dgb_block_desc *blocks, size_t nblk, const dgb_
     }
     p->d_items.assign(kNumTileShapes, nullptr);
     p->nitems.assign(kNumTileShapes, 0);
-    p->ctas_per_sm = 1;
-    size_t maxslot = 0;
-    for (int v = 0; v < kNumTileShapes; v++) maxslot = std::max(maxslot, rhs_scratch_per_cta(v));
-    p->scratch_doubles = maxslot * (size_t)p->nsm * p->ctas_per_sm;
+    // workspace for the largest resident grid over all compiled schedules
+    size_t maxcta = 0;
+    for (int v = 0; v < kNumTileShapes; v++)
+        for (int q = 0; q < 2; q++) {
+            const int occ = rhs_max_ctas_per_sm(v, q);
+            p->occupancy[v][q] = std::max(1, std::min(occ, 4));
+            maxcta = std::max(maxcta, rhs_scratch_per_cta(v) * (size_t)p->occupancy[v][q]);
+        }
+    p->scratch_doubles = maxcta * (size_t)p->nsm;
     cudaError_t e = cudaSuccess;
     if (nblk) {
         e = cudaMalloc(&p->d_blocks, nblk * sizeof(DevBlock));

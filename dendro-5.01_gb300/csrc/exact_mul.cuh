@@ -1,0 +1,94 @@
+// Correctly rounded product of a double and a small positive integer
+// constant, computed on the integer pipes.
+//
+// On GB300 the FP64 pipe retires 2 lanes per clock per SM while the integer
+// ALU / IMAD pipes retire 64, so the stencil tap products RN(c * u)
+// (c in {2, 6, 9, 15, 20, 27, 45, 270, 490}) are cheaper as integer
+// arithmetic than as DMUL.  The result is bit-identical to the IEEE-754
+// round-to-nearest-even product (the rounding the reference's stencils use):
+// for x = m * 2^(e-1075) with a 53-bit significand m, c*m is an exact integer
+// below 2^63; it is shifted back to 53 bits with round-half-even on the
+// dropped bits.  Zero, subnormal, infinite/NaN inputs and results that could
+// leave the normal range take the hardware multiply.
+#pragma once
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define DGB_XM_HD __host__ __device__ __forceinline__
+#else
+#define DGB_XM_HD static inline
+#endif
+
+DGB_XM_HD uint64_t dgb_dbits(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    return b;
+#endif
+}
+
+DGB_XM_HD double dgb_bitsd(uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
+#endif
+}
+
+DGB_XM_HD int dgb_clz64(uint64_t v)
+{
+#if defined(__CUDA_ARCH__)
+    return __clzll((long long)v);
+#else
+    return v ? __builtin_clzll(v) : 64;
+#endif
+}
+
+// 2 * x: exact, an exponent increment for normal x.
+DGB_XM_HD double dgb_mul2(double x)
+{
+    const uint64_t b = dgb_dbits(x);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    if (e == 0u || e >= 0x7FEu) {
+#if defined(__CUDA_ARCH__)
+        return __dmul_rn(2.0, x);
+#else
+        return 2.0 * x;
+#endif
+    }
+    return dgb_bitsd(b + (1ull << 52));
+}
+
+// RN(C * x) for a compile-time constant 2 <= C < 1024.
+template <uint32_t C>
+DGB_XM_HD double dgb_mul_const(double x)
+{
+    static_assert(C >= 2 && C < 1024, "small integer constants only");
+    const uint64_t b = dgb_dbits(x);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    if (e == 0u || e >= 0x7FFu - 10u) {
+#if defined(__CUDA_ARCH__)
+        return __dmul_rn((double)C, x);
+#else
+        return (double)C * x;
+#endif
+    }
+    const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+    const uint64_t p = m * (uint64_t)C;           // exact, < 2^63
+    const int sh = 11 - dgb_clz64(p);             // bits beyond 53 (0..10)
+    uint64_t q = p >> sh;
+    const uint64_t rem = p & ((1ull << sh) - 1ull);
+    const uint64_t half = (1ull << sh) >> 1;      // 0 when sh == 0
+    q += (uint64_t)((rem > half) | ((rem == half) & (sh != 0) & (uint32_t)(q & 1u)));
+    const uint64_t carry = q >> 53;               // rounding reached 2^53
+    q >>= carry;
+    const uint64_t ex = (uint64_t)(e + (uint32_t)sh + (uint32_t)carry) << 52;
+    return dgb_bitsd((b & 0x8000000000000000ull) | ex | (q & 0x000FFFFFFFFFFFFFull));
+}

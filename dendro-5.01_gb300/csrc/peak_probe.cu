@@ -62,3 +62,92 @@ extern "C" dgb_status dgb_measure_fp64_peak(double *gflops, double *ms_out)
     if (ms_out) *ms_out = best;
     return DGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Self-test of the integer-pipe exact products (exact_mul.cuh) against the
+// FP64 multiply, on the host or on the current device.
+#include "exact_mul.cuh"
+#include "synth.cuh"
+
+namespace dgb {
+namespace {
+
+DGB_HD double selftest_input(uint64_t seed, uint64_t i)
+{
+    uint64_t b = dgb_mix64(seed ^ dgb_mix64(i));
+    const uint64_t r = dgb_mix64(b);
+    switch (i & 3u) {
+    case 0: b = (b & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(900 + (r % 300)) << 52); break;
+    case 1: b = (b & 0x800FFFFFFFFFF000ull) | (1023ull << 52) | (r & 0xFFFull); break;
+    default: break;  // any bit pattern (zero, subnormal, huge, inf, nan included)
+    }
+    return dgb_bitsd(b);
+}
+
+template <uint32_t C>
+DGB_HD uint64_t selftest_one(double x)
+{
+#if defined(__CUDA_ARCH__)
+    const double a = __dmul_rn((double)C, x);
+#else
+    const double a = (double)C * x;
+#endif
+    const double c = dgb_mul_const<C>(x);
+    const uint64_t ba = dgb_dbits(a), bc = dgb_dbits(c);
+    const bool nan_a = (ba & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+    const bool nan_c = (bc & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+    return (ba != bc && !(nan_a && nan_c)) ? 1u : 0u;
+}
+
+DGB_HD uint64_t selftest_all(double x)
+{
+    uint64_t bad = selftest_one<6>(x) + selftest_one<9>(x) + selftest_one<15>(x)
+                 + selftest_one<20>(x) + selftest_one<27>(x) + selftest_one<45>(x)
+                 + selftest_one<270>(x) + selftest_one<490>(x);
+#if defined(__CUDA_ARCH__)
+    const double two = __dmul_rn(2.0, x);
+#else
+    const double two = 2.0 * x;
+#endif
+    const double t2 = dgb_mul2(x);
+    if (dgb_dbits(two) != dgb_dbits(t2) && two == two) bad++;
+    return bad;
+}
+
+__global__ void selftest_kernel(uint64_t n, uint64_t seed, unsigned long long *bad)
+{
+    unsigned long long local = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        local += selftest_all(selftest_input(seed, i));
+    if (local) atomicAdd(bad, local);
+}
+
+}  // namespace
+}  // namespace dgb
+
+extern "C" dgb_status dgb_selftest_exact_mul(int on_device, uint64_t n, uint64_t seed,
+                                             uint64_t *mismatches)
+{
+    using namespace dgb;
+    if (!mismatches) return DGB_ERR_INVALID;
+    if (!on_device) {
+        uint64_t bad = 0;
+        for (uint64_t i = 0; i < n; i++) bad += selftest_all(selftest_input(seed, i));
+        *mismatches = bad;
+        return DGB_OK;
+    }
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, sizeof *d) != cudaSuccess) return DGB_ERR_ALLOC;
+    cudaMemset(d, 0, sizeof *d);
+    selftest_kernel<<<1024, 256>>>(n, seed, d);
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        set_error(std::string("selftest: ") + cudaGetErrorString(e));
+        return DGB_ERR_CUDA;
+    }
+    *mismatches = h;
+    return DGB_OK;
+}

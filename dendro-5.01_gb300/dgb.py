@@ -11,7 +11,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libdendro_gb300.so")
+# DGB_LIB selects another build of the same library (build experiments)
+LIB_PATH = os.environ.get("DGB_LIB") or os.path.join(HERE, "libdendro_gb300.so")
 NUM_VARS = 24
 
 VAR_NAMES = ["alpha", "chi", "K", "Gt0", "Gt1", "Gt2", "beta0", "beta1", "beta2",
@@ -92,7 +93,16 @@ _SIGS = {
     "dgb_synth_blocks": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(BlockDesc),
                                    C.POINTER(C.c_size_t)]),
     "dgb_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "dgb_selftest_exact_mul": (C.c_int, [C.c_int, C.c_uint64, C.c_uint64,
+                                         C.POINTER(C.c_uint64)]),
 }
+
+
+def selftest_exact_mul(on_device, n, seed=1):
+    bad = C.c_uint64()
+    check(lib().dgb_selftest_exact_mul(on_device, n, seed, C.byref(bad)),
+          "dgb_selftest_exact_mul")
+    return bad.value
 
 
 def measure_fp64_peak():

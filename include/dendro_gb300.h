@@ -142,6 +142,13 @@ dgb_status dgb_synth_blocks(int which, uint64_t seed, dgb_block_desc *blocks, si
  * RHS.  No reference counterpart (measurement support). */
 dgb_status dgb_measure_fp64_peak(double *gflops, double *ms);
 
+/* Self-test of the integer-pipe exact tap products used by the FP64
+ * stencils: mismatches against the IEEE multiply over n pseudo-random
+ * doubles (host when on_device == 0, else the current device).  No
+ * reference counterpart (test support). */
+dgb_status dgb_selftest_exact_mul(int on_device, uint64_t n, uint64_t seed,
+                                  uint64_t *mismatches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,103 @@
+#!/usr/bin/env python3
+"""Generate the golden vectors in this folder from the REFERENCE's own code.
+
+Runs only where the reference tree exists: oracle/Makefile.ref compiles the
+reference's sources (QuadGrav/src/derivs.cpp, the generated
+BSSN_GR/scripts/bssnrhs_*.h drivers and
+BSSN_GR/src/bssneqs_eta_const_standard_gauge.cpp inside the bssnrhs harness
+oracle/ref_bssnrhs.cpp, and BSSN_GR/src/bssn_constraints.cpp).
+
+Inputs come from the library's seeded synthetic generator (host fill); their
+SHA-256 is stored so that a change of the generator is detected.
+
+  python tests/golden/make_golden.py
+"""
+import hashlib
+import importlib.util
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import oracle_py  # noqa: E402
+from workloads import SEED1, interior_mask, repack  # noqa: E402
+
+# uniform 13^3 blocks: 288 holds the puncture at x = -1, 0 is a corner block
+RHS_BLOCKS = [288, 0]
+SIGMA = 0.1
+
+
+def load_dgb():
+    spec = importlib.util.spec_from_file_location("dgb", os.path.join(ROOT, "dendro-5.01_gb300",
+                                                                     "dgb.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def sha(arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def constraint_state(n=64, seed=11):
+    """A perturbed BSSN state for enforce_bssn_constraints (det != 1, trace != 0)."""
+    rng = np.random.default_rng(seed)
+    v = [rng.normal(0.0, 1e-2, n) for _ in range(24)]
+    for q in (12, 15, 17):
+        v[q] += 1.0
+    v[0] += 0.6
+    v[1] += 0.4
+    v[1][:4] = 1e-6  # chi below the floor
+    v[0][4:8] = -0.1  # alpha below the floor
+    return v
+
+
+def main():
+    dgb = load_dgb()
+    oracle_py.build_ref()
+    ref = oracle_py.Reference()
+    blocks = repack(dgb, dgb.synth_blocks(1), RHS_BLOCKS)
+    n = dgb.unzipped_size(blocks)
+    u = [np.zeros(n) for _ in range(24)]
+    dgb.synth_fill_host(blocks, u, SEED1, 1e-6)
+    prm = dgb.params_vector(dgb.default_params(SIGMA))
+    r = [np.zeros(n) for _ in range(24)]
+    for b in blocks:
+        assert ref.bssnrhs(r, u, b, prm) == 0
+    mask = interior_mask(blocks, n)
+    rhs = np.stack([x[mask] for x in r])
+
+    # reference stencils on one field (chi) of the puncture block
+    b0 = blocks[0]
+    sz = tuple(b0.sz)
+    chi = u[1][:sz[0] * sz[1] * sz[2]].reshape(sz[2], sz[1], sz[0])
+    h = (b0.ptmax[0] - b0.ptmin[0]) / (sz[0] - 1)
+    st = {}
+    for kind in ("d1", "d2", "ko"):
+        for d in range(3):
+            st[f"{kind}_{d}"] = ref.stencil(kind, d, chi, h)[3:-3, 3:-3, 3:-3].copy()
+
+    cs = constraint_state()
+    out = [x.copy() for x in cs]
+    for node in range(len(out[0])):
+        ref.enforce(out, node, 1e-4)
+
+    np.savez_compressed(
+        os.path.join(HERE, "bssn_reference.npz"),
+        rhs_blocks=np.array(RHS_BLOCKS), rhs_seed=np.array(SEED1), rhs_sigma=np.array(SIGMA),
+        rhs_input_sha256=np.array(sha(u)), rhs=rhs,
+        stencil_h=np.array(h), **{f"stencil_{k}": v for k, v in st.items()},
+        enforce_in=np.stack(cs), enforce_out=np.stack(out), enforce_chi_floor=np.array(1e-4))
+    print("wrote", os.path.join(HERE, "bssn_reference.npz"))
+
+
+if __name__ == "__main__":
+    main()

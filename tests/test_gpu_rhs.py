@@ -162,3 +162,8 @@ def test_rk4_stage_matches_oracle(dgb, gpu, oracle):
         got = [t.cpu().numpy() for t in dd]
         for v in range(24):
             np.testing.assert_allclose(got[v], want[v], rtol=1e-13, atol=1e-15)
+
+
+def test_exact_mul_device_matches_dmul(dgb, gpu):
+    """The integer-pipe tap products equal DMUL bit for bit on the device."""
+    assert dgb.selftest_exact_mul(1, 1 << 24, seed=3) == 0

@@ -1,0 +1,120 @@
+"""CPU tests of the oracle: pinned to the reference's golden vectors
+(tests/golden/bssn_reference.npz, made by tests/golden/make_golden.py from
+the reference's own compiled sources) and, where the reference tree exists,
+to the reference code itself on more blocks."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from workloads import SEED1, SEED2, host_fields, interior_mask, normwise, repack, sample_uneven
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "bssn_reference.npz")
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN)
+
+
+def golden_inputs(dgb, g):
+    blocks = repack(dgb, dgb.synth_blocks(1), [int(b) for b in g["rhs_blocks"]])
+    u = host_fields(dgb, blocks, int(g["rhs_seed"]))
+    return blocks, u
+
+
+def test_golden_inputs_regenerate(dgb, golden):
+    """The seeded generator still produces the inputs the goldens were made from."""
+    blocks, u = golden_inputs(dgb, golden)
+    h = hashlib.sha256()
+    for a in u:
+        h.update(np.ascontiguousarray(a).tobytes())
+    assert h.hexdigest() == str(golden["rhs_input_sha256"])
+
+
+def test_oracle_rhs_matches_golden(dgb, oracle, golden):
+    blocks, u = golden_inputs(dgb, golden)
+    n = len(u[0])
+    r = [np.zeros(n) for _ in range(24)]
+    prm = dgb.params_vector(dgb.default_params(float(golden["rhs_sigma"])))
+    assert oracle.bssnrhs_blocks(r, u, blocks, prm) == 0
+    mask = interior_mask(blocks, n)
+    got = [x[mask] for x in r]
+    want = list(golden["rhs"])
+    err = normwise(got, want, np.ones(len(got[0]), dtype=bool))
+    assert err.max() <= 1e-13, dict(zip(dgb.VAR_NAMES, err))
+
+
+@pytest.mark.parametrize("kind", ["d1", "d2", "ko"])
+def test_oracle_stencils_bit_exact(dgb, oracle, golden, kind):
+    """Same taps, same order, no contraction: bit-identical to the reference."""
+    blocks, u = golden_inputs(dgb, golden)
+    b0 = blocks[0]
+    sz = tuple(b0.sz)
+    chi = u[1][: sz[0] * sz[1] * sz[2]].reshape(sz[2], sz[1], sz[0])
+    h = float(golden["stencil_h"])
+    for d in range(3):
+        got = oracle.stencil(kind, d, chi, h)[3:-3, 3:-3, 3:-3]
+        assert np.array_equal(got, golden[f"stencil_{kind}_{d}"]), (kind, d)
+
+
+def test_oracle_enforce_matches_golden(oracle, golden):
+    import ctypes as C
+    state = [np.ascontiguousarray(x) for x in golden["enforce_in"]]
+    out = [x.copy() for x in state]
+    arr = (C.c_void_p * 24)(*[a.ctypes.data for a in out])
+    pp = C.cast(arr, C.POINTER(C.c_void_p))
+    for node in range(len(out[0])):
+        oracle.L.orc_enforce_bssn_constraints(pp, node, float(golden["enforce_chi_floor"]))
+    want = golden["enforce_out"]
+    for v in range(24):
+        np.testing.assert_allclose(out[v], want[v], rtol=2e-15, atol=1e-18)
+
+
+def test_oracle_rk4_stage_formula(oracle):
+    """Stage sums of RK_BSSN::performSingleIteration (rkBSSN.cpp:895-905,
+    996-1011) on a state the constraint closure leaves unchanged."""
+    rng = np.random.default_rng(3)
+    n = 257
+    prev = [np.zeros(n) for _ in range(24)]
+    prev[0][:] = 0.7
+    prev[1][:] = 0.5
+    for q in (12, 15, 17):
+        prev[q][:] = 1.0
+    ks = [[np.zeros(n) for _ in range(24)] for _ in range(4)]
+    for s in range(4):
+        for v in (0, 1, 2, 6, 9):  # fields the closure does not touch
+            ks[s][v][:] = rng.normal(0, 1, n)
+    dt = 0.01
+    U = [0.0, 0.5, 0.5, 1.0]
+    Cc = [1 / 6, 1 / 3, 1 / 3, 1 / 6]
+    for s in range(4):
+        out = [np.zeros(n) for _ in range(24)]
+        oracle.rk4_stage(s, out, prev, ks[: s + 1], dt, 1e-4)
+        for v in (2, 6, 9):
+            if s < 3:
+                want = prev[v] + U[s + 1] * dt * ks[s][v]
+            else:
+                want = prev[v].copy()
+                for q in range(4):
+                    want = want + Cc[q] * dt * ks[q][v]
+            np.testing.assert_array_equal(out[v], want)
+
+
+def test_oracle_matches_reference_code(dgb, oracle, reference):
+    """Live pin on more blocks: all 512 uniform blocks (both punctures inside)
+    and a sample of every size class of the uneven batch."""
+    for blocks, seed in ((dgb.synth_blocks(1), SEED1),
+                         (repack(dgb, dgb.synth_blocks(2, SEED2),
+                                 sample_uneven(dgb.synth_blocks(2, SEED2), (4, 2, 1, 0))), SEED2)):
+        u = host_fields(dgb, blocks, seed)
+        n = len(u[0])
+        prm = dgb.params_vector(dgb.default_params(0.1))
+        r1 = [np.zeros(n) for _ in range(24)]
+        r2 = [np.zeros(n) for _ in range(24)]
+        assert oracle.bssnrhs_blocks(r1, u, blocks, prm) == 0
+        for b in blocks:
+            assert reference.bssnrhs(r2, u, b, prm) == 0
+        err = normwise(r1, r2, interior_mask(blocks, n))
+        assert err.max() <= 1e-13, dict(zip(dgb.VAR_NAMES, err))
