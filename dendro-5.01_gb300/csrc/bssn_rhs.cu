@@ -1,42 +1,6 @@
-// BSSN right-hand side on padded octant blocks: one persistent, work-queued
-// launch over all blocks of a plan, whatever their sizes.
-//
-// Work item = a rectangular tile (<= TX x TY x TZ interior points) of one
-// block.  A CTA takes items from a global atomic queue and, per item:
-//   phase D  for each of the 24 fields: stage the padded tile region
-//            (tile + 3 on each side) in shared memory (cp.async, double
-//            buffered: field v+1 lands while field v is differentiated),
-//            then write every derivative the algebra reads, plus the KO sum
-//            kx+ky+kz, to the CTA's slice of the derivative workspace;
-//   phase A  one thread per tile point: the generated algebra
-//            (bssn_algebra.cuh) reads the fields and the workspace and
-//            writes rhs = algebra + sigma * KO for the interior point.
-//
-// Reference behaviour reproduced (BSSN_GR/src/rhs.cpp:86-392 with the
-// QuadGrav 6th-order binding, QuadGrav/include/derivs.h:80-97):
-//   first derivatives  deriv64_{x,y,z}   (QuadGrav/src/derivs.cpp:2141-2560)
-//   second             deriv64_{xx,yy,zz} (:2569-2910)
-//   mixed              d_y(d_x u), d_z(d_x u), d_z(d_y u)
-//                      (BSSN_GR/scripts/bssnrhs_derivs.h), so d_x u is formed
-//                      on the tile plus 3 rows in y and z, d_y u plus 3 in z
-//   advective          deriv64adv_* = centred deriv64 (:2913-2953), hence the
-//                      advective slots alias the first-derivative slots
-//   KO                 ko_deriv42_{x,y,z} (BSSN_GR/src/derivs.cpp:914-1410),
-//                      rhs += sigma * (kx + ky + kz) (rhs.cpp:336-373)
-// Only interior (bflag == 0) blocks; the host rejects others.
-//
-// The mixed-precision variant (MIXED = true) splits each staged FP64 value
-// into an exact float pair hi + lo by integer bit operations (no FP64 pipe
-// work), evaluates every stencil in FP32 on symmetric differences
-// (u[+k] -/+ u[-k] - ..., exact by Sterbenz for smooth data) for the hi and
-// lo parts, and widens the float result to FP64 by integer bit operations.
-// The algebra, the KO accumulate and all field I/O stay FP64.
-#include <cuda_runtime.h>
-#include <stdint.h>
-
-#include "bssn_algebra.cuh"
-#include "dgb_internal.h"
-#include "exact_mul.cuh"
+// Persistent, work-queued launch of the BSSN right-hand side over all blocks
+// of a plan; the per-tile work is rhs_item (rhs_item.cuh).
+#include "rhs_item.cuh"
 
 namespace dgb {
 
@@ -45,199 +9,10 @@ const int kNumTileShapes = sizeof(kTileShapes) / sizeof(kTileShapes[0]);
 
 namespace {
 
-constexpr int kThreads = 256;
-#ifndef DGB_RHS_MIN_CTAS
-#define DGB_RHS_MIN_CTAS 2
-#endif
-// CTAs per SM the register budget is sized for (255 registers at 1, 128 at 2)
-constexpr int kMinBlocks = DGB_RHS_MIN_CTAS;
-
-// fields with second derivatives, VAR order -> D2 index (or -1)
-__constant__ int8_t c_d2index[NV] = {0, 1, -1, -1, -1, -1, 2, 3, 4, -1, -1, -1,
-                                     5, 6, 7, 8, 9, 10, -1, -1, -1, -1, -1, -1};
-
-// ---------------------------------------------------------------- FP64 stencils
-// The reference's rounding sequence, operation by operation: every tap is a
-// rounded product added left to right, then one rounded scale
-// (QuadGrav/src/derivs.cpp:2164-2170, :2592-2598; BSSN_GR/src/derivs.cpp:963-971).
-// Explicit _rn intrinsics keep nvcc from contracting to FMA: an FMA rounds
-// once where the reference rounds twice, and on fields of size ~1 whose
-// right-hand side is ~1e-6 that difference alone reaches 1e-11 normwise.
-// Multiplications by -1, 1 are exact and are not issued; the tap products
-// by the integer coefficients are formed on the integer pipes, bit-identical
-// to DMUL (exact_mul.cuh), which leaves the FP64 pipe the adds and the scale.
-__device__ __forceinline__ double d1_64(const double *u, int s, double c60)
-{
-    double t = __dadd_rn(-u[-3 * s], dgb_mul_const<9>(u[-2 * s]));
-    t = __dsub_rn(t, dgb_mul_const<45>(u[-s]));
-    t = __dadd_rn(t, dgb_mul_const<45>(u[s]));
-    t = __dsub_rn(t, dgb_mul_const<9>(u[2 * s]));
-    t = __dadd_rn(t, u[3 * s]);
-    return __dmul_rn(t, c60);
-}
-__device__ __forceinline__ double d2_64(const double *u, int s, double c180)
-{
-    double t = __dsub_rn(dgb_mul2(u[-3 * s]), dgb_mul_const<27>(u[-2 * s]));
-    t = __dadd_rn(t, dgb_mul_const<270>(u[-s]));
-    t = __dsub_rn(t, dgb_mul_const<490>(u[0]));
-    t = __dadd_rn(t, dgb_mul_const<270>(u[s]));
-    t = __dsub_rn(t, dgb_mul_const<27>(u[2 * s]));
-    t = __dadd_rn(t, dgb_mul2(u[3 * s]));
-    return __dmul_rn(t, c180);
-}
-__device__ __forceinline__ double ko_64(const double *u, int s, double pre)
-{
-    double t = __dadd_rn(-u[-3 * s], dgb_mul_const<6>(u[-2 * s]));
-    t = __dsub_rn(t, dgb_mul_const<15>(u[-s]));
-    t = __dadd_rn(t, dgb_mul_const<20>(u[0]));
-    t = __dsub_rn(t, dgb_mul_const<15>(u[s]));
-    t = __dadd_rn(t, dgb_mul_const<6>(u[2 * s]));
-    t = __dsub_rn(t, u[3 * s]);
-    return __dmul_rn(pre, t);
-}
-
-// ---------------------------------------------------------------- FP32 split stencils
-// A double u is held as (hi, lo) floats with u = hi + lo up to 2^-48 relative:
-// hi = u with its mantissa truncated to 23 bits, lo = the remaining 29 bits,
-// rounded to float.  Built with integer operations only.
-struct F2 {
-    float hi, lo;
-};
-
-__device__ __forceinline__ F2 split_double(double u)
-{
-    const unsigned long long b = __double_as_longlong(u);
-    const unsigned int sign = (unsigned int)(b >> 63);
-    const int e = (int)((b >> 52) & 0x7FF);
-    F2 r;
-    if (e < 1023 - 126 + 1 || e > 1023 + 127) {  // |u| outside normal float range
-        r.hi = 0.0f;
-        r.lo = 0.0f;
-        if (e > 1023 + 127) r.hi = __int_as_float((sign << 31) | 0x7F800000u);
-        return r;
-    }
-    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
-    r.hi = __int_as_float((sign << 31) | ((unsigned int)(e - 1023 + 127) << 23)
-                          | (unsigned int)(mant >> 29));
-    // remaining 29 mantissa bits times 2^(e-1023-52)
-    const unsigned int rest = (unsigned int)(mant & 0x1FFFFFFFull);
-    const int se = e - 1023 - 52;  // exponent of the lowest mantissa bit
-    float scale;
-    if (se >= -126) {
-        scale = __int_as_float((unsigned int)(se + 127) << 23);
-        r.lo = (float)rest * scale;
-    } else {
-        // scale below the normal float range: two steps
-        scale = __int_as_float((unsigned int)(se + 64 + 127) << 23);
-        r.lo = ((float)rest * scale) * 5.421010862427522e-20f;  // 2^-64
-    }
-    if (sign) r.lo = -r.lo;
-    return r;
-}
-
-// float -> double by bit manipulation (exact; zero and normal floats).
-__device__ __forceinline__ double widen(float f)
-{
-    const unsigned int b = __float_as_uint(f);
-    const unsigned int e = (b >> 23) & 0xFF;
-    if (e == 0) return 0.0;  // zero (float subnormals flush; never reached by derivative data)
-    const unsigned long long sign = (unsigned long long)(b >> 31) << 63;
-    const unsigned long long exp = (unsigned long long)(e - 127 + 1023) << 52;
-    const unsigned long long man = (unsigned long long)(b & 0x7FFFFF) << 29;
-    return __longlong_as_double(sign | exp | man);
-}
-
-// first derivative numerator on a float row: 45 a1 - 9 a2 + a3, a_k = u[k]-u[-k]
-__device__ __forceinline__ float n1_32(const float *u, int s)
-{
-    const float a1 = u[s] - u[-s], a2 = u[2 * s] - u[-2 * s], a3 = u[3 * s] - u[-3 * s];
-    return fmaf(45.0f, a1, fmaf(-9.0f, a2, a3));
-}
-// second derivative numerator: 270 s1 - 27 s2 + 2 s3, s_k = (u[k]-u0)+(u[-k]-u0)
-__device__ __forceinline__ float n2_32(const float *u, int s)
-{
-    const float c = u[0];
-    const float s1 = (u[s] - c) + (u[-s] - c), s2 = (u[2 * s] - c) + (u[-2 * s] - c),
-                s3 = (u[3 * s] - c) + (u[-3 * s] - c);
-    return fmaf(270.0f, s1, fmaf(-27.0f, s2, 2.0f * s3));
-}
-// KO numerator: -(t3) + 6 t2 - 15 t1 with t_k = (u[k]-u0)+(u[-k]-u0)
-// (the 20 u0 term is absorbed: -2 + 12 - 30 + 20 = 0)
-__device__ __forceinline__ float nko_32(const float *u, int s)
-{
-    const float c = u[0];
-    const float t1 = (u[s] - c) + (u[-s] - c), t2 = (u[2 * s] - c) + (u[-2 * s] - c),
-                t3 = (u[3 * s] - c) + (u[-3 * s] - c);
-    return fmaf(-15.0f, t1, fmaf(6.0f, t2, -t3));
-}
-
-// ---------------------------------------------------------------- cp.async
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
-{
-    const unsigned int s = (unsigned int)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-// ---------------------------------------------------------------- algebra I/O
-struct AlgIOw {
-    const double *const *uu;
-    double *const *rr;
-    const double *S;
-    int pmax, p;
-    uint64_t gi;
-    double sigma;
-    __device__ __forceinline__ double u(int v) const { return __ldg(uu[v] + gi); }
-    __device__ __forceinline__ double d(int s) const { return S[(size_t)s * pmax + p]; }
-    // rhs += sigma * (kx + ky + kz) with the reference's two roundings
-    // (BSSN_GR/src/rhs.cpp:336-373); the KO sum is stored pre-added.
-    __device__ __forceinline__ void out(int v, double x) const
-    {
-        rr[v][gi] = __dadd_rn(x, __dmul_rn(sigma, S[(size_t)(DGB_NUM_DERIV + v) * pmax + p]));
-    }
-};
-
-struct AlgPrm {
-    double l1, l2, l3, l4, lf0, lf1;
-};
-
-template <int TX, int TY, int TZ>
-struct Geo {
-    static constexpr int PX = TX + 6, PY = TY + 6, PZ = TZ + 6;
-    static constexpr int FBUF = PX * PY * PZ;        // staged field (doubles)
-    static constexpr int DXB = TX * PY * PZ;         // d_x box (cross region)
-    static constexpr int DYB = TX * TY * PZ;         // d_y box
-    static constexpr int PMAX = TX * TY * TZ;
-};
-
-template <int TX, int TY, int TZ, bool MIXED>
-struct Smem {
-    using G = Geo<TX, TY, TZ>;
-    // FP64: two field buffers + d_x box + d_y box (doubles)
-    // MIXED: two field buffers (doubles) + hi/lo float planes + float boxes
-    static constexpr size_t bytes = MIXED
-        ? (2 * G::FBUF * 8 + 2 * G::FBUF * 4 + (G::DXB + G::DYB) * 4)
-        : (2 * G::FBUF * 8 + (G::DXB + G::DYB) * 8);
-};
-
 template <int TX, int TY, int TZ, bool MIXED>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) rhs_kernel(const RhsArgs args)
 {
     using G = Geo<TX, TY, TZ>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    double *fb0 = reinterpret_cast<double *>(smem_raw);
-    double *fb1 = fb0 + G::FBUF;
-    // FP64 boxes
-    double *dxb = fb1 + G::FBUF;
-    double *dyb = dxb + G::DXB;
-    // FP32 planes (MIXED)
-    float *fhi = reinterpret_cast<float *>(fb1 + G::FBUF);
-    float *flo = fhi + G::FBUF;
-    float *dxf = flo + G::FBUF;
-    float *dyf = dxf + G::DXB;
-
     __shared__ int s_item;
     const int tid = threadIdx.x;
     double *S = args.scratch + (size_t)blockIdx.x * DGB_NUM_SLOTS * G::PMAX;
@@ -252,194 +27,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) rhs_kernel(const RhsArgs
         if (it >= (int)args.nitems) break;
         const WorkItem w = args.items[it];
         const DevBlock blk = args.blocks[w.blk];
-        const int nx = blk.sz[0], ny = blk.sz[1];
-        const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
-        const int px = ex + 6, py = ey + 6, pz = ez + 6;
-        const int npad = px * py * pz;
-        const int P = ex * ey * ez;
-        // region start in padded block coordinates = interior origin
-        const uint64_t rbase = blk.offset + (uint64_t)w.o[0]
-                             + (uint64_t)nx * ((uint64_t)w.o[1] + (uint64_t)ny * w.o[2]);
-        const double hx = blk.h[0], hy = blk.h[1], hz = blk.h[2];
-        const double c60[3] = {(1.0 / hx) / 60.0, (1.0 / hy) / 60.0, (1.0 / hz) / 60.0};
-        const double c180[3] = {(1.0 / (hx * hx)) / 180.0, (1.0 / (hy * hy)) / 180.0,
-                                (1.0 / (hz * hz)) / 180.0};
-        const double ko[3] = {-1.0 / 64.0 / hx, -1.0 / 64.0 / hy, -1.0 / 64.0 / hz};
-        const int sy = px, sz = px * py;  // strides in the staged region
-
-        auto issue_load = [&](int v, double *dst) {
-            const double *src = args.u[v] + rbase;
-            for (int q = tid; q < npad; q += kThreads) {
-                const int i = q % px, r = q / px, j = r % py, k = r / py;
-                cp_async8(dst + q, src + i + (uint64_t)nx * (j + (uint64_t)ny * k));
-            }
-            cp_async_commit();
-        };
-
-        // ------------------------------------------------------------ phase D
-        issue_load(0, fb0);
-        for (int v = 0; v < NV; v++) {
-            double *F = (v & 1) ? fb1 : fb0;
-            if (v + 1 < NV) {
-                issue_load(v + 1, (v & 1) ? fb0 : fb1);
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
-            __syncthreads();
-            const int q2 = c_d2index[v];
-            double *Sg = S + (size_t)(3 * v) * G::PMAX;
-            double *Sko = S + (size_t)(DGB_NUM_DERIV + v) * G::PMAX;
-            if constexpr (!MIXED) {
-                if (q2 < 0) {
-                    for (int p = tid; p < P; p += kThreads) {
-                        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
-                        const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                        Sg[p] = d1_64(c, 1, c60[0]);
-                        Sg[G::PMAX + p] = d1_64(c, sy, c60[1]);
-                        Sg[2 * G::PMAX + p] = d1_64(c, sz, c60[2]);
-                        Sko[p] = ko_64(c, 1, ko[0]) + ko_64(c, sy, ko[1]) + ko_64(c, sz, ko[2]);
-                    }
-                } else {
-                    double *S2 = S + (size_t)(DGB_NUM_GRAD + 6 * q2) * G::PMAX;
-                    // (1a) d_x on the cross region: x in tile, (y ext, z tile) or (y tile, z ext)
-                    const int bx_y = ey + 6;  // d_x box rows
-                    const int nA = ex * bx_y * ez, nB = ex * ey * 6;
-                    for (int q = tid; q < nA + nB; q += kThreads) {
-                        int ti, tj, tk;  // box coords: tj in [0,ey+6), tk in [0,ez+6)
-                        if (q < nA) {
-                            ti = q % ex; const int r = q / ex; tj = r % bx_y; tk = r / bx_y + 3;
-                        } else {
-                            const int q3 = q - nA;
-                            ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 3;
-                            const int kk = r / ey;  // 0..5
-                            tk = kk < 3 ? kk : ez + kk;
-                        }
-                        const double *c = F + (ti + 3) + sy * tj + sz * tk;
-                        dxb[ti + ex * (tj + bx_y * tk)] = d1_64(c, 1, c60[0]);
-                    }
-                    // (1b) d_y on x,y in tile, z extended
-                    const int nC = ex * ey * pz;
-                    for (int q = tid; q < nC; q += kThreads) {
-                        const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
-                        const double *c = F + (ti + 3) + sy * (tj + 3) + sz * tk;
-                        dyb[q] = d1_64(c, sy, c60[1]);
-                    }
-                    // (1c) pointwise: d_z, xx, yy, zz, KO
-                    for (int p = tid; p < P; p += kThreads) {
-                        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
-                        const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                        Sg[2 * G::PMAX + p] = d1_64(c, sz, c60[2]);
-                        S2[0 * G::PMAX + p] = d2_64(c, 1, c180[0]);
-                        S2[3 * G::PMAX + p] = d2_64(c, sy, c180[1]);
-                        S2[5 * G::PMAX + p] = d2_64(c, sz, c180[2]);
-                        Sko[p] = ko_64(c, 1, ko[0]) + ko_64(c, sy, ko[1]) + ko_64(c, sz, ko[2]);
-                    }
-                    __syncthreads();
-                    // (2) mixed from the boxes; d_x, d_y at tile points
-                    for (int p = tid; p < P; p += kThreads) {
-                        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
-                        const double *cx = dxb + ti + ex * ((tj + 3) + bx_y * (tk + 3));
-                        const double *cy = dyb + ti + ex * (tj + ey * (tk + 3));
-                        Sg[p] = cx[0];
-                        Sg[G::PMAX + p] = cy[0];
-                        S2[1 * G::PMAX + p] = d1_64(cx, ex, c60[1]);
-                        S2[2 * G::PMAX + p] = d1_64(cx, ex * bx_y, c60[2]);
-                        S2[4 * G::PMAX + p] = d1_64(cy, ex * ey, c60[2]);
-                    }
-                }
-            } else {
-                // ---------------- mixed precision: split staged doubles into float pairs
-                for (int q = tid; q < npad; q += kThreads) {
-                    const F2 f2 = split_double(F[q]);
-                    fhi[q] = f2.hi;
-                    flo[q] = f2.lo;
-                }
-                __syncthreads();
-                const float s60[3] = {(float)c60[0], (float)c60[1], (float)c60[2]};
-                const float s180[3] = {(float)c180[0], (float)c180[1], (float)c180[2]};
-                const float sko[3] = {(float)ko[0], (float)ko[1], (float)ko[2]};
-                auto D1 = [&](int off, int s, float c) {
-                    return (n1_32(fhi + off, s) + n1_32(flo + off, s)) * c;
-                };
-                auto D2 = [&](int off, int s, float c) {
-                    return (n2_32(fhi + off, s) + n2_32(flo + off, s)) * c;
-                };
-                auto KO = [&](int off, int s, float c) {
-                    return (nko_32(fhi + off, s) + nko_32(flo + off, s)) * c;
-                };
-                if (q2 < 0) {
-                    for (int p = tid; p < P; p += kThreads) {
-                        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
-                        const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                        Sg[p] = widen(D1(off, 1, s60[0]));
-                        Sg[G::PMAX + p] = widen(D1(off, sy, s60[1]));
-                        Sg[2 * G::PMAX + p] = widen(D1(off, sz, s60[2]));
-                        Sko[p] = widen(KO(off, 1, sko[0]) + KO(off, sy, sko[1]) + KO(off, sz, sko[2]));
-                    }
-                } else {
-                    double *S2 = S + (size_t)(DGB_NUM_GRAD + 6 * q2) * G::PMAX;
-                    const int bx_y = ey + 6;
-                    const int nA = ex * bx_y * ez, nB = ex * ey * 6;
-                    for (int q = tid; q < nA + nB; q += kThreads) {
-                        int ti, tj, tk;
-                        if (q < nA) {
-                            ti = q % ex; const int r = q / ex; tj = r % bx_y; tk = r / bx_y + 3;
-                        } else {
-                            const int q3 = q - nA;
-                            ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 3;
-                            const int kk = r / ey;
-                            tk = kk < 3 ? kk : ez + kk;
-                        }
-                        dxf[ti + ex * (tj + bx_y * tk)] = D1((ti + 3) + sy * tj + sz * tk, 1, s60[0]);
-                    }
-                    const int nC = ex * ey * pz;
-                    for (int q = tid; q < nC; q += kThreads) {
-                        const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
-                        dyf[q] = D1((ti + 3) + sy * (tj + 3) + sz * tk, sy, s60[1]);
-                    }
-                    for (int p = tid; p < P; p += kThreads) {
-                        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
-                        const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                        Sg[2 * G::PMAX + p] = widen(D1(off, sz, s60[2]));
-                        S2[0 * G::PMAX + p] = widen(D2(off, 1, s180[0]));
-                        S2[3 * G::PMAX + p] = widen(D2(off, sy, s180[1]));
-                        S2[5 * G::PMAX + p] = widen(D2(off, sz, s180[2]));
-                        Sko[p] = widen(KO(off, 1, sko[0]) + KO(off, sy, sko[1]) + KO(off, sz, sko[2]));
-                    }
-                    __syncthreads();
-                    for (int p = tid; p < P; p += kThreads) {
-                        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
-                        const float *cx = dxf + ti + ex * ((tj + 3) + bx_y * (tk + 3));
-                        const float *cy = dyf + ti + ex * (tj + ey * (tk + 3));
-                        Sg[p] = widen(cx[0]);
-                        Sg[G::PMAX + p] = widen(cy[0]);
-                        S2[1 * G::PMAX + p] = widen(n1_32(cx, ex) * s60[1]);
-                        S2[2 * G::PMAX + p] = widen(n1_32(cx, ex * bx_y) * s60[2]);
-                        S2[4 * G::PMAX + p] = widen(n1_32(cy, ex * ey) * s60[2]);
-                    }
-                }
-            }
-            __syncthreads();  // buffer F and the boxes are reused
-        }
-
-        // ------------------------------------------------------------ phase A
-        for (int p = tid; p < P; p += kThreads) {
-            const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
-            const int i = w.o[0] + ti + 3, j = w.o[1] + tj + 3, k = w.o[2] + tk + 3;
-            const uint64_t gi = blk.offset + (uint64_t)i + (uint64_t)nx * ((uint64_t)j + (uint64_t)ny * k);
-            const double x = blk.pmin[0] + i * hx;
-            const double y = blk.pmin[1] + j * hy;
-            const double z = blk.pmin[2] + k * hz;
-            const double rr = sqrt(x * x + y * y + z * z);
-            double eta = args.prm.eta_const;
-            if (rr >= args.prm.eta_r0) {
-                const double q = args.prm.eta_r0 / rr;
-                eta *= (args.prm.eta_exp == 1.0) ? q : pow(q, args.prm.eta_exp);
-            }
-            AlgIOw io{args.u, args.rhs, S, G::PMAX, p, gi, args.prm.sigma};
-            dgb_bssn_algebra(io, aprm, eta);
-        }
+        rhs_item<TX, TY, TZ, MIXED>(args, w, blk, S, aprm);
     }
 }
 
