@@ -80,6 +80,9 @@ _SIGS = {
     "dgb_bssnrhs_block_host": (C.c_int, [PtrArr, PtrArr, C.c_uint64, C.POINTER(C.c_double),
                                          C.POINTER(C.c_double), C.POINTER(C.c_uint32),
                                          C.c_uint32, C.POINTER(BssnParams), C.c_int]),
+    "dgb_bssnrhs_block_noalloc": (C.c_int, [PtrArr, PtrArr, C.c_uint64, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double), C.POINTER(C.c_uint32),
+                                            C.c_uint32, C.POINTER(BssnParams), C.c_void_p]),
     "dgb_plan_autotune": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
     "dgb_plan_tile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint32)]),
     "dgb_num_tile_variants": (C.c_int, []),

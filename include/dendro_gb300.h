@@ -103,6 +103,28 @@ dgb_status dgb_bssnrhs_block_host(double *const *rhs, const double *const *u,
                                   const uint32_t *sz, uint32_t bflag,
                                   const dgb_bssn_params *prm, int precision);
 
+/* One block, DEVICE arrays, and no allocation of any kind.  No counterpart
+ * in the reference (it allocates 210 scratch arrays per block call,
+ * BSSN_GR/scripts/bssnrhs_memalloc.h); it exists for callers that cannot
+ * call cudaMalloc where they need the right-hand side: a solver whose
+ * device memory is fully reserved by its own pool, a host runtime that owns
+ * the device allocator, or a time-step loop that must not pay the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  The derivative
+ * workspace is a fixed array inside the library (DGB_NOALLOC_MAX_TILES
+ * slices, 64 MiB, held on every device that loads the library until exit),
+ * so a block may span at most DGB_NOALLOC_MAX_TILES tiles of 6^3 interior
+ * points (a cube of at most 42^3 padded points); larger blocks are rejected
+ * with DGB_ERR_INVALID.  FP64 only, same results as dgb_bssn_rhs.  The first
+ * call on a device looks up the workspace's device address; make that first
+ * call before any stream capture.  All calls share the workspace: calls
+ * that overlap on the GPU (other streams, other threads) race on it.  The
+ * launch is asynchronous on `stream`. */
+#define DGB_NOALLOC_MAX_TILES 239
+dgb_status dgb_bssnrhs_block_noalloc(double *const *rhs, const double *const *u,
+                                     uint64_t offset, const double *ptmin, const double *ptmax,
+                                     const uint32_t *sz, uint32_t bflag,
+                                     const dgb_bssn_params *prm, void *stream);
+
 /* Autotuner: times the candidate tile schedules for each block-size class of
  * the plan on device buffers and keeps the fastest.  Optional. */
 dgb_status dgb_plan_autotune(dgb_plan *plan, double *const *rhs, const double *const *u,
