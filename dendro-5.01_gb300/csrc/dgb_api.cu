@@ -87,6 +87,12 @@ dgb_status build_items(dgb_plan *p, int variant)
         for (auto &kz : sz)
             for (auto &jy : sy)
                 for (auto &ix : sx) {
+                    if (d.bflag != 0 && (ix.second < 3 || jy.second < 3 || kz.second < 3)) {
+                        // a closure reads up to 5 points inward from a face: the tile
+                        // holding the face must stage them
+                        set_error("tile schedule cuts a boundary block into tiles thinner than 3");
+                        return DGB_ERR_INVALID;
+                    }
                     WorkItem w;
                     w.blk = (uint32_t)b;
                     w.o[0] = (uint16_t)ix.first; w.o[1] = (uint16_t)jy.first; w.o[2] = (uint16_t)kz.first;
@@ -207,13 +213,18 @@ dgb_status dgb_plan_create(const dgb_block_desc *blocks, size_t nblk, const dgb_
             delete p;
             return DGB_ERR_INVALID;
         }
-        if (d.bflag != 0) {
-            set_error("block " + std::to_string(b) +
-                      ": domain-boundary blocks (bflag != 0) are not supported by this build");
+        if (d.bflag > 63u) {
+            set_error("block " + std::to_string(b) + ": bflag has bits beyond the six faces");
             delete p;
-            return DGB_ERR_UNSUPPORTED;
+            return DGB_ERR_INVALID;
         }
-        if ((d.sz[0] - 6) > 65535 || (d.sz[1] - 6) > 65535) { delete p; return DGB_ERR_INVALID; }
+        if (d.bflag != 0 && (d.sz[0] < 13 || d.sz[1] < 13 || d.sz[2] < 13)) {
+            // the one-sided closures read interior points 3..8 from each flagged face
+            set_error("block " + std::to_string(b) +
+                      ": domain-boundary blocks need at least 13 points per side");
+            delete p;
+            return DGB_ERR_INVALID;
+        }
         const uint64_t n = (uint64_t)d.sz[0] * d.sz[1] * d.sz[2];
         p->unzipped = std::max(p->unzipped, d.offset + n);
         p->interior += (uint64_t)(d.sz[0] - 6) * (d.sz[1] - 6) * (d.sz[2] - 6);
@@ -228,7 +239,7 @@ dgb_status dgb_plan_create(const dgb_block_desc *blocks, size_t nblk, const dgb_
                 return DGB_ERR_INVALID;
             }
         }
-        db[b].pad_ = 0;
+        db[b].bflag = d.bflag;
         first[b] = d.offset;
     }
     p->d_items.assign(kNumTileShapes, nullptr);

@@ -16,7 +16,7 @@ constexpr int NV = DGB_NUM_VARS;
 struct DevBlock {
     uint64_t offset;
     uint32_t sz[3];
-    uint32_t pad_;
+    uint32_t bflag;  // domain-boundary faces, bit 2a / 2a+1 = low / high side of axis a
     double pmin[3];
     double h[3];
 };

@@ -42,7 +42,10 @@
 namespace dgb {
 namespace {
 
-constexpr int kThreads = 256;
+#ifndef DGB_RHS_THREADS
+#define DGB_RHS_THREADS 256
+#endif
+constexpr int kThreads = DGB_RHS_THREADS;
 #ifndef DGB_RHS_MIN_CTAS
 #define DGB_RHS_MIN_CTAS 2
 #endif
@@ -92,6 +95,99 @@ __device__ __forceinline__ double ko_64(const double *u, int s, double pre)
     t = __dsub_rn(t, u[3 * s]);
     return __dmul_rn(pre, t);
 }
+
+// ---------------------------------------------------------------- boundary closures
+// One-sided stencils at domain-boundary faces (bflag bit 2a: low side of
+// axis a, bit 2a+1: high side; OCT_DIR_* of include/dendro.h:84-89), as the
+// reference writes them: first derivative QuadGrav/src/derivs.cpp:2174-2230
+// (scale (1/h)/12), second :2602-2650 (scale (1/h^2)/12), KO
+// BSSN_GR/src/derivs.cpp:997-1075 (divided by {59,43,49}/48*64*h).  Taps are
+// (index along the axis, coefficient) in evaluation order; low-side indices
+// are absolute (3..8), high-side ones relative to ie = n - 3.  Rounded
+// product per tap, added left to right: the reference's rounding.
+struct Taps {
+    int n;
+    int idx[6];
+    double c[6];
+};
+__constant__ Taps c_d1lo[3] = {{5, {3, 4, 5, 6, 7}, {-25.0, 48.0, -36.0, 16.0, -3.0}},
+                               {5, {3, 4, 5, 6, 7}, {-3.0, -10.0, 18.0, -6.0, 1.0}},
+                               {4, {3, 4, 6, 7}, {1.0, -8.0, 8.0, -1.0}}};
+__constant__ Taps c_d1hi[3] = {{4, {-5, -4, -2, -1}, {1.0, -8.0, 8.0, -1.0}},
+                               {5, {-5, -4, -3, -2, -1}, {-1.0, 6.0, -18.0, 10.0, 3.0}},
+                               {5, {-5, -4, -3, -2, -1}, {3.0, -16.0, 36.0, -48.0, 25.0}}};
+__constant__ Taps c_d2lo[3] = {{5, {3, 4, 5, 6, 7}, {35.0, -104.0, 114.0, -56.0, 11.0}},
+                               {5, {3, 4, 5, 6, 7}, {11.0, -20.0, 6.0, 4.0, -1.0}},
+                               {5, {3, 4, 5, 6, 7}, {-1.0, 16.0, -30.0, 16.0, -1.0}}};
+__constant__ Taps c_d2hi[3] = {{5, {-5, -4, -3, -2, -1}, {-1.0, 16.0, -30.0, 16.0, -1.0}},
+                               {5, {-5, -4, -3, -2, -1}, {-1.0, 4.0, 6.0, -20.0, 11.0}},
+                               {5, {-5, -4, -3, -2, -1}, {11.0, -56.0, 114.0, -104.0, 35.0}}};
+__constant__ Taps c_kolo[3] = {{4, {6, 5, 4, 3}, {1.0, -3.0, 3.0, -1.0}},
+                               {5, {7, 6, 5, 4, 3}, {1.0, -6.0, 12.0, -10.0, 3.0}},
+                               {6, {8, 7, 6, 5, 4, 3}, {1.0, -6.0, 15.0, -19.0, 12.0, -3.0}}};
+__constant__ Taps c_kohi[3] = {{6, {-6, -5, -4, -3, -2, -1}, {1.0, -6.0, 15.0, -19.0, 12.0, -3.0}},
+                               {5, {-5, -4, -3, -2, -1}, {1.0, -6.0, 12.0, -10.0, 3.0}},
+                               {4, {-4, -3, -2, -1}, {1.0, -3.0, 3.0, -1.0}}};
+
+// c points at the value of the current point (index pos along the axis,
+// stride s); tap index a is read at c[(a + base - pos) * s].
+__device__ __forceinline__ double eval_taps(const double *c, int s, int shift, const Taps &t)
+{
+    double acc = __dmul_rn(t.c[0], c[(t.idx[0] + shift) * s]);
+    for (int q = 1; q < t.n; q++) acc = __dadd_rn(acc, __dmul_rn(t.c[q], c[(t.idx[q] + shift) * s]));
+    return acc;
+}
+
+// Per-axis scales of one block (h = block spacing along the axis).
+struct AxisScale {
+    double c60, c12, c180, c12sq, pre, smr[3];
+};
+
+__device__ __forceinline__ AxisScale axis_scale(double h)
+{
+    AxisScale a;
+    a.c60 = (1.0 / h) / 60.0;
+    a.c12 = (1.0 / h) / 12.0;
+    a.c180 = (1.0 / (h * h)) / 180.0;
+    a.c12sq = (1.0 / (h * h)) / 12.0;
+    a.pre = -1.0 / 64.0 / h;
+    a.smr[0] = __dmul_rn(59.0 / 48.0 * 64, h);  // point 3 / ie-1
+    a.smr[1] = __dmul_rn(43.0 / 48.0 * 64, h);  // point 4 / ie-2
+    a.smr[2] = __dmul_rn(49.0 / 48.0 * 64, h);  // point 5 / ie-3
+    return a;
+}
+
+// Stencils at index pos of an axis of n points with boundary flags lo/hi.
+__device__ __forceinline__ double d1_at(const double *c, int s, int pos, int n, bool lo, bool hi,
+                                        const AxisScale &a)
+{
+    if (lo && pos < 6) return __dmul_rn(eval_taps(c, s, -pos, c_d1lo[pos - 3]), a.c12);
+    if (hi && pos >= n - 6) return __dmul_rn(eval_taps(c, s, n - 3 - pos, c_d1hi[pos - (n - 6)]), a.c12);
+    return d1_64(c, s, a.c60);
+}
+__device__ __forceinline__ double d2_at(const double *c, int s, int pos, int n, bool lo, bool hi,
+                                        const AxisScale &a)
+{
+    if (lo && pos < 6) return __dmul_rn(eval_taps(c, s, -pos, c_d2lo[pos - 3]), a.c12sq);
+    if (hi && pos >= n - 6) return __dmul_rn(eval_taps(c, s, n - 3 - pos, c_d2hi[pos - (n - 6)]), a.c12sq);
+    return d2_64(c, s, a.c180);
+}
+__device__ __forceinline__ double ko_at(const double *c, int s, int pos, int n, bool lo, bool hi,
+                                        const AxisScale &a)
+{
+    if (lo && pos < 6) return __ddiv_rn(eval_taps(c, s, -pos, c_kolo[pos - 3]), a.smr[pos - 3]);
+    if (hi && pos >= n - 6) {
+        const int q = pos - (n - 6);
+        return __ddiv_rn(eval_taps(c, s, n - 3 - pos, c_kohi[q]), a.smr[2 - q]);
+    }
+    return ko_64(c, s, a.pre);
+}
+
+// bssn_bcs falloff / asymptotic value per variable (BSSN_GR/src/rhs.cpp:269-321).
+__constant__ double c_bc_falloff[NV] = {1, 1, 1, 2, 2, 2, 1, 1, 1, 1, 1, 1,
+                                        1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2};
+__constant__ double c_bc_asym[NV] = {1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+                                     1, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0, 0};
 
 // ---------------------------------------------------------------- FP32 split stencils
 // A double u is held as (hi, lo) floats with u = hi + lo up to 2^-48 relative:
@@ -253,6 +349,16 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                             (1.0 / (hz * hz)) / 180.0};
     const double ko[3] = {-1.0 / 64.0 / hx, -1.0 / 64.0 / hy, -1.0 / 64.0 / hz};
     const int sy = px, sz = px * py;  // strides in the staged region
+    const int nz = blk.sz[2];
+    const uint32_t bflag = blk.bflag;
+    const bool blo[3] = {(bflag & 1u) != 0, (bflag & 4u) != 0, (bflag & 16u) != 0};
+    const bool bhi[3] = {(bflag & 2u) != 0, (bflag & 8u) != 0, (bflag & 32u) != 0};
+    AxisScale ax[3];
+    if (bflag != 0) {
+        ax[0] = axis_scale(hx);
+        ax[1] = axis_scale(hy);
+        ax[2] = axis_scale(hz);
+    }
 
     auto issue_load = [&](int v, double *dst) {
         const double *src = args.u[v] + rbase;
@@ -277,7 +383,69 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
         const int q2 = c_d2index[v];
         double *Sg = S + (size_t)(3 * v) * G::PMAX;
         double *Sko = S + (size_t)(DGB_NUM_DERIV + v) * G::PMAX;
-        if constexpr (!MIXED) {
+        if (bflag != 0) {
+            // ---------------- domain-boundary block: closures, FP64 in both precisions
+            if (q2 < 0) {
+                for (int p = tid; p < P; p += kThreads) {
+                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    const int pi = w.o[0] + ti + 3, pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
+                    const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                    Sg[p] = d1_at(c, 1, pi, nx, blo[0], bhi[0], ax[0]);
+                    Sg[G::PMAX + p] = d1_at(c, sy, pj, ny, blo[1], bhi[1], ax[1]);
+                    Sg[2 * G::PMAX + p] = d1_at(c, sz, pk, nz, blo[2], bhi[2], ax[2]);
+                    Sko[p] = ko_at(c, 1, pi, nx, blo[0], bhi[0], ax[0])
+                           + ko_at(c, sy, pj, ny, blo[1], bhi[1], ax[1])
+                           + ko_at(c, sz, pk, nz, blo[2], bhi[2], ax[2]);
+                }
+            } else {
+                double *S2 = S + (size_t)(DGB_NUM_GRAD + 6 * q2) * G::PMAX;
+                const int bx_y = ey + 6;
+                const int nA = ex * bx_y * ez, nB = ex * ey * 6;
+                for (int q = tid; q < nA + nB; q += kThreads) {
+                    int ti, tj, tk;
+                    if (q < nA) {
+                        ti = q % ex; const int r = q / ex; tj = r % bx_y; tk = r / bx_y + 3;
+                    } else {
+                        const int q3 = q - nA;
+                        ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 3;
+                        const int kk = r / ey;
+                        tk = kk < 3 ? kk : ez + kk;
+                    }
+                    const double *c = F + (ti + 3) + sy * tj + sz * tk;
+                    dxb[ti + ex * (tj + bx_y * tk)] = d1_at(c, 1, w.o[0] + ti + 3, nx, blo[0], bhi[0], ax[0]);
+                }
+                const int nC = ex * ey * pz;
+                for (int q = tid; q < nC; q += kThreads) {
+                    const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
+                    const double *c = F + (ti + 3) + sy * (tj + 3) + sz * tk;
+                    dyb[q] = d1_at(c, sy, w.o[1] + tj + 3, ny, blo[1], bhi[1], ax[1]);
+                }
+                for (int p = tid; p < P; p += kThreads) {
+                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    const int pi = w.o[0] + ti + 3, pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
+                    const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                    Sg[2 * G::PMAX + p] = d1_at(c, sz, pk, nz, blo[2], bhi[2], ax[2]);
+                    S2[0 * G::PMAX + p] = d2_at(c, 1, pi, nx, blo[0], bhi[0], ax[0]);
+                    S2[3 * G::PMAX + p] = d2_at(c, sy, pj, ny, blo[1], bhi[1], ax[1]);
+                    S2[5 * G::PMAX + p] = d2_at(c, sz, pk, nz, blo[2], bhi[2], ax[2]);
+                    Sko[p] = ko_at(c, 1, pi, nx, blo[0], bhi[0], ax[0])
+                           + ko_at(c, sy, pj, ny, blo[1], bhi[1], ax[1])
+                           + ko_at(c, sz, pk, nz, blo[2], bhi[2], ax[2]);
+                }
+                __syncthreads();
+                for (int p = tid; p < P; p += kThreads) {
+                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    const int pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
+                    const double *cx = dxb + ti + ex * ((tj + 3) + bx_y * (tk + 3));
+                    const double *cy = dyb + ti + ex * (tj + ey * (tk + 3));
+                    Sg[p] = cx[0];
+                    Sg[G::PMAX + p] = cy[0];
+                    S2[1 * G::PMAX + p] = d1_at(cx, ex, pj, ny, blo[1], bhi[1], ax[1]);
+                    S2[2 * G::PMAX + p] = d1_at(cx, ex * bx_y, pk, nz, blo[2], bhi[2], ax[2]);
+                    S2[4 * G::PMAX + p] = d1_at(cy, ex * ey, pk, nz, blo[2], bhi[2], ax[2]);
+                }
+            }
+        } else if constexpr (!MIXED) {
             if (q2 < 0) {
                 for (int p = tid; p < P; p += kThreads) {
                     const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
@@ -415,10 +583,29 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
         const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
         const int i = w.o[0] + ti + 3, j = w.o[1] + tj + 3, k = w.o[2] + tk + 3;
         const uint64_t gi = blk.offset + (uint64_t)i + (uint64_t)nx * ((uint64_t)j + (uint64_t)ny * k);
-        const double x = blk.pmin[0] + i * hx;
-        const double y = blk.pmin[1] + j * hy;
-        const double z = blk.pmin[2] + k * hz;
-        const double rr = sqrt(x * x + y * y + z * z);
+        // coordinates and radius with the reference's roundings (rhs.cpp:210-219)
+        const double x = __dadd_rn(blk.pmin[0], __dmul_rn((double)i, hx));
+        const double y = __dadd_rn(blk.pmin[1], __dmul_rn((double)j, hy));
+        const double z = __dadd_rn(blk.pmin[2], __dmul_rn((double)k, hz));
+        const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+        if (bflag != 0 && ((blo[0] && i == 3) || (bhi[0] && i == nx - 4) || (blo[1] && j == 3) ||
+                           (bhi[1] && j == ny - 4) || (blo[2] && k == 3) || (bhi[2] && k == nz - 4))) {
+            // outgoing-radiation condition on a domain face (BSSN_GR/src/rhs.cpp:838-982):
+            // rhs = -(1/r)(x f_x + y f_y + z f_z + falloff (f - asymptotic)),
+            // replacing the algebra at this point, then + sigma * KO as elsewhere
+            const double ninv_r = -__ddiv_rn(1.0, __dsqrt_rn(r2));
+            for (int v = 0; v < NV; v++) {
+                const double f = __ldg(args.u[v] + gi);
+                const double *g = S + (size_t)(3 * v) * G::PMAX + p;
+                double t = __dadd_rn(__dmul_rn(x, g[0]), __dmul_rn(y, g[G::PMAX]));
+                t = __dadd_rn(t, __dmul_rn(z, g[2 * G::PMAX]));
+                t = __dadd_rn(t, __dmul_rn(c_bc_falloff[v], __dsub_rn(f, c_bc_asym[v])));
+                const double ko_sum = S[(size_t)(DGB_NUM_DERIV + v) * G::PMAX + p];
+                args.rhs[v][gi] = __dadd_rn(__dmul_rn(ninv_r, t), __dmul_rn(args.prm.sigma, ko_sum));
+            }
+            continue;
+        }
+        const double rr = __dsqrt_rn(r2);
         double eta = args.prm.eta_const;
         if (rr >= args.prm.eta_r0) {
             const double q = args.prm.eta_r0 / rr;

@@ -139,7 +139,7 @@ extern "C" dgb_status dgb_bssnrhs_block_noalloc(double *const *rhs, const double
         return DGB_ERR_INVALID;
     }
     blk.offset = offset;
-    blk.pad_ = 0;
+    blk.bflag = 0;
     double *ws = nullptr;
     dgb_status s = workspace_on_current_device(&ws);
     if (s != DGB_OK) return s;

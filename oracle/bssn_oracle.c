@@ -66,10 +66,94 @@ static inline double ko_4(const double *u, long s, double pre)
                   - 15.0 * u[s] + 6.0 * u[2 * s] - u[3 * s]);
 }
 
+/* One-sided closures at domain-boundary faces (bflag bit 2*dir: low side,
+ * bit 2*dir+1: high side; OCT_DIR_* in include/dendro.h:84-89), taps listed
+ * in the reference's evaluation order as (index along dir, coefficient).
+ * Low-side indices are absolute (3..8); high-side ones are relative to
+ * ie = n - 3.  First/second derivatives: QuadGrav/src/derivs.cpp:2174-2230
+ * (deriv64_x) and :2602-2650 (deriv64_xx), scaled by (1/h)/12 and
+ * (1/h^2)/12; KO: BSSN_GR/src/derivs.cpp:997-1075, divided by
+ * smr = {49,43,59}/48*64*h. */
+typedef struct { int n; int idx[6]; double c[6]; } orc_taps;
+static const orc_taps D1_LO[3] = {
+    {5, {3, 4, 5, 6, 7}, {-25.0, 48.0, -36.0, 16.0, -3.0}},
+    {5, {3, 4, 5, 6, 7}, {-3.0, -10.0, 18.0, -6.0, 1.0}},
+    {4, {3, 4, 6, 7}, {1.0, -8.0, 8.0, -1.0}}};
+static const orc_taps D1_HI[3] = {
+    {4, {-5, -4, -2, -1}, {1.0, -8.0, 8.0, -1.0}},
+    {5, {-5, -4, -3, -2, -1}, {-1.0, 6.0, -18.0, 10.0, 3.0}},
+    {5, {-5, -4, -3, -2, -1}, {3.0, -16.0, 36.0, -48.0, 25.0}}};
+static const orc_taps D2_LO[3] = {
+    {5, {3, 4, 5, 6, 7}, {35.0, -104.0, 114.0, -56.0, 11.0}},
+    {5, {3, 4, 5, 6, 7}, {11.0, -20.0, 6.0, 4.0, -1.0}},
+    {5, {3, 4, 5, 6, 7}, {-1.0, 16.0, -30.0, 16.0, -1.0}}};
+static const orc_taps D2_HI[3] = {
+    {5, {-5, -4, -3, -2, -1}, {-1.0, 16.0, -30.0, 16.0, -1.0}},
+    {5, {-5, -4, -3, -2, -1}, {-1.0, 4.0, 6.0, -20.0, 11.0}},
+    {5, {-5, -4, -3, -2, -1}, {11.0, -56.0, 114.0, -104.0, 35.0}}};
+static const orc_taps KO_LO[3] = {
+    {4, {6, 5, 4, 3}, {1.0, -3.0, 3.0, -1.0}},
+    {5, {7, 6, 5, 4, 3}, {1.0, -6.0, 12.0, -10.0, 3.0}},
+    {6, {8, 7, 6, 5, 4, 3}, {1.0, -6.0, 15.0, -19.0, 12.0, -3.0}}};
+static const orc_taps KO_HI[3] = {
+    {6, {-6, -5, -4, -3, -2, -1}, {1.0, -6.0, 15.0, -19.0, 12.0, -3.0}},
+    {5, {-5, -4, -3, -2, -1}, {1.0, -6.0, 12.0, -10.0, 3.0}},
+    {4, {-4, -3, -2, -1}, {1.0, -3.0, 3.0, -1.0}}};
+
+/* line = u at index 0 along dir; s = stride; base = 0 (low) or n-3 (high) */
+static double eval_taps(const double *line, long s, int base, const orc_taps *t)
+{
+    double acc = t->c[0] * line[(base + t->idx[0]) * s];
+    for (int q = 1; q < t->n; q++) acc = acc + t->c[q] * line[(base + t->idx[q]) * s];
+    return acc;
+}
+
+enum { ORC_D1 = 0, ORC_D2 = 1, ORC_KO = 2 };
+
+/* Overwrite the three closure points at each flagged end of dir, over the
+ * same (other-axis) ranges as the main loop. */
+static void apply_closures(int kind, int dir, double *D, const double *u, double h,
+                           const unsigned *sz, unsigned bflag, int jb, int je, int kb, int ke)
+{
+    const int nx = sz[0], ny = sz[1], nz = sz[2];
+    const int n = dir == 0 ? nx : dir == 1 ? ny : nz;
+    const long s = dir == 0 ? 1 : dir == 1 ? nx : (long)nx * ny;
+    const int lo = (bflag >> (2 * dir)) & 1u, hi = (bflag >> (2 * dir + 1)) & 1u;
+    if (!lo && !hi) return;
+    const orc_taps *TL = kind == ORC_D1 ? D1_LO : kind == ORC_D2 ? D2_LO : KO_LO;
+    const orc_taps *TH = kind == ORC_D1 ? D1_HI : kind == ORC_D2 ? D2_HI : KO_HI;
+    const double idx_by_12 = (1.0 / h) / 12.0;
+    const double idx_sqrd_by_12 = (1.0 / (h * h)) / 12.0;
+    const double smr[3] = {59.0 / 48.0 * 64 * h, 43.0 / 48.0 * 64 * h, 49.0 / 48.0 * 64 * h};
+    /* (a, b) run over the two other axes with the caller's ranges */
+    for (int b = kb; b < ke; b++)
+        for (int a = jb; a < je; a++) {
+            int i0, j0, k0; /* index of position 0 along dir */
+            if (dir == 0) { i0 = 0; j0 = a; k0 = b; }
+            else if (dir == 1) { i0 = a; j0 = 0; k0 = b; }
+            else { i0 = a; j0 = b; k0 = 0; }
+            const double *line = &u[IX(i0, j0, k0)];
+            double *out = &D[IX(i0, j0, k0)];
+            for (int q = 0; q < 3; q++) {
+                if (lo) {
+                    const double acc = eval_taps(line, s, 0, &TL[q]);
+                    out[(3 + q) * s] = kind == ORC_D1 ? acc * idx_by_12
+                                     : kind == ORC_D2 ? acc * idx_sqrd_by_12 : acc / smr[q];
+                }
+                if (hi) {
+                    const double acc = eval_taps(line, s, n - 3, &TH[q]);
+                    out[(n - 6 + q) * s] = kind == ORC_D1 ? acc * idx_by_12
+                                         : kind == ORC_D2 ? acc * idx_sqrd_by_12 : acc / smr[2 - q];
+                }
+            }
+        }
+}
+
 /* dir 0: i in [3,nx-3), j,k full (derivs.cpp:2151-2156)
  * dir 1: i,j in [3,n-3), k full;  dir 2: interior.  Values outside the
  * computed range are left untouched, as in the reference. */
-void orc_deriv64(int dir, double *D, const double *u, double h, const unsigned *sz)
+void orc_deriv64(int dir, double *D, const double *u, double h, const unsigned *sz,
+                 unsigned bflag)
 {
     const int nx = sz[0], ny = sz[1], nz = sz[2];
     const double c60 = (1.0 / h) / 60.0;
@@ -79,9 +163,14 @@ void orc_deriv64(int dir, double *D, const double *u, double h, const unsigned *
     for (int k = kb; k < ke; k++)
         for (int j = jb; j < je; j++)
             for (int i = 3; i < nx - 3; i++) D[IX(i, j, k)] = d1_6(&u[IX(i, j, k)], s, c60);
+    /* closure loops run over the other two axes with the main loop's ranges */
+    if (dir == 0) apply_closures(ORC_D1, 0, D, u, h, sz, bflag, 0, ny, 0, nz);
+    else if (dir == 1) apply_closures(ORC_D1, 1, D, u, h, sz, bflag, 3, nx - 3, 0, nz);
+    else apply_closures(ORC_D1, 2, D, u, h, sz, bflag, 3, nx - 3, 3, ny - 3);
 }
 
-void orc_deriv64_2(int dir, double *D, const double *u, double h, const unsigned *sz)
+void orc_deriv64_2(int dir, double *D, const double *u, double h, const unsigned *sz,
+                   unsigned bflag)
 {
     const int nx = sz[0], ny = sz[1], nz = sz[2];
     const double c180 = (1.0 / (h * h)) / 180.0;
@@ -89,9 +178,12 @@ void orc_deriv64_2(int dir, double *D, const double *u, double h, const unsigned
     for (int k = 3; k < nz - 3; k++)
         for (int j = 3; j < ny - 3; j++)
             for (int i = 3; i < nx - 3; i++) D[IX(i, j, k)] = d2_6(&u[IX(i, j, k)], s, c180);
+    if (dir == 0) apply_closures(ORC_D2, 0, D, u, h, sz, bflag, 3, ny - 3, 3, nz - 3);
+    else if (dir == 1) apply_closures(ORC_D2, 1, D, u, h, sz, bflag, 3, nx - 3, 3, nz - 3);
+    else apply_closures(ORC_D2, 2, D, u, h, sz, bflag, 3, nx - 3, 3, ny - 3);
 }
 
-void orc_ko42(int dir, double *D, const double *u, double h, const unsigned *sz)
+void orc_ko42(int dir, double *D, const double *u, double h, const unsigned *sz, unsigned bflag)
 {
     const int nx = sz[0], ny = sz[1], nz = sz[2];
     const double pre = -1.0 / 64.0 / h;
@@ -99,6 +191,40 @@ void orc_ko42(int dir, double *D, const double *u, double h, const unsigned *sz)
     for (int k = 3; k < nz - 3; k++)
         for (int j = 3; j < ny - 3; j++)
             for (int i = 3; i < nx - 3; i++) D[IX(i, j, k)] = ko_4(&u[IX(i, j, k)], s, pre);
+    if (dir == 0) apply_closures(ORC_KO, 0, D, u, h, sz, bflag, 3, ny - 3, 3, nz - 3);
+    else if (dir == 1) apply_closures(ORC_KO, 1, D, u, h, sz, bflag, 3, nx - 3, 3, nz - 3);
+    else apply_closures(ORC_KO, 2, D, u, h, sz, bflag, 3, nx - 3, 3, ny - 3);
+}
+
+/* Outgoing-radiation condition on the flagged faces' boundary layer
+ * (BSSN_GR/src/rhs.cpp:838-982):
+ * rhs = -(1/r) (x f_x + y f_y + z f_z + falloff (f - asymptotic)). */
+static void orc_bssn_bcs(double *f_rhs, const double *f, const double *dxf, const double *dyf,
+                         const double *dzf, const double *pmin, const double *pmax,
+                         double falloff, double asym, const unsigned *sz, unsigned bflag)
+{
+    const int nx = sz[0], ny = sz[1], nz = sz[2];
+    const double hx = (pmax[0] - pmin[0]) / (nx - 1), hy = (pmax[1] - pmin[1]) / (ny - 1),
+                 hz = (pmax[2] - pmin[2]) / (nz - 1);
+    const int ib = 3, jb = 3, kb = 3, ie = nx - 3, je = ny - 3, ke = nz - 3;
+    for (int face = 0; face < 6; face++) {
+        if (!(bflag & (1u << face))) continue;
+        const int dir = face / 2, hi = face & 1;
+        const int fixed = dir == 0 ? (hi ? ie - 1 : ib) : dir == 1 ? (hi ? je - 1 : jb) : (hi ? ke - 1 : kb);
+        const int na = dir == 0 ? jb : ib, ea = dir == 0 ? je : ie;   /* first free axis */
+        const int nb = dir == 2 ? jb : kb, eb = dir == 2 ? je : ke;   /* second free axis */
+        for (int b = nb; b < eb; b++)
+            for (int a = na; a < ea; a++) {
+                const int i = dir == 0 ? fixed : a;
+                const int j = dir == 1 ? fixed : (dir == 0 ? a : b);
+                const int k = dir == 2 ? fixed : b;
+                const double x = pmin[0] + i * hx, y = pmin[1] + j * hy, z = pmin[2] + k * hz;
+                const size_t pp = IX(i, j, k);
+                const double inv_r = 1.0 / sqrt(x * x + y * y + z * z);
+                f_rhs[pp] = -inv_r * (x * dxf[pp] + y * dyf[pp] + z * dzf[pp]
+                                      + falloff * (f[pp] - asym));
+            }
+    }
 }
 
 /* ---------------- point algebra (CodeGen/bssn.py, dendro.py) ---------------- */
@@ -316,11 +442,20 @@ static const int HAS_D2[NV] = {1, 1, 0, 0, 0, 0, 1, 1, 1, 0, 0, 0,
 
 /* Returns 0 on success, -1 for a domain-boundary block, -2 on allocation
  * failure.  Writes only interior points of each rhs[v] + offset. */
-int orc_bssnrhs(double **rhs, const double **uz, unsigned long offset,
-                const double *pmin, const double *pmax, const unsigned *sz,
-                unsigned bflag, const double *prm)
+/* bssn_bcs falloff / asymptotic value per variable, VAR order
+ * (BSSN_GR/src/rhs.cpp:269-321). */
+static const double BC_FALLOFF[NV] = {1, 1, 1, 2, 2, 2, 1, 1, 1, 1, 1, 1,
+                                      1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2};
+static const double BC_ASYM[NV] = {1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+                                   1, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0, 0};
+
+/* apply_bcs = 0 skips bssn_bcs (used to pin the closures alone against the
+ * reference harness, which cannot compile bssn_bcs). */
+int orc_bssnrhs_ex(double **rhs, const double **uz, unsigned long offset,
+                   const double *pmin, const double *pmax, const unsigned *sz,
+                   unsigned bflag, const double *prm, int apply_bcs)
 {
-    if (bflag != 0) return -1;
+    if (bflag != 0 && (sz[0] < 13 || sz[1] < 13 || sz[2] < 13)) return -1;
     const int nx = sz[0], ny = sz[1], nz = sz[2];
     const size_t n = (size_t)nx * ny * nz;
     const double h[3] = {(pmax[0] - pmin[0]) / (nx - 1), (pmax[1] - pmin[1]) / (ny - 1),
@@ -337,14 +472,14 @@ int orc_bssnrhs(double **rhs, const double **uz, unsigned long offset,
     }
     for (int v = 0; v < NV; v++) {
         const double *u = uz[v] + offset;
-        for (int d = 0; d < 3; d++) orc_deriv64(d, grad[v][d], u, h[d], sz);
+        for (int d = 0; d < 3; d++) orc_deriv64(d, grad[v][d], u, h[d], sz, bflag);
         if (HAS_D2[v]) {
-            orc_deriv64_2(0, grad2[v][0], u, h[0], sz);
-            orc_deriv64_2(1, grad2[v][3], u, h[1], sz);
-            orc_deriv64_2(2, grad2[v][5], u, h[2], sz);
-            orc_deriv64(1, grad2[v][1], grad[v][0], h[1], sz); /* d_y(d_x u) */
-            orc_deriv64(2, grad2[v][2], grad[v][0], h[2], sz); /* d_z(d_x u) */
-            orc_deriv64(2, grad2[v][4], grad[v][1], h[2], sz); /* d_z(d_y u) */
+            orc_deriv64_2(0, grad2[v][0], u, h[0], sz, bflag);
+            orc_deriv64_2(1, grad2[v][3], u, h[1], sz, bflag);
+            orc_deriv64_2(2, grad2[v][5], u, h[2], sz, bflag);
+            orc_deriv64(1, grad2[v][1], grad[v][0], h[1], sz, bflag); /* d_y(d_x u) */
+            orc_deriv64(2, grad2[v][2], grad[v][0], h[2], sz, bflag); /* d_z(d_x u) */
+            orc_deriv64(2, grad2[v][4], grad[v][1], h[2], sz, bflag); /* d_z(d_y u) */
         }
     }
     static const int Q[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
@@ -401,11 +536,15 @@ int orc_bssnrhs(double **rhs, const double **uz, unsigned long offset,
             }
         }
     }
+    if (bflag != 0 && apply_bcs)
+        for (int v = 0; v < NV; v++)
+            orc_bssn_bcs(rhs[v] + offset, uz[v] + offset, grad[v][0], grad[v][1], grad[v][2],
+                         pmin, pmax, BC_FALLOFF[v], BC_ASYM[v], sz, bflag);
     /* KO dissipation reuses the first-derivative scratch (bssnrhs_ko_derivs.h) */
     const double sigma = prm[9];
     for (int v = 0; v < NV; v++) {
         const double *u = uz[v] + offset;
-        for (int d = 0; d < 3; d++) orc_ko42(d, grad[v][d], u, h[d], sz);
+        for (int d = 0; d < 3; d++) orc_ko42(d, grad[v][d], u, h[d], sz, bflag);
         double *o = rhs[v] + offset;
         for (int k = 3; k < nz - 3; k++)
             for (int j = 3; j < ny - 3; j++)
@@ -416,6 +555,12 @@ int orc_bssnrhs(double **rhs, const double **uz, unsigned long offset,
     }
     free(pool);
     return 0;
+}
+
+int orc_bssnrhs(double **rhs, const double **uz, unsigned long offset, const double *pmin,
+                const double *pmax, const unsigned *sz, unsigned bflag, const double *prm)
+{
+    return orc_bssnrhs_ex(rhs, uz, offset, pmin, pmax, sz, bflag, prm, 1);
 }
 
 /* bssnRHS over a block list (BSSN_GR/src/rhs.cpp:9-76), OpenMP over blocks

@@ -43,6 +43,9 @@ class Oracle:
         L = C.CDLL(path)
         L.orc_bssnrhs.restype = C.c_int
         L.orc_bssnrhs.argtypes = [_PP, _PP, C.c_ulong, _D, _D, C.POINTER(C.c_uint), C.c_uint, _D]
+        L.orc_bssnrhs_ex.restype = C.c_int
+        L.orc_bssnrhs_ex.argtypes = [_PP, _PP, C.c_ulong, _D, _D, C.POINTER(C.c_uint), C.c_uint,
+                                     _D, C.c_int]
         L.orc_bssnrhs_blocks.restype = C.c_int
         L.orc_bssnrhs_blocks.argtypes = [_PP, _PP, C.c_long, C.POINTER(C.c_ulong),
                                          C.POINTER(C.c_uint), C.POINTER(C.c_uint), _D, _D, _D,
@@ -55,7 +58,7 @@ class Oracle:
         for nm in ("orc_deriv64", "orc_deriv64_2", "orc_ko42"):
             f = getattr(L, nm)
             f.restype = None
-            f.argtypes = [C.c_int, _D, _D, C.c_double, C.POINTER(C.c_uint)]
+            f.argtypes = [C.c_int, _D, _D, C.c_double, C.POINTER(C.c_uint), C.c_uint]
         self.L = L
 
     def bssnrhs_blocks(self, rhs, u, blocks, prm, nthreads=0):
@@ -72,15 +75,26 @@ class Oracle:
         return self.L.orc_bssnrhs_blocks(r, uu, n, off, sz, bf, pmin.ctypes.data_as(_D),
                                          pmax.ctypes.data_as(_D), p.ctypes.data_as(_D), nthreads)
 
-    def stencil(self, kind, dirn, u3, h):
+    def stencil(self, kind, dirn, u3, h, bflag=0):
         """kind in {'d1','d2','ko'} on a 3-D array u3[z][y][x]; returns D (zeros
         where the reference leaves the output untouched)."""
         fn = {"d1": self.L.orc_deriv64, "d2": self.L.orc_deriv64_2, "ko": self.L.orc_ko42}[kind]
         u = np.ascontiguousarray(u3, dtype=np.float64)
         D = np.zeros_like(u)
         sz = (C.c_uint * 3)(u.shape[2], u.shape[1], u.shape[0])
-        fn(dirn, D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz)
+        fn(dirn, D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz, bflag)
         return D
+
+    def bssnrhs_block(self, rhs, u, block, prm, apply_bcs=True):
+        r, k1 = _ptrs(rhs)
+        uu, k2 = _ptrs(u)
+        pmin = np.array(list(block.ptmin), dtype=np.float64)
+        pmax = np.array(list(block.ptmax), dtype=np.float64)
+        sz = (C.c_uint * 3)(*block.sz)
+        p = np.ascontiguousarray(prm, dtype=np.float64)
+        return self.L.orc_bssnrhs_ex(r, uu, block.offset, pmin.ctypes.data_as(_D),
+                                     pmax.ctypes.data_as(_D), sz, block.bflag,
+                                     p.ctypes.data_as(_D), 1 if apply_bcs else 0)
 
     def rk4_stage(self, s, dst, prev, k, dt, chi_floor):
         n = dst[0].size
@@ -113,7 +127,7 @@ class Reference:
                    "ref_ko_deriv42_z"):
             f = getattr(L, nm)
             f.restype = None
-            f.argtypes = [_D, _D, C.c_double, C.POINTER(C.c_uint)]
+            f.argtypes = [_D, _D, C.c_double, C.POINTER(C.c_uint), C.c_uint]
         self.L = L
 
     def bssnrhs(self, rhs, u, block, prm):
@@ -126,14 +140,14 @@ class Reference:
         return self.L.ref_bssnrhs(r, uu, block.offset, pmin.ctypes.data_as(_D),
                                   pmax.ctypes.data_as(_D), sz, block.bflag, p.ctypes.data_as(_D))
 
-    def stencil(self, kind, dirn, u3, h):
+    def stencil(self, kind, dirn, u3, h, bflag=0):
         nm = {"d1": ["ref_deriv64_x", "ref_deriv64_y", "ref_deriv64_z"],
               "d2": ["ref_deriv64_xx", "ref_deriv64_yy", "ref_deriv64_zz"],
               "ko": ["ref_ko_deriv42_x", "ref_ko_deriv42_y", "ref_ko_deriv42_z"]}[kind][dirn]
         u = np.ascontiguousarray(u3, dtype=np.float64)
         D = np.zeros_like(u)
         sz = (C.c_uint * 3)(u.shape[2], u.shape[1], u.shape[0])
-        getattr(self.L, nm)(D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz)
+        getattr(self.L, nm)(D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz, bflag)
         return D
 
     def enforce(self, fields, node, chi_floor):

@@ -11,8 +11,10 @@
  * the KO accumulate loop (rhs.cpp:328-373).  The stencils are bound to the
  * 6th-order family through QuadGrav/include/derivs.h
  * (QUADGRAV_USE_6TH_ORDER_DERIVS), i.e. QuadGrav/src/derivs.cpp.
- * Domain-boundary blocks (bflag != 0) are rejected: bssn_bcs lives in a
- * translation unit that needs the mesh and MPI.
+ * Domain-boundary blocks (bflag != 0) get the reference's one-sided
+ * closures (they live in derivs.cpp) but NOT bssn_bcs, which lives in a
+ * translation unit that needs the mesh and MPI; callers compare against a
+ * restatement run without the boundary condition.
  */
 #include <cmath>
 #include <cstdlib>
@@ -32,7 +34,6 @@ extern "C" int ref_bssnrhs(double **unzipVarsRHS, const double **uZipVars,
                            const double *pmax, const unsigned int *sz,
                            unsigned int bflag, const double *prm)
 {
-    if (bflag != 0) return -1;
     const unsigned int lambda[4] = {(unsigned)prm[0], (unsigned)prm[1],
                                     (unsigned)prm[2], (unsigned)prm[3]};
     const double lambda_f[2] = {prm[4], prm[5]};
@@ -128,13 +129,17 @@ extern "C" void ref_enforce_bssn_constraints(double **uiVar, unsigned int node, 
     enforce_bssn_constraints(uiVar, node);
 }
 
-/* The reference stencils themselves, exported for per-stencil pins. */
-extern "C" void ref_deriv64_x(double *D, const double *u, double h, const unsigned *sz) { deriv64_x(D, u, h, sz, 0); }
-extern "C" void ref_deriv64_y(double *D, const double *u, double h, const unsigned *sz) { deriv64_y(D, u, h, sz, 0); }
-extern "C" void ref_deriv64_z(double *D, const double *u, double h, const unsigned *sz) { deriv64_z(D, u, h, sz, 0); }
-extern "C" void ref_deriv64_xx(double *D, const double *u, double h, const unsigned *sz) { deriv64_xx(D, u, h, sz, 0); }
-extern "C" void ref_deriv64_yy(double *D, const double *u, double h, const unsigned *sz) { deriv64_yy(D, u, h, sz, 0); }
-extern "C" void ref_deriv64_zz(double *D, const double *u, double h, const unsigned *sz) { deriv64_zz(D, u, h, sz, 0); }
-extern "C" void ref_ko_deriv42_x(double *D, const double *u, double h, const unsigned *sz) { ko_deriv42_x(D, u, h, sz, 0); }
-extern "C" void ref_ko_deriv42_y(double *D, const double *u, double h, const unsigned *sz) { ko_deriv42_y(D, u, h, sz, 0); }
-extern "C" void ref_ko_deriv42_z(double *D, const double *u, double h, const unsigned *sz) { ko_deriv42_z(D, u, h, sz, 0); }
+/* The reference stencils themselves (with their boundary closures when
+ * bflag is set), exported for per-stencil pins. */
+#define REF_STENCIL(name, fn) \
+    extern "C" void name(double *D, const double *u, double h, const unsigned *sz, unsigned bflag) \
+    { fn(D, u, h, sz, bflag); }
+REF_STENCIL(ref_deriv64_x, deriv64_x)
+REF_STENCIL(ref_deriv64_y, deriv64_y)
+REF_STENCIL(ref_deriv64_z, deriv64_z)
+REF_STENCIL(ref_deriv64_xx, deriv64_xx)
+REF_STENCIL(ref_deriv64_yy, deriv64_yy)
+REF_STENCIL(ref_deriv64_zz, deriv64_zz)
+REF_STENCIL(ref_ko_deriv42_x, ko_deriv42_x)
+REF_STENCIL(ref_ko_deriv42_y, ko_deriv42_y)
+REF_STENCIL(ref_ko_deriv42_z, ko_deriv42_z)

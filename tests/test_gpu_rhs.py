@@ -167,3 +167,27 @@ def test_rk4_stage_matches_oracle(dgb, gpu, oracle):
 def test_exact_mul_device_matches_dmul(dgb, gpu):
     """The integer-pipe tap products equal DMUL bit for bit on the device."""
     assert dgb.selftest_exact_mul(1, 1 << 24, seed=3) == 0
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_rhs_boundary_blocks_match_oracle(dgb, gpu, oracle, precision):
+    """Domain-boundary blocks (bflag != 0): one-sided closures and the
+    outgoing-radiation condition, with the padding beyond the flagged faces
+    left as NaN as an unzip leaves it.  Boundary blocks take the FP64 path in
+    both precisions."""
+    from test_oracle import boundary_blocks, poison_outside
+    torch = gpu
+    blocks = boundary_blocks(dgb)
+    u = host_fields(dgb, blocks, SEED1)
+    poison_outside(blocks, u)
+    plan = dgb.Plan(blocks, dgb.default_params(0.1))
+    got = run_device(dgb, torch, plan, u, precision=precision)
+    want = oracle_rhs(dgb, oracle, blocks, u, 0.1)
+    bmask = np.zeros(len(u[0]), dtype=bool)
+    full = interior_mask(blocks, len(u[0]))
+    for b in blocks:
+        if b.bflag:
+            bmask[b.offset:b.offset + 13 ** 3] = True
+    mask = full & bmask
+    err = normwise(got, want, mask)
+    assert np.all(err <= FP64_TOL), dict(zip(dgb.VAR_NAMES, err))

@@ -118,3 +118,73 @@ def test_oracle_matches_reference_code(dgb, oracle, reference):
             assert reference.bssnrhs(r2, u, b, prm) == 0
         err = normwise(r1, r2, interior_mask(blocks, n))
         assert err.max() <= 1e-13, dict(zip(dgb.VAR_NAMES, err))
+
+
+def boundary_blocks(dgb):
+    """13^3 blocks of the uniform workload flagged as domain-boundary blocks
+    (every face combination class: single faces, edges, corners, opposite
+    faces), laid out contiguously."""
+    allb = dgb.synth_blocks(1)
+    picks = [(0, 1 | 4 | 16), (7, 2), (63, 2 | 8), (511, 2 | 8 | 32), (300, 4), (301, 48),
+             (302, 3), (292, 0)]
+    rows, off = [], 0
+    for i, f in picks:
+        b = allb[i]
+        rows.append((off, tuple(b.sz), f, tuple(b.ptmin), tuple(b.ptmax)))
+        off += 13 ** 3
+    return dgb.blocks_array(rows)
+
+
+def poison_outside(blocks, u):
+    """NaN in the padding beyond each flagged face: a mesh leaves it unfilled."""
+    for b in blocks:
+        nx, ny, nz = b.sz
+        for v in range(24):
+            a = u[v][b.offset:b.offset + nx * ny * nz].reshape(nz, ny, nx)
+            if b.bflag & 1: a[:, :, :3] = np.nan
+            if b.bflag & 2: a[:, :, nx - 3:] = np.nan
+            if b.bflag & 4: a[:, :3, :] = np.nan
+            if b.bflag & 8: a[:, ny - 3:, :] = np.nan
+            if b.bflag & 16: a[:3, :, :] = np.nan
+            if b.bflag & 32: a[nz - 3:, :, :] = np.nan
+
+
+@pytest.mark.parametrize("kind", ["d1", "d2", "ko"])
+def test_oracle_boundary_closures_bit_exact(oracle, reference, kind):
+    """One-sided closures for every flag combination equal the reference's."""
+    rng = np.random.default_rng(0)
+    u3 = rng.normal(size=(17, 19, 21))
+    for bflag in range(64):
+        for d in range(3):
+            a = oracle.stencil(kind, d, u3, 0.1, bflag)
+            b = reference.stencil(kind, d, u3, 0.1, bflag)
+            assert np.array_equal(a, b), (kind, d, bflag)
+
+
+def test_oracle_boundary_rhs_matches_reference(dgb, oracle, reference):
+    """Boundary blocks: closures in the derivatives, the mixed compositions and
+    KO agree with the reference harness (which cannot apply bssn_bcs, so both
+    run without it here)."""
+    blocks = boundary_blocks(dgb)
+    u = host_fields(dgb, blocks, SEED1)
+    prm = dgb.params_vector(dgb.default_params(0.1))
+    n = len(u[0])
+    r1 = [np.zeros(n) for _ in range(24)]
+    r2 = [np.zeros(n) for _ in range(24)]
+    for b in blocks:
+        assert oracle.bssnrhs_block(r1, u, b, prm, apply_bcs=False) == 0
+        assert reference.bssnrhs(r2, u, b, prm) == 0
+    err = normwise(r1, r2, interior_mask(blocks, n))
+    assert err.max() <= 1e-13, dict(zip(dgb.VAR_NAMES, err))
+
+
+def test_oracle_boundary_ignores_unfilled_padding(dgb, oracle):
+    blocks = boundary_blocks(dgb)
+    u = host_fields(dgb, blocks, SEED1)
+    poison_outside(blocks, u)
+    prm = dgb.params_vector(dgb.default_params(0.1))
+    n = len(u[0])
+    r = [np.zeros(n) for _ in range(24)]
+    assert oracle.bssnrhs_blocks(r, u, blocks, prm) == 0
+    mask = interior_mask(blocks, n)
+    assert all(np.isfinite(x[mask]).all() for x in r)
