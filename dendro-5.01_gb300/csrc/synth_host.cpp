@@ -148,3 +148,24 @@ extern "C" dgb_status dgb_synth_fill_host(const dgb_block_desc *blocks, size_t n
     (void)nthreads;
     return DGB_OK;
 }
+
+extern "C" dgb_status dgb_synth_fill_points_host(const double *xyz, uint64_t n, double *const *u,
+                                                 uint64_t seed, double noise, int nthreads)
+{
+    if ((!xyz && n) || !u) return DGB_ERR_INVALID;
+    for (int v = 0; v < DGB_NUM_VARS; v++)
+        if (!u[v]) return DGB_ERR_INVALID;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(static)
+#endif
+    for (long long p = 0; p < (long long)n; p++) {
+        const double x = xyz[3 * p], y = xyz[3 * p + 1], z = xyz[3 * p + 2];
+        for (int v = 0; v < DGB_NUM_VARS; v++) {
+            const uint64_t key = dgb_noise_key(seed, (uint64_t)p, (uint32_t)v);
+            u[v][p] = SY_ADD(dgb_bl_value(v, x, y, z), SY_MUL(noise, dgb_noise_unit(key, 0)));
+        }
+    }
+    (void)nthreads;
+    return DGB_OK;
+}

@@ -95,6 +95,25 @@ _SIGS = {
                                         C.c_void_p]),
     "dgb_synth_blocks": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(BlockDesc),
                                    C.POINTER(C.c_size_t)]),
+    "dgb_mesh_create": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "dgb_mesh_destroy": (C.c_int, [C.c_void_p]),
+    "dgb_mesh_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "dgb_mesh_blocks": (C.c_int, [C.c_void_p, C.POINTER(BlockDesc)]),
+    "dgb_mesh_dof_coords": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "dgb_mesh_leaf_levels": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "dgb_mesh_unzip_operator": (C.c_int, [C.c_void_p] + [C.c_void_p] * 6),
+    "dgb_unzip_plan_create": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint64,
+                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.POINTER(C.c_void_p)]),
+    "dgb_unzip_plan_destroy": (C.c_int, [C.c_void_p]),
+    "dgb_unzip": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
+    "dgb_zip": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
+    "dgb_stepper_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "dgb_stepper_destroy": (C.c_int, [C.c_void_p]),
+    "dgb_rk4_step": (C.c_int, [C.c_void_p, PtrArr, C.c_double, C.c_double, C.c_int,
+                               C.c_void_p]),
+    "dgb_synth_fill_points_host": (C.c_int, [C.c_void_p, C.c_uint64, PtrArr, C.c_uint64,
+                                             C.c_double, C.c_int]),
     "dgb_measure_fp64_peak": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "dgb_selftest_exact_mul": (C.c_int, [C.c_int, C.c_uint64, C.c_uint64,
                                          C.POINTER(C.c_uint64)]),
@@ -245,3 +264,136 @@ def rk4_stage(stage, dst_ptrs, prev_ptrs, k_ptrs, nnodes, dt, chi_floor=1e-4, st
     kk, k3 = ptr_array(k_ptrs)
     check(lib().dgb_rk4_stage(stage, d, p, kk, nnodes, dt, chi_floor, C.c_void_p(stream)),
           "dgb_rk4_stage")
+
+
+# ----------------------------------------------------------------------------- mesh
+class MeshParams(C.Structure):
+    _fields_ = [("domain_min", C.c_double * 3), ("domain_max", C.c_double * 3),
+                ("max_level", C.c_int), ("min_level", C.c_int), ("ele_order", C.c_int),
+                ("num_punctures", C.c_int), ("puncture", (C.c_double * 3) * 4),
+                ("fine_radius", C.c_double), ("max_block_refine", C.c_int)]
+
+
+def mesh_params(max_level=10, min_level=4, fine_radius=1.0, domain=32.0, max_block_refine=3,
+                punctures=((1.0, 0.0, 0.00123), (-1.0, 0.0, 0.00123))):
+    """Two-puncture octree on [-domain, domain]^3 (Brill-Lindquist masses at
+    (+-1, 0, 0.00123))."""
+    p = MeshParams()
+    p.domain_min[:] = [-domain] * 3
+    p.domain_max[:] = [domain] * 3
+    p.max_level, p.min_level, p.ele_order = max_level, min_level, 6
+    p.num_punctures = len(punctures)
+    for i, c in enumerate(punctures):
+        p.puncture[i][:] = list(c)
+    p.fine_radius = fine_radius
+    p.max_block_refine = max_block_refine
+    return p
+
+
+class Mesh:
+    """Host octree mesh and its unzip / zip operators (numpy arrays)."""
+
+    def __init__(self, params):
+        h = C.c_void_p()
+        check(lib().dgb_mesh_create(C.byref(params), C.byref(h)), "dgb_mesh_create")
+        self.h = h
+        s = (C.c_uint64 * 6)()
+        check(lib().dgb_mesh_sizes(h, s), "dgb_mesh_sizes")
+        (self.num_leaves, self.ndof, self.nblocks, self.nunzipped, self.ninterp,
+         self.nnz) = [int(x) for x in s]
+        self.blocks = (BlockDesc * self.nblocks)()
+        check(lib().dgb_mesh_blocks(h, self.blocks), "dgb_mesh_blocks")
+
+    def dof_coords(self):
+        xyz = np.zeros((self.ndof, 3))
+        check(lib().dgb_mesh_dof_coords(self.h, xyz.ctypes.data), "dgb_mesh_dof_coords")
+        return xyz
+
+    def leaves(self):
+        lev = np.zeros(self.num_leaves, dtype=np.uint8)
+        anc = np.zeros((self.num_leaves, 3), dtype=np.uint32)
+        check(lib().dgb_mesh_leaf_levels(self.h, lev.ctypes.data, anc.ctypes.data),
+              "dgb_mesh_leaf_levels")
+        return lev, anc
+
+    def operator(self):
+        cp = np.zeros(self.nunzipped, dtype=np.uint32)
+        idst = np.zeros(self.ninterp, dtype=np.uint64)
+        iptr = np.zeros(self.ninterp + 1, dtype=np.uint64)
+        icol = np.zeros(self.nnz, dtype=np.uint32)
+        iw = np.zeros(self.nnz)
+        zs = np.zeros(self.ndof, dtype=np.uint64)
+        check(lib().dgb_mesh_unzip_operator(self.h, cp.ctypes.data, idst.ctypes.data,
+                                            iptr.ctypes.data, icol.ctypes.data, iw.ctypes.data,
+                                            zs.ctypes.data), "dgb_mesh_unzip_operator")
+        return {"copy_src": cp, "interp_dst": idst, "interp_ptr": iptr, "interp_col": icol,
+                "interp_w": iw, "zip_src": zs}
+
+    def close(self):
+        if self.h:
+            lib().dgb_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+SENTINEL = 0xFFFFFFFF
+
+
+def synth_fill_points(xyz, fields, seed, noise=1e-6, nthreads=0):
+    pa, keep = host_ptrs(fields)
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    check(lib().dgb_synth_fill_points_host(xyz.ctypes.data, len(xyz), pa, seed, noise, nthreads),
+          "dgb_synth_fill_points_host")
+
+
+class UnzipPlan:
+    def __init__(self, op, ndof):
+        h = C.c_void_p()
+        n = len(op["copy_src"])
+        ni = len(op["interp_dst"])
+        check(lib().dgb_unzip_plan_create(ndof, n, op["copy_src"].ctypes.data, ni,
+                                          op["interp_dst"].ctypes.data,
+                                          op["interp_ptr"].ctypes.data,
+                                          op["interp_col"].ctypes.data,
+                                          op["interp_w"].ctypes.data, op["zip_src"].ctypes.data,
+                                          C.byref(h)), "dgb_unzip_plan_create")
+        self.h = h
+
+    def unzip(self, zipped_ptrs, unzipped_ptrs, stream=0):
+        z, k1 = ptr_array(zipped_ptrs)
+        u, k2 = ptr_array(unzipped_ptrs)
+        check(lib().dgb_unzip(self.h, z, u, len(zipped_ptrs), C.c_void_p(stream)), "dgb_unzip")
+
+    def zip(self, unzipped_ptrs, zipped_ptrs, stream=0):
+        u, k1 = ptr_array(unzipped_ptrs)
+        z, k2 = ptr_array(zipped_ptrs)
+        check(lib().dgb_zip(self.h, u, z, len(zipped_ptrs), C.c_void_p(stream)), "dgb_zip")
+
+    def close(self):
+        if self.h:
+            lib().dgb_unzip_plan_destroy(self.h)
+            self.h = None
+
+
+class Stepper:
+    def __init__(self, plan, uz, precision=PREC_FP64):
+        h = C.c_void_p()
+        check(lib().dgb_stepper_create(plan.h, uz.h, precision, C.byref(h)),
+              "dgb_stepper_create")
+        self.h = h
+        self._keep = (plan, uz)
+
+    def step(self, state_ptrs, dt, nsteps=1, chi_floor=1e-4, stream=0):
+        s, k = ptr_array(state_ptrs)
+        check(lib().dgb_rk4_step(self.h, s, dt, chi_floor, nsteps, C.c_void_p(stream)),
+              "dgb_rk4_step")
+
+    def close(self):
+        if self.h:
+            lib().dgb_stepper_destroy(self.h)
+            self.h = None

@@ -159,6 +159,79 @@ dgb_status dgb_synth_fill_device(dgb_plan *plan, double *const *u, uint64_t seed
  * get the count. */
 dgb_status dgb_synth_blocks(int which, uint64_t seed, dgb_block_desc *blocks, size_t *nblk);
 
+/* ------------------------------------------------------------------------
+ * Octree mesh, unzip / zip and the full RK4 step
+ * ------------------------------------------------------------------------ */
+
+/* Synthetic 2:1-balanced octree on a cubic domain, refined to max_level
+ * within fine_radius of each puncture and one level coarser per doubling of
+ * the distance, down to min_level; leaves merged into blocks of up to
+ * 2^max_block_refine leaves per side.  Host-side; replaces the mesh the
+ * reference builds in ot::Mesh (src/mesh.cpp:283, :8640-8790). */
+typedef struct {
+    double domain_min[3], domain_max[3];
+    int max_level, min_level, ele_order; /* ele_order must be 6 */
+    int num_punctures;
+    double puncture[4][3];
+    double fine_radius;
+    int max_block_refine; /* 0..3 */
+} dgb_mesh_params;
+typedef struct dgb_mesh dgb_mesh;
+dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **mesh);
+dgb_status dgb_mesh_destroy(dgb_mesh *mesh);
+/* sizes[0..5]: leaves, independent nodes (zipped length), blocks, padded
+ * points (unzipped length), interpolation rows, interpolation terms. */
+dgb_status dgb_mesh_sizes(const dgb_mesh *mesh, uint64_t *sizes);
+dgb_status dgb_mesh_blocks(const dgb_mesh *mesh, dgb_block_desc *blocks);
+dgb_status dgb_mesh_dof_coords(const dgb_mesh *mesh, double *xyz);
+dgb_status dgb_mesh_leaf_levels(const dgb_mesh *mesh, uint8_t *level, uint32_t *anchor);
+/* The mesh's unzip / zip operators in the generic form dgb_unzip_plan_create
+ * takes (array lengths from dgb_mesh_sizes). */
+dgb_status dgb_mesh_unzip_operator(const dgb_mesh *mesh, uint32_t *copy_src, uint64_t *interp_dst,
+                                   uint64_t *interp_ptr, uint32_t *interp_col, double *interp_w,
+                                   uint64_t *zip_src);
+
+/* Device unzip / zip for any mesh, from the operator: padded point p copies
+ * zipped node copy_src[p] (0xFFFFFFFF: not written), or, for the rows listed
+ * in interp_dst, takes sum_t interp_w[t] * zipped[interp_col[t]] over the
+ * CSR row interp_ptr[r]..interp_ptr[r+1]; zipped node d reads padded point
+ * zip_src[d].  A host maintainer builds the operator once per mesh from
+ * ot::Mesh's maps. */
+typedef struct dgb_unzip_plan dgb_unzip_plan;
+dgb_status dgb_unzip_plan_create(uint64_t ndof, uint64_t unzipped_size, const uint32_t *copy_src,
+                                 uint64_t ninterp, const uint64_t *interp_dst,
+                                 const uint64_t *interp_ptr, const uint32_t *interp_col,
+                                 const double *interp_w, const uint64_t *zip_src,
+                                 dgb_unzip_plan **plan);
+dgb_status dgb_unzip_plan_destroy(dgb_unzip_plan *plan);
+/* Replaces ot::Mesh::unzip(const T* in, T* out, unsigned dof) for nvars
+ * fields (include/mesh.h:1697, include/mesh.tcc:7436-8690), device arrays. */
+dgb_status dgb_unzip(dgb_unzip_plan *plan, const double *const *zipped, double *const *unzipped,
+                     int nvars, void *stream);
+/* Replaces ot::Mesh::zip(const T* unzipped, T* zipped) (include/mesh.h:1740,
+ * include/mesh.tcc:3775-3822), device arrays. */
+dgb_status dgb_zip(dgb_unzip_plan *plan, const double *const *unzipped, double *const *zipped,
+                   int nvars, void *stream);
+
+/* Full RK4 step on the zipped state (24 device arrays of the plan's ndof),
+ * in place: for each stage, unzip -> bssnRHS (+KO, boundary conditions) ->
+ * zip -> stage update with the constraint closure; the four stages of one
+ * step are one CUDA graph, captured on the first call and replayed.
+ * Replaces RK_BSSN::performSingleIteration's RK4 branch
+ * (BSSN_GR/src/rkBSSN.cpp:603-1012).  The stepper owns the unzipped and
+ * stage buffers. */
+typedef struct dgb_stepper dgb_stepper;
+dgb_status dgb_stepper_create(dgb_plan *rhs_plan, dgb_unzip_plan *uz, int precision,
+                              dgb_stepper **stepper);
+dgb_status dgb_stepper_destroy(dgb_stepper *stepper);
+dgb_status dgb_rk4_step(dgb_stepper *stepper, double *const *state, double dt, double chi_floor,
+                        int nsteps, void *stream);
+
+/* Seeded Brill-Lindquist + noise at arbitrary points (zipped vectors);
+ * noise keyed by (seed, point index, variable). */
+dgb_status dgb_synth_fill_points_host(const double *xyz, uint64_t n, double *const *u,
+                                      uint64_t seed, double noise, int nthreads);
+
 /* Measured FP64 FMA throughput of the current device (GFLOP/s, 2 per FMA)
  * and the probe kernel's time: the roofline denominator of the FP64-bound
  * RHS.  No reference counterpart (measurement support). */
