@@ -3,7 +3,7 @@
 // node numbering (the "zipped" vector) and the unzip / zip operators.
 //
 // What it restates (the reference's own mesh needs MPI and LAPACK and is not
-// compiled here; see the oracle notes):
+// compiled here):
 //   octree + 2:1 balance        ot::Mesh construction (src/mesh.cpp:283),
 //                               balance across faces, edges and corners
 //   blocks                      octree2BlockDecomposition (src/octUtils.cpp:556)
@@ -17,26 +17,31 @@
 //                               lattice of every leaf whose closure contains it;
 //                               the others are hanging
 //   Mesh::unzip                 every padded point inside the domain gets the mesh
-//   (include/mesh.tcc:7436-8690) field at its position: the degree-p Lagrange
-//                               interpolant of the coarsest leaf containing it,
-//                               whose hanging nodes are themselves interpolated
-//                               from coarser leaves.  This equals the reference's
-//                               element copy, same-level padding copy, coarser
-//                               neighbour parent->child interpolation
-//                               (FEM/include/refel.h:249-296), finer neighbour
-//                               child->parent injection (mesh.tcc:7399-7433) and
-//                               edge/corner padding, written as one rule.
-//   Mesh::zip                   every independent node takes the block value
-//   (include/mesh.tcc:3775-3822) at its position from one owning block (the
-//                               finest block holding it in its interior, first
-//                               in block order on ties).
-// Points outside the domain are not written by unzip (they are the padding
-// beyond domain faces of boundary blocks).
+//   (include/mesh.tcc:7436-8690) field at its position: an independent node's value,
+//                               or the degree-p Lagrange interpolant of the coarsest
+//                               leaf containing it, evaluated from that leaf's nodal
+//                               values, whose hanging nodes are interpolated the same
+//                               way from coarser leaves (getElementNodalValues,
+//                               mesh.tcc:2467).  This is the reference's element copy,
+//                               same-level padding copy, coarser-neighbour
+//                               parent->child interpolation (FEM/include/refel.h:249-296),
+//                               finer-neighbour child->parent injection
+//                               (mesh.tcc:7399-7433) and edge/corner padding, as one rule.
+//   Mesh::zip                   every independent node takes the block value at its
+//   (include/mesh.tcc:3775-3822) position from one owning block (the finest block
+//                               holding it in its interior, first in block order on ties).
+//
+// Operator encoding (see dgb_unzip_plan_create): a node reference is a 64-bit
+// word; bit 63 clear: copy independent node (low 32 bits); bit 63 set:
+// interpolate from source leaf (bits 12..42) at local position codes
+// (bits 0..11, 4 bits per axis, code = 2 * xi, xi in [0, 6]).  Source leaves
+// hold their 343 nodal values and are filled coarsest level first.
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -50,6 +55,9 @@
 namespace {
 
 constexpr int P = 6;  // element order
+constexpr int NPE = (P + 1) * (P + 1) * (P + 1);
+constexpr uint64_t kInterp = 1ull << 63;
+constexpr uint64_t kNone = ~0ull;
 
 struct Leaf {
     uint32_t a[3];  // anchor in node-lattice units
@@ -60,15 +68,7 @@ inline uint64_t key(int lev, uint32_t x, uint32_t y, uint32_t z)
 {
     return ((uint64_t)lev << 48) | ((uint64_t)x << 32) | ((uint64_t)y << 16) | (uint64_t)z;
 }
-inline uint64_t pkey(uint32_t x, uint32_t y, uint32_t z)
-{
-    return ((uint64_t)x << 32) | ((uint64_t)y << 16) | (uint64_t)z;
-}
-
-struct Term {
-    uint32_t dof;
-    double w;
-};
+inline uint64_t pkey(uint64_t x, uint64_t y, uint64_t z) { return (x << 32) | (y << 16) | z; }
 
 }  // namespace
 
@@ -82,24 +82,21 @@ struct dgb_mesh {
     std::vector<dgb_block_desc> blocks;
     std::vector<int> block_lev;
     std::vector<uint32_t> block_anchor;  // 3 per block (lattice units)
-    std::unordered_map<uint64_t, uint32_t> dof_of;  // pkey(position) -> dof
-    std::vector<uint32_t> dof_pos;                   // 3 per dof
-    std::vector<uint64_t> unzipped_total;
+    std::vector<uint64_t> dof_keys;      // sorted positions of the independent nodes
     // unzip operator
-    std::vector<uint32_t> copy_src;     // per padded point: dof, or sentinel
-    std::vector<uint64_t> interp_dst;   // padded point of each interpolation row
-    std::vector<uint64_t> interp_ptr;   // CSR
-    std::vector<uint32_t> interp_col;
-    std::vector<double> interp_w;
-    std::vector<uint64_t> zip_src;      // per dof: padded point it is read from
-    std::unordered_map<uint64_t, std::vector<Term>> memo;  // hanging-node rows
+    std::vector<uint32_t> copy_src;      // per padded point: dof, or 0xFFFFFFFF
+    std::vector<uint64_t> interp_dst, interp_ref;
+    std::vector<uint64_t> src_leaf;      // source leaves, by level ascending
+    std::vector<uint64_t> src_refs;      // 343 refs per source leaf
+    std::vector<uint64_t> level_ptr;     // source-leaf ranges per distinct level
+    std::vector<uint64_t> zip_src;       // per dof: padded point it is read from
 
-    uint32_t S(int lev) const { return (uint32_t)P << (D - lev); }   // leaf size
-    uint32_t sp(int lev) const { return 1u << (D - lev); }          // node spacing
+    uint32_t S(int lev) const { return (uint32_t)P << (D - lev); }  // leaf size
+    uint32_t sp(int lev) const { return 1u << (D - lev); }         // node spacing
 
     // Leaf containing the point q + eps * dir (dir components in {-1, +1}),
-    // or -1 outside the domain.
-    // hint: a level to try first (2:1 balance keeps neighbours within one level)
+    // or -1 outside the domain.  hint: a level to try first (2:1 balance keeps
+    // neighbours within one level).
     int64_t leaf_at(const int64_t q[3], const int dir[3], int hint = -1) const
     {
         int64_t c[3];
@@ -126,7 +123,6 @@ struct dgb_mesh {
         }
         return -1;
     }
-    // Leaf whose half-open box holds the lattice point c (inside the domain).
     int64_t leaf_holding(const int64_t c[3]) const
     {
         const int dir[3] = {1, 1, 1};
@@ -147,94 +143,44 @@ struct dgb_mesh {
         for (int c = 0; c < 8; c++) {
             const int dir[3] = {(c & 1) ? 1 : -1, (c & 2) ? 1 : -1, (c & 4) ? 1 : -1};
             const int64_t e = leaf_at(q, dir, hint);
-            if (e >= 0) hint = leaves[e].lev;
             if (e < 0) continue;
+            hint = leaves[e].lev;
             if (!on_lattice(leaves[e], q)) indep = false;
             if (best < 0 || leaves[e].lev < leaves[best].lev) best = e;
         }
         if (independent) *independent = indep;
         return best;
     }
+    int64_t dof(const int64_t q[3]) const
+    {
+        const uint64_t k = pkey(q[0], q[1], q[2]);
+        auto it = std::lower_bound(dof_keys.begin(), dof_keys.end(), k);
+        return (it != dof_keys.end() && *it == k) ? (int64_t)(it - dof_keys.begin()) : -1;
+    }
+    // Reference for the field at lattice point q (kNone outside the domain);
+    // interpolation references carry the LEAF index until sources are numbered.
+    uint64_t resolve(const int64_t q[3], int hint) const
+    {
+        bool indep = false;
+        const int64_t e = coarsest_at(q, &indep, hint);
+        if (e < 0) return kNone;
+        if (indep) {
+            const int64_t d = dof(q);
+            return d < 0 ? kNone : (uint64_t)d;
+        }
+        const Leaf &L = leaves[e];
+        const int64_t s = sp(L.lev);
+        uint64_t codes = 0;
+        for (int a = 0; a < 3; a++) {
+            const int64_t d2 = 2 * (q[a] - (int64_t)L.a[a]);
+            if (d2 % s != 0) return kNone;  // not on the half lattice: 2:1 balance violated
+            codes |= (uint64_t)(d2 / s) << (4 * a);
+        }
+        return kInterp | ((uint64_t)e << 12) | codes;
+    }
 };
 
 namespace {
-
-// Lagrange basis weight of node i (uniform nodes 0..P) at xi.
-double lagrange(int i, double xi)
-{
-    double num = 1.0, den = 1.0;
-    for (int m = 0; m <= P; m++) {
-        if (m == i) continue;
-        num *= (xi - m);
-        den *= (double)(i - m);
-    }
-    return num / den;
-}
-
-// Field at lattice point q as a combination of independent node values.
-void eval_point(dgb_mesh &M, const int64_t q[3], std::vector<Term> &out, double scale, int hint)
-{
-    bool indep = false;
-    const int64_t e = M.coarsest_at(q, &indep, hint);
-    if (e < 0) return;
-    if (indep) {
-        auto it = M.dof_of.find(pkey((uint32_t)q[0], (uint32_t)q[1], (uint32_t)q[2]));
-        if (it != M.dof_of.end()) {
-            out.push_back({it->second, scale});
-            return;
-        }
-    }
-    const uint64_t mk = pkey((uint32_t)q[0], (uint32_t)q[1], (uint32_t)q[2]);
-    auto mit = M.memo.find(mk);
-    if (mit == M.memo.end()) {
-        const Leaf L = M.leaves[e];
-        const int64_t s = M.sp(L.lev);
-        int idx[3][P + 1];
-        double wt[3][P + 1];
-        int cnt[3];
-        for (int a = 0; a < 3; a++) {
-            const int64_t d = q[a] - (int64_t)L.a[a];
-            if (d % s == 0) {
-                cnt[a] = 1;
-                idx[a][0] = (int)(d / s);
-                wt[a][0] = 1.0;
-            } else {
-                cnt[a] = P + 1;
-                const double xi = (double)d / (double)s;
-                for (int i = 0; i <= P; i++) {
-                    idx[a][i] = i;
-                    wt[a][i] = lagrange(i, xi);
-                }
-            }
-        }
-        std::vector<Term> row;
-        for (int k = 0; k < cnt[2]; k++)
-            for (int j = 0; j < cnt[1]; j++)
-                for (int i = 0; i < cnt[0]; i++) {
-                    const double w = wt[0][i] * wt[1][j] * wt[2][k];
-                    const int64_t n[3] = {(int64_t)L.a[0] + s * idx[0][i],
-                                          (int64_t)L.a[1] + s * idx[1][j],
-                                          (int64_t)L.a[2] + s * idx[2][k]};
-                    if (n[0] == q[0] && n[1] == q[1] && n[2] == q[2]) {
-                        // q itself is a hanging node of the coarsest leaf: cannot happen,
-                        // the coarsest leaf holds q on its lattice only if q is independent
-                        continue;
-                    }
-                    eval_point(M, n, row, w, L.lev);
-                }
-        // merge duplicates
-        std::sort(row.begin(), row.end(), [](const Term &x, const Term &y) { return x.dof < y.dof; });
-        std::vector<Term> merged;
-        for (const Term &t : row) {
-            if (!merged.empty() && merged.back().dof == t.dof)
-                merged.back().w += t.w;
-            else
-                merged.push_back(t);
-        }
-        mit = M.memo.emplace(mk, std::move(merged)).first;
-    }
-    for (const Term &t : mit->second) out.push_back({t.dof, t.w * scale});
-}
 
 int target_level(const dgb_mesh &M, const Leaf &o)
 {
@@ -260,6 +206,14 @@ int target_level(const dgb_mesh &M, const Leaf &o)
         r *= 2.0;
     }
     return lev;
+}
+
+void children(const dgb_mesh &M, const Leaf &o, std::vector<Leaf> &out)
+{
+    const uint32_t h = M.S(o.lev + 1);
+    for (int c = 0; c < 8; c++)
+        out.push_back(Leaf{{o.a[0] + ((c & 1) ? h : 0), o.a[1] + ((c & 2) ? h : 0),
+                            o.a[2] + ((c & 4) ? h : 0)}, o.lev + 1});
 }
 
 }  // namespace
@@ -291,14 +245,10 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
     while (!work.empty()) {
         Leaf o = work.back();
         work.pop_back();
-        if (o.lev < target_level(*M, o)) {
-            const uint32_t h = M->S(o.lev + 1);
-            for (int c = 0; c < 8; c++)
-                work.push_back(Leaf{{o.a[0] + ((c & 1) ? h : 0), o.a[1] + ((c & 2) ? h : 0),
-                                     o.a[2] + ((c & 4) ? h : 0)}, o.lev + 1});
-        } else {
+        if (o.lev < target_level(*M, o))
+            children(*M, o, work);
+        else
             leaves.push_back(o);
-        }
     }
     // ---- 2:1 balance across faces, edges and corners
     auto rebuild_index = [&]() {
@@ -310,9 +260,10 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
     };
     for (;;) {
         rebuild_index();
-        std::vector<char> refine(leaves.size(), 0);
-        bool any = false;
-        for (size_t i = 0; i < leaves.size(); i++) {
+        std::vector<uint8_t> refine(leaves.size(), 0);
+        int any = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(| : any)
+        for (long long i = 0; i < (long long)leaves.size(); i++) {
             const Leaf &e = leaves[i];
             const int64_t s = M->S(e.lev);
             for (int dz = -1; dz <= 1; dz++)
@@ -329,8 +280,8 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
                         if (!inside) continue;
                         const int64_t nb = M->leaf_holding(c);
                         if (nb >= 0 && leaves[nb].lev < e.lev - 1) {
-                            refine[nb] = 1;
-                            any = true;
+                            __atomic_store_n(&refine[nb], (uint8_t)1, __ATOMIC_RELAXED);
+                            any = 1;
                         }
                     }
         }
@@ -338,29 +289,22 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
         std::vector<Leaf> next;
         next.reserve(leaves.size() + 8);
         for (size_t i = 0; i < leaves.size(); i++) {
-            if (!refine[i]) {
+            if (refine[i])
+                children(*M, leaves[i], next);
+            else
                 next.push_back(leaves[i]);
-                continue;
-            }
-            const Leaf o = leaves[i];
-            const uint32_t h = M->S(o.lev + 1);
-            for (int c = 0; c < 8; c++)
-                next.push_back(Leaf{{o.a[0] + ((c & 1) ? h : 0), o.a[1] + ((c & 2) ? h : 0),
-                                     o.a[2] + ((c & 4) ? h : 0)}, o.lev + 1});
         }
         leaves.swap(next);
     }
-    // Morton order of the leaves (by anchor bits, coarse-to-fine interleave)
+    // Morton order of the leaves
     auto morton = [&](const Leaf &l) {
         uint64_t m = 0;
         for (int b = 15; b >= 0; b--)
             for (int a = 2; a >= 0; a--) m = (m << 1) | ((l.a[a] / P) >> b & 1u);
         return m;
     };
-    std::sort(leaves.begin(), leaves.end(), [&](const Leaf &x, const Leaf &y) {
-        const uint64_t mx = morton(x), my = morton(y);
-        return mx != my ? mx < my : x.lev < y.lev;
-    });
+    std::sort(leaves.begin(), leaves.end(),
+              [&](const Leaf &x, const Leaf &y) { return morton(x) < morton(y); });
     rebuild_index();
 
     // ---- blocks: maximal aligned cubes of 2^k leaves of one level
@@ -386,7 +330,6 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
                     }
             if (ok) {
                 kbest = k;
-                anc[0] = A[0]; anc[1] = A[1]; anc[2] = A[2];
                 break;
             }
         }
@@ -414,70 +357,180 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
         M->block_anchor.insert(M->block_anchor.end(), anc, anc + 3);
     }
 
-    // ---- independent nodes (the zipped vector), leaf by leaf
-    M->dof_of.reserve(leaves.size() * 250);
-    for (size_t i = 0; i < leaves.size(); i++) {
-        const Leaf &e = leaves[i];
-        const int64_t s = M->sp(e.lev);
-        for (int k = 0; k <= P; k++)
-            for (int j = 0; j <= P; j++)
-                for (int ii = 0; ii <= P; ii++) {
-                    const int64_t q[3] = {(int64_t)e.a[0] + s * ii, (int64_t)e.a[1] + s * j,
-                                          (int64_t)e.a[2] + s * k};
-                    const uint64_t pk = pkey((uint32_t)q[0], (uint32_t)q[1], (uint32_t)q[2]);
-                    if (M->dof_of.count(pk)) continue;
-                    bool indep = true;
-                    if (ii == 0 || ii == P || j == 0 || j == P || k == 0 || k == P)
-                        M->coarsest_at(q, &indep, e.lev);  // inner nodes belong to e alone
-                    if (!indep) continue;
-                    const uint32_t id = (uint32_t)M->dof_pos.size() / 3;
-                    M->dof_of.emplace(pk, id);
-                    M->dof_pos.push_back((uint32_t)q[0]);
-                    M->dof_pos.push_back((uint32_t)q[1]);
-                    M->dof_pos.push_back((uint32_t)q[2]);
-                }
+    // ---- independent nodes: candidates per leaf, then sort + unique
+    {
+        std::vector<std::vector<uint64_t>> part;
+        int nt = 1;
+#ifdef _OPENMP
+        nt = omp_get_max_threads();
+#endif
+        part.resize(nt);
+#pragma omp parallel
+        {
+            int t = 0;
+#ifdef _OPENMP
+            t = omp_get_thread_num();
+#endif
+            std::vector<uint64_t> &mine = part[t];
+#pragma omp for schedule(dynamic, 256)
+            for (long long i = 0; i < (long long)leaves.size(); i++) {
+                const Leaf &e = leaves[i];
+                const int64_t s = M->sp(e.lev);
+                for (int k = 0; k <= P; k++)
+                    for (int j = 0; j <= P; j++)
+                        for (int ii = 0; ii <= P; ii++) {
+                            const int64_t q[3] = {(int64_t)e.a[0] + s * ii, (int64_t)e.a[1] + s * j,
+                                                  (int64_t)e.a[2] + s * k};
+                            bool indep = true;
+                            if (ii == 0 || ii == P || j == 0 || j == P || k == 0 || k == P)
+                                M->coarsest_at(q, &indep, e.lev);  // inner nodes belong to e alone
+                            if (indep) mine.push_back(pkey(q[0], q[1], q[2]));
+                        }
+            }
+        }
+        size_t tot = 0;
+        for (auto &v : part) tot += v.size();
+        M->dof_keys.reserve(tot);
+        for (auto &v : part) {
+            M->dof_keys.insert(M->dof_keys.end(), v.begin(), v.end());
+            std::vector<uint64_t>().swap(v);
+        }
+        std::sort(M->dof_keys.begin(), M->dof_keys.end());
+        M->dof_keys.erase(std::unique(M->dof_keys.begin(), M->dof_keys.end()), M->dof_keys.end());
     }
-    const uint64_t ndof = M->dof_pos.size() / 3;
+    const uint64_t ndof = M->dof_keys.size();
+    if (ndof >= 0xFFFFFFFFull) {
+        delete M;
+        return DGB_ERR_INVALID;
+    }
 
-    // ---- unzip operator and zip owners
+    // ---- padded points: copy or interpolation reference (parallel over blocks)
     const uint32_t SENT = 0xFFFFFFFFu;
     M->copy_src.assign(off, SENT);
+    std::vector<uint8_t> is_src(leaves.size(), 0);
+    std::vector<std::vector<std::pair<uint64_t, uint64_t>>> rows_part;
+    int ntr = 1;
+#ifdef _OPENMP
+    ntr = omp_get_max_threads();
+#endif
+    rows_part.resize(ntr);
+    std::atomic<int> bad{0};
+#pragma omp parallel
+    {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+#pragma omp for schedule(dynamic, 4)
+        for (long long b = 0; b < (long long)M->blocks.size(); b++) {
+            const dgb_block_desc &B = M->blocks[b];
+            const int lev = M->block_lev[b];
+            const int64_t s = M->sp(lev);
+            const uint32_t *A = &M->block_anchor[3 * b];
+            const int n = (int)B.sz[0];
+            for (int k = 0; k < n; k++)
+                for (int j = 0; j < n; j++)
+                    for (int i = 0; i < n; i++) {
+                        const int64_t q[3] = {(int64_t)A[0] + s * (i - 3), (int64_t)A[1] + s * (j - 3),
+                                              (int64_t)A[2] + s * (k - 3)};
+                        bool inside = true;
+                        for (int a = 0; a < 3; a++)
+                            if (q[a] < 0 || q[a] > (int64_t)M->N) inside = false;
+                        if (!inside) continue;
+                        const uint64_t dst = B.offset + (uint64_t)i + (uint64_t)n * (j + (uint64_t)n * k);
+                        const uint64_t r = M->resolve(q, lev);
+                        if (r == kNone) {
+                            bad = 1;
+                        } else if (r & kInterp) {
+                            rows_part[t].push_back({dst, r});
+                            __atomic_store_n(&is_src[(r >> 12) & 0x7FFFFFFFull], (uint8_t)1, __ATOMIC_RELAXED);
+                        } else {
+                            M->copy_src[dst] = (uint32_t)r;
+                        }
+                    }
+        }
+    }
+    if (bad) {
+        delete M;
+        return DGB_ERR_INVALID;
+    }
+    // ---- source leaves: close under hanging-node references, finest level first
+    std::vector<std::vector<uint64_t>> leaf_refs(leaves.size());
+    for (int lev = M->D; lev >= 0; lev--) {
+        std::vector<long long> at;
+        for (size_t i = 0; i < leaves.size(); i++)
+            if (is_src[i] && leaves[i].lev == lev) at.push_back((long long)i);
+#pragma omp parallel for schedule(dynamic, 16)
+        for (long long q2 = 0; q2 < (long long)at.size(); q2++) {
+            const long long i = at[q2];
+            const Leaf &e = leaves[i];
+            const int64_t s = M->sp(e.lev);
+            std::vector<uint64_t> refs(NPE);
+            for (int k = 0; k <= P; k++)
+                for (int j = 0; j <= P; j++)
+                    for (int ii = 0; ii <= P; ii++) {
+                        const int64_t q[3] = {(int64_t)e.a[0] + s * ii, (int64_t)e.a[1] + s * j,
+                                              (int64_t)e.a[2] + s * k};
+                        const uint64_t r = M->resolve(q, e.lev);
+                        refs[ii + (P + 1) * (j + (P + 1) * k)] = r;
+                        if (r == kNone) bad = 1;
+                        else if (r & kInterp)
+                            __atomic_store_n(&is_src[(r >> 12) & 0x7FFFFFFFull], (uint8_t)1, __ATOMIC_RELAXED);
+                    }
+            leaf_refs[i].swap(refs);
+        }
+    }
+    if (bad) {
+        delete M;
+        return DGB_ERR_INVALID;
+    }
+    // number the sources by level ascending; remap leaf indices to source indices
+    std::vector<uint64_t> src_of(leaves.size(), kNone);
+    for (int lev = 0; lev <= M->D; lev++) {
+        bool opened = false;
+        for (size_t i = 0; i < leaves.size(); i++) {
+            if (!is_src[i] || leaves[i].lev != lev) continue;
+            if (!opened) {
+                M->level_ptr.push_back(M->src_leaf.size());
+                opened = true;
+            }
+            src_of[i] = M->src_leaf.size();
+            M->src_leaf.push_back(i);
+        }
+    }
+    M->level_ptr.push_back(M->src_leaf.size());
+    auto remap = [&](uint64_t r) -> uint64_t {
+        if (!(r & kInterp)) return r;
+        const uint64_t leaf = (r >> 12) & 0x7FFFFFFFull;
+        return kInterp | (src_of[leaf] << 12) | (r & 0xFFFull);
+    };
+    M->src_refs.resize(M->src_leaf.size() * NPE);
+    for (size_t sidx = 0; sidx < M->src_leaf.size(); sidx++) {
+        const auto &refs = leaf_refs[M->src_leaf[sidx]];
+        for (int n = 0; n < NPE; n++) M->src_refs[sidx * NPE + n] = remap(refs[n]);
+    }
+    for (auto &part : rows_part) {
+        for (auto &dr : part) {
+            M->interp_dst.push_back(dr.first);
+            M->interp_ref.push_back(remap(dr.second));
+        }
+        std::vector<std::pair<uint64_t, uint64_t>>().swap(part);
+    }
+    // ---- zip owners: finest block holding the node in its interior, first on ties
     M->zip_src.assign(ndof, ~0ull);
-    std::vector<int> owner_lev(ndof, -1);
-    M->interp_ptr.push_back(0);
-    std::vector<Term> row;
+    std::vector<int8_t> owner_lev(ndof, -1);
     for (size_t b = 0; b < M->blocks.size(); b++) {
         const dgb_block_desc &B = M->blocks[b];
         const int lev = M->block_lev[b];
-        const int64_t s = M->sp(lev);
-        const uint32_t *A = &M->block_anchor[3 * b];
         const int n = (int)B.sz[0];
-        for (int k = 0; k < n; k++)
-            for (int j = 0; j < n; j++)
-                for (int i = 0; i < n; i++) {
-                    const int64_t q[3] = {(int64_t)A[0] + s * (i - 3), (int64_t)A[1] + s * (j - 3),
-                                          (int64_t)A[2] + s * (k - 3)};
-                    bool inside = true;
-                    for (int a = 0; a < 3; a++)
-                        if (q[a] < 0 || q[a] > (int64_t)M->N) inside = false;
-                    if (!inside) continue;
+        for (int k = 3; k < n - 3; k++)
+            for (int j = 3; j < n - 3; j++)
+                for (int i = 3; i < n - 3; i++) {
                     const uint64_t dst = B.offset + (uint64_t)i + (uint64_t)n * (j + (uint64_t)n * k);
-                    row.clear();
-                    eval_point(*M, q, row, 1.0, lev);
-                    if (row.size() == 1 && row[0].w == 1.0) {
-                        M->copy_src[dst] = row[0].dof;
-                        const bool interior = i >= 3 && i < n - 3 && j >= 3 && j < n - 3 && k >= 3 && k < n - 3;
-                        if (interior && lev > owner_lev[row[0].dof]) {
-                            owner_lev[row[0].dof] = lev;
-                            M->zip_src[row[0].dof] = dst;
-                        }
-                    } else if (!row.empty()) {
-                        M->interp_dst.push_back(dst);
-                        for (const Term &t : row) {
-                            M->interp_col.push_back(t.dof);
-                            M->interp_w.push_back(t.w);
-                        }
-                        M->interp_ptr.push_back(M->interp_col.size());
+                    const uint32_t d = M->copy_src[dst];
+                    if (d != SENT && lev > owner_lev[d]) {
+                        owner_lev[d] = (int8_t)lev;
+                        M->zip_src[d] = dst;
                     }
                 }
     }
@@ -486,7 +539,6 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
             delete M;
             return DGB_ERR_INVALID;  // an independent node without an owning block
         }
-    M->memo.clear();
     *out = M;
     return DGB_OK;
 }
@@ -501,11 +553,12 @@ dgb_status dgb_mesh_sizes(const dgb_mesh *M, uint64_t *sizes)
 {
     if (!M || !sizes) return DGB_ERR_INVALID;
     sizes[0] = M->leaves.size();
-    sizes[1] = M->dof_pos.size() / 3;
+    sizes[1] = M->dof_keys.size();
     sizes[2] = M->blocks.size();
     sizes[3] = M->copy_src.size();
     sizes[4] = M->interp_dst.size();
-    sizes[5] = M->interp_col.size();
+    sizes[5] = M->src_leaf.size();
+    sizes[6] = M->level_ptr.size() ? M->level_ptr.size() - 1 : 0;
     return DGB_OK;
 }
 
@@ -519,10 +572,12 @@ dgb_status dgb_mesh_blocks(const dgb_mesh *M, dgb_block_desc *out)
 dgb_status dgb_mesh_dof_coords(const dgb_mesh *M, double *xyz)
 {
     if (!M || !xyz) return DGB_ERR_INVALID;
-    const size_t n = M->dof_pos.size() / 3;
-    for (size_t d = 0; d < n; d++)
-        for (int a = 0; a < 3; a++)
-            xyz[3 * d + a] = M->prm.domain_min[a] + M->dof_pos[3 * d + a] * M->unit;
+    const size_t n = M->dof_keys.size();
+    for (size_t d = 0; d < n; d++) {
+        const uint64_t k = M->dof_keys[d];
+        const uint64_t c[3] = {k >> 32, (k >> 16) & 0xFFFF, k & 0xFFFF};
+        for (int a = 0; a < 3; a++) xyz[3 * d + a] = M->prm.domain_min[a] + c[a] * M->unit;
+    }
     return DGB_OK;
 }
 
@@ -538,15 +593,15 @@ dgb_status dgb_mesh_leaf_levels(const dgb_mesh *M, uint8_t *lev, uint32_t *ancho
 }
 
 dgb_status dgb_mesh_unzip_operator(const dgb_mesh *M, uint32_t *copy_src, uint64_t *interp_dst,
-                                   uint64_t *interp_ptr, uint32_t *interp_col, double *interp_w,
+                                   uint64_t *interp_ref, uint64_t *src_refs, uint64_t *level_ptr,
                                    uint64_t *zip_src)
 {
     if (!M) return DGB_ERR_INVALID;
     if (copy_src) memcpy(copy_src, M->copy_src.data(), M->copy_src.size() * 4);
     if (interp_dst) memcpy(interp_dst, M->interp_dst.data(), M->interp_dst.size() * 8);
-    if (interp_ptr) memcpy(interp_ptr, M->interp_ptr.data(), M->interp_ptr.size() * 8);
-    if (interp_col) memcpy(interp_col, M->interp_col.data(), M->interp_col.size() * 4);
-    if (interp_w) memcpy(interp_w, M->interp_w.data(), M->interp_w.size() * 8);
+    if (interp_ref) memcpy(interp_ref, M->interp_ref.data(), M->interp_ref.size() * 8);
+    if (src_refs) memcpy(src_refs, M->src_refs.data(), M->src_refs.size() * 8);
+    if (level_ptr) memcpy(level_ptr, M->level_ptr.data(), M->level_ptr.size() * 8);
     if (zip_src) memcpy(zip_src, M->zip_src.data(), M->zip_src.size() * 8);
     return DGB_OK;
 }

@@ -1,18 +1,23 @@
-// Device unzip / zip from a generic mesh operator, and the full RK4 step as
-// one CUDA graph per step.
+// Device unzip / zip from a mesh operator, and the full RK4 step as one CUDA
+// graph per step.
 //
-// unzip: a copy pass (one thread per padded point, all fields per thread, the
-// zipped index read once) and an interpolation pass (one thread per
-// interpolation row: hanging nodes and padding next to coarser leaves,
-// 2..343 terms).  zip: one gather per independent node.  All three are
-// HBM-bound; the RK4 step around them is
-//   for s in 0..3: unzip(prev or im) -> bssnRHS -> zip -> stage update
-// (BSSN_GR/src/rkBSSN.cpp:803-1012), captured once and replayed.
+// unzip (per call, for nvars fields):
+//   1. source elements, one launch per refinement level, coarsest first: the
+//      343 nodal values of every element something interpolates from, each a
+//      zipped-node copy or (a hanging node) an interpolation from a coarser
+//      source element;
+//   2. copies: one thread per padded point, all fields per thread;
+//   3. interpolated padded points: one thread per row, the separable degree-6
+//      Lagrange sum over one source element (1, 7, 49 or 343 terms).
+// zip: one gather per independent node.  All HBM/L2-bound; the RK4 step
+// around them is  for s in 0..3: unzip(prev or im) -> bssnRHS -> zip ->
+// stage update  (BSSN_GR/src/rkBSSN.cpp:803-1012), captured once and replayed.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
 
 #include <string>
+#include <vector>
 
 #include "dgb_internal.h"
 
@@ -20,12 +25,81 @@ namespace dgb {
 namespace {
 
 constexpr uint32_t kSentinel = 0xFFFFFFFFu;
+constexpr uint64_t kInterp = 1ull << 63;
+constexpr int kNpe = 343;
 
 struct FieldPtrs {
     const double *in[NV];
     double *out[NV];
     int nvars;
 };
+
+// 1-D Lagrange weights at xi = code/2 for the odd codes 1, 3, ..., 11
+struct LagTable {
+    double w[6][7];
+};
+
+__device__ __forceinline__ int axis_terms(uint32_t code, const LagTable &T, double *w, int *idx)
+{
+    if ((code & 1u) == 0) {
+        w[0] = 1.0;
+        idx[0] = (int)(code >> 1);
+        return 1;
+    }
+    const int r = (int)(code >> 1);
+#pragma unroll
+    for (int i = 0; i < 7; i++) {
+        w[i] = T.w[r][i];
+        idx[i] = i;
+    }
+    return 7;
+}
+
+// Value of reference ref for field v (zipped array z, source table dg).
+__device__ __forceinline__ double ref_value(uint64_t ref, const double *__restrict__ z,
+                                            const double *__restrict__ dg, const LagTable &T)
+{
+    if (!(ref & kInterp)) return __ldg(z + (uint32_t)ref);
+    const uint64_t src = (ref >> 12) & 0x7FFFFFFFull;
+    double wx[7], wy[7], wz[7];
+    int ix[7], iy[7], iz[7];
+    const int nx = axis_terms((uint32_t)(ref & 0xF), T, wx, ix);
+    const int ny = axis_terms((uint32_t)((ref >> 4) & 0xF), T, wy, iy);
+    const int nz = axis_terms((uint32_t)((ref >> 8) & 0xF), T, wz, iz);
+    const double *e = dg + src * kNpe;
+    double acc = 0.0;
+    for (int c = 0; c < nz; c++) {
+        double accy = 0.0;
+        for (int b = 0; b < ny; b++) {
+            const double *row = e + 7 * (iy[b] + 7 * iz[c]);
+            double accx = 0.0;
+            for (int a = 0; a < nx; a++) accx = fma(wx[a], row[ix[a]], accx);
+            accy = fma(wy[b], accx, accy);
+        }
+        acc = fma(wz[c], accy, acc);
+    }
+    return acc;
+}
+
+struct DgArgs {
+    const double *z[NV];
+    double *dg[NV];
+    int nvars;
+    const uint64_t *refs;
+    uint64_t first, count;  // source range of this level
+    LagTable T;
+};
+
+__global__ void __launch_bounds__(256) dg_fill_kernel(const DgArgs a)
+{
+    const uint64_t n = a.count * kNpe;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += stride) {
+        const uint64_t slot = a.first * kNpe + t;
+        const uint64_t ref = __ldg(a.refs + slot);
+        for (int v = 0; v < a.nvars; v++) a.dg[v][slot] = ref_value(ref, a.z[v], a.dg[v], a.T);
+    }
+}
 
 __global__ void __launch_bounds__(256) unzip_copy_kernel(const FieldPtrs f, const uint32_t *__restrict__ src,
                                                          uint64_t n)
@@ -38,27 +112,20 @@ __global__ void __launch_bounds__(256) unzip_copy_kernel(const FieldPtrs f, cons
     }
 }
 
-__global__ void __launch_bounds__(128) unzip_interp_kernel(const FieldPtrs f, const uint64_t *__restrict__ dst,
-                                                           const uint64_t *__restrict__ ptr,
-                                                           const uint32_t *__restrict__ col,
-                                                           const double *__restrict__ w, uint64_t nrows)
+struct InterpArgs {
+    FieldPtrs f;
+    const double *dg[NV];
+    const uint64_t *dst, *ref;
+    uint64_t nrows;
+    LagTable T;
+};
+
+__global__ void __launch_bounds__(128) unzip_interp_kernel(const InterpArgs a)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < nrows; r += stride) {
-        const uint64_t b = ptr[r], e = ptr[r + 1], d = dst[r];
-        double acc[NV];
-#pragma unroll
-        for (int v = 0; v < NV; v++) acc[v] = 0.0;
-        for (uint64_t t = b; t < e; t++) {
-            const uint32_t c = __ldg(col + t);
-            const double wt = __ldg(w + t);
-#pragma unroll
-            for (int v = 0; v < NV; v++)
-                if (v < f.nvars) acc[v] = fma(wt, __ldg(f.in[v] + c), acc[v]);
-        }
-#pragma unroll
-        for (int v = 0; v < NV; v++)
-            if (v < f.nvars) f.out[v][d] = acc[v];
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < a.nrows; r += stride) {
+        const uint64_t d = __ldg(a.dst + r), ref = __ldg(a.ref + r);
+        for (int v = 0; v < a.f.nvars; v++) a.f.out[v][d] = ref_value(ref, a.f.in[v], a.dg[v], a.T);
     }
 }
 
@@ -84,17 +151,38 @@ unsigned grid_for(uint64_t n, int threads)
     return (unsigned)g;
 }
 
+// Uniform-node Lagrange basis on 0..6 (the reference's interpolation matrices
+// come from a Vandermonde solve on the same nodes, FEM/src/refel.cpp:84-170).
+LagTable lagrange_table()
+{
+    LagTable T;
+    for (int r = 0; r < 6; r++) {
+        const double xi = r + 0.5;
+        for (int i = 0; i < 7; i++) {
+            double num = 1.0, den = 1.0;
+            for (int m = 0; m < 7; m++) {
+                if (m == i) continue;
+                num *= (xi - m);
+                den *= (double)(i - m);
+            }
+            T.w[r][i] = num / den;
+        }
+    }
+    return T;
+}
+
 }  // namespace
 }  // namespace dgb
 
 using namespace dgb;
 
 struct dgb_unzip_plan {
-    uint64_t ndof = 0, nunz = 0, ninterp = 0, nnz = 0;
+    uint64_t ndof = 0, nunz = 0, ninterp = 0, nsrc = 0;
+    std::vector<uint64_t> level_ptr;
     uint32_t *d_copy = nullptr;
-    uint64_t *d_idst = nullptr, *d_iptr = nullptr, *d_zip = nullptr;
-    uint32_t *d_icol = nullptr;
-    double *d_iw = nullptr;
+    uint64_t *d_idst = nullptr, *d_iref = nullptr, *d_srefs = nullptr, *d_zip = nullptr;
+    double *d_dg = nullptr;  // nsrc * 343 * 24 source nodal values
+    LagTable T;
 };
 
 struct dgb_stepper {
@@ -124,6 +212,25 @@ namespace {
 dgb_status do_unzip(dgb_unzip_plan *p, const double *const *zipped, double *const *unzipped,
                     int nvars, cudaStream_t st)
 {
+    double *dg[NV];
+    for (int v = 0; v < NV; v++) dg[v] = p->d_dg + (size_t)v * p->nsrc * kNpe;
+    if (p->nsrc) {
+        DgArgs a;
+        for (int v = 0; v < NV; v++) {
+            a.z[v] = v < nvars ? zipped[v] : nullptr;
+            a.dg[v] = dg[v];
+        }
+        a.nvars = nvars;
+        a.refs = p->d_srefs;
+        a.T = p->T;
+        for (size_t l = 0; l + 1 < p->level_ptr.size(); l++) {
+            a.first = p->level_ptr[l];
+            a.count = p->level_ptr[l + 1] - p->level_ptr[l];
+            if (!a.count) continue;
+            dg_fill_kernel<<<grid_for(a.count * kNpe, 256), 256, 0, st>>>(a);
+            DGB_CUDA(cudaGetLastError());
+        }
+    }
     FieldPtrs f;
     f.nvars = nvars;
     for (int v = 0; v < NV; v++) {
@@ -135,8 +242,14 @@ dgb_status do_unzip(dgb_unzip_plan *p, const double *const *zipped, double *cons
         DGB_CUDA(cudaGetLastError());
     }
     if (p->ninterp) {
-        unzip_interp_kernel<<<grid_for(p->ninterp, 128), 128, 0, st>>>(f, p->d_idst, p->d_iptr, p->d_icol,
-                                                                      p->d_iw, p->ninterp);
+        InterpArgs a;
+        a.f = f;
+        for (int v = 0; v < NV; v++) a.dg[v] = dg[v];
+        a.dst = p->d_idst;
+        a.ref = p->d_iref;
+        a.nrows = p->ninterp;
+        a.T = p->T;
+        unzip_interp_kernel<<<grid_for(p->ninterp, 128), 128, 0, st>>>(a);
         DGB_CUDA(cudaGetLastError());
     }
     return DGB_OK;
@@ -187,42 +300,58 @@ dgb_status enqueue_step(dgb_stepper *s, double *const *state, double dt, double 
     return DGB_OK;
 }
 
+bool ref_ok(uint64_t ref, uint64_t ndof, uint64_t src_limit)
+{
+    if (!(ref & kInterp)) return ref < ndof;
+    if (((ref >> 12) & 0x7FFFFFFFull) >= src_limit) return false;
+    if (ref & 0x7FFFF80000000000ull) return false;  // bits 43..62 unused
+    for (int a = 0; a < 3; a++)
+        if (((ref >> (4 * a)) & 0xF) > 12) return false;
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
 
 dgb_status dgb_unzip_plan_create(uint64_t ndof, uint64_t unzipped_size, const uint32_t *copy_src,
                                  uint64_t ninterp, const uint64_t *interp_dst,
-                                 const uint64_t *interp_ptr, const uint32_t *interp_col,
-                                 const double *interp_w, const uint64_t *zip_src,
+                                 const uint64_t *interp_ref, uint64_t nsrc,
+                                 const uint64_t *src_refs, uint64_t nlevels,
+                                 const uint64_t *level_ptr, const uint64_t *zip_src,
                                  dgb_unzip_plan **out)
 {
     if (!out || (unzipped_size && !copy_src) || (ndof && !zip_src) ||
-        (ninterp && (!interp_dst || !interp_ptr || !interp_col || !interp_w))) {
+        (ninterp && (!interp_dst || !interp_ref)) || (nsrc && (!src_refs || !level_ptr))) {
         set_error("dgb_unzip_plan_create: null argument");
         return DGB_ERR_INVALID;
     }
-    if (ndof >= kSentinel) {
-        set_error("dgb_unzip_plan_create: more than 2^32-1 zipped nodes");
+    if (ndof >= kSentinel || nsrc >= (1ull << 31)) {
+        set_error("dgb_unzip_plan_create: operator too large for its encoding");
         return DGB_ERR_INVALID;
     }
-    // validate the operator so the kernels cannot read or write out of range
+    // validate the operator so the kernels cannot read or write out of range,
+    // and sources are only read after they are filled
     for (uint64_t p = 0; p < unzipped_size; p++)
         if (copy_src[p] != kSentinel && copy_src[p] >= ndof) {
             set_error("dgb_unzip_plan_create: copy source out of range");
             return DGB_ERR_INVALID;
         }
-    const uint64_t nnz = ninterp ? interp_ptr[ninterp] : 0;
-    if (ninterp && interp_ptr[0] != 0) return DGB_ERR_INVALID;
-    for (uint64_t r = 0; r < ninterp; r++) {
-        if (interp_dst[r] >= unzipped_size || interp_ptr[r + 1] < interp_ptr[r]) {
-            set_error("dgb_unzip_plan_create: bad interpolation row");
-            return DGB_ERR_INVALID;
-        }
+    if (nsrc && (level_ptr[0] != 0 || level_ptr[nlevels] != nsrc)) {
+        set_error("dgb_unzip_plan_create: level_ptr must span the sources");
+        return DGB_ERR_INVALID;
     }
-    for (uint64_t t = 0; t < nnz; t++)
-        if (interp_col[t] >= ndof) {
-            set_error("dgb_unzip_plan_create: interpolation column out of range");
+    for (uint64_t l = 0; nsrc && l < nlevels; l++) {
+        if (level_ptr[l + 1] < level_ptr[l]) return DGB_ERR_INVALID;
+        for (uint64_t t = level_ptr[l] * kNpe; t < level_ptr[l + 1] * kNpe; t++)
+            if (!ref_ok(src_refs[t], ndof, level_ptr[l])) {
+                set_error("dgb_unzip_plan_create: a source element reads an unfilled source");
+                return DGB_ERR_INVALID;
+            }
+    }
+    for (uint64_t r = 0; r < ninterp; r++)
+        if (interp_dst[r] >= unzipped_size || !ref_ok(interp_ref[r], ndof, nsrc)) {
+            set_error("dgb_unzip_plan_create: bad interpolation row");
             return DGB_ERR_INVALID;
         }
     for (uint64_t d = 0; d < ndof; d++)
@@ -234,7 +363,9 @@ dgb_status dgb_unzip_plan_create(uint64_t ndof, uint64_t unzipped_size, const ui
     p->ndof = ndof;
     p->nunz = unzipped_size;
     p->ninterp = ninterp;
-    p->nnz = nnz;
+    p->nsrc = nsrc;
+    if (nsrc) p->level_ptr.assign(level_ptr, level_ptr + nlevels + 1);
+    p->T = lagrange_table();
     cudaError_t e = cudaSuccess;
     auto up = [&](void **dst, const void *src, size_t bytes) {
         if (e != cudaSuccess || bytes == 0) return;
@@ -244,9 +375,9 @@ dgb_status dgb_unzip_plan_create(uint64_t ndof, uint64_t unzipped_size, const ui
     up((void **)&p->d_copy, copy_src, unzipped_size * 4);
     up((void **)&p->d_zip, zip_src, ndof * 8);
     up((void **)&p->d_idst, interp_dst, ninterp * 8);
-    up((void **)&p->d_iptr, interp_ptr, ninterp ? (ninterp + 1) * 8 : 0);
-    up((void **)&p->d_icol, interp_col, nnz * 4);
-    up((void **)&p->d_iw, interp_w, nnz * 8);
+    up((void **)&p->d_iref, interp_ref, ninterp * 8);
+    up((void **)&p->d_srefs, src_refs, nsrc * kNpe * 8);
+    if (e == cudaSuccess && nsrc) e = cudaMalloc(&p->d_dg, nsrc * kNpe * NV * sizeof(double));
     if (e != cudaSuccess) {
         set_error(std::string("dgb_unzip_plan_create: ") + cudaGetErrorString(e));
         dgb_unzip_plan_destroy(p);
@@ -262,9 +393,9 @@ dgb_status dgb_unzip_plan_destroy(dgb_unzip_plan *p)
     cudaFree(p->d_copy);
     cudaFree(p->d_zip);
     cudaFree(p->d_idst);
-    cudaFree(p->d_iptr);
-    cudaFree(p->d_icol);
-    cudaFree(p->d_iw);
+    cudaFree(p->d_iref);
+    cudaFree(p->d_srefs);
+    cudaFree(p->d_dg);
     delete p;
     return DGB_OK;
 }

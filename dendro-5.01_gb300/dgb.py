@@ -103,8 +103,9 @@ _SIGS = {
     "dgb_mesh_leaf_levels": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "dgb_mesh_unzip_operator": (C.c_int, [C.c_void_p] + [C.c_void_p] * 6),
     "dgb_unzip_plan_create": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint64,
-                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                        C.c_void_p, C.POINTER(C.c_void_p)]),
+                                        C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
+                                        C.c_uint64, C.c_void_p, C.c_void_p,
+                                        C.POINTER(C.c_void_p)]),
     "dgb_unzip_plan_destroy": (C.c_int, [C.c_void_p]),
     "dgb_unzip": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
     "dgb_zip": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
@@ -297,10 +298,10 @@ class Mesh:
         h = C.c_void_p()
         check(lib().dgb_mesh_create(C.byref(params), C.byref(h)), "dgb_mesh_create")
         self.h = h
-        s = (C.c_uint64 * 6)()
+        s = (C.c_uint64 * 7)()
         check(lib().dgb_mesh_sizes(h, s), "dgb_mesh_sizes")
         (self.num_leaves, self.ndof, self.nblocks, self.nunzipped, self.ninterp,
-         self.nnz) = [int(x) for x in s]
+         self.nsrc, self.nlevels) = [int(x) for x in s]
         self.blocks = (BlockDesc * self.nblocks)()
         check(lib().dgb_mesh_blocks(h, self.blocks), "dgb_mesh_blocks")
 
@@ -319,15 +320,15 @@ class Mesh:
     def operator(self):
         cp = np.zeros(self.nunzipped, dtype=np.uint32)
         idst = np.zeros(self.ninterp, dtype=np.uint64)
-        iptr = np.zeros(self.ninterp + 1, dtype=np.uint64)
-        icol = np.zeros(self.nnz, dtype=np.uint32)
-        iw = np.zeros(self.nnz)
+        iref = np.zeros(self.ninterp, dtype=np.uint64)
+        srefs = np.zeros(self.nsrc * 343, dtype=np.uint64)
+        lptr = np.zeros(self.nlevels + 1, dtype=np.uint64)
         zs = np.zeros(self.ndof, dtype=np.uint64)
         check(lib().dgb_mesh_unzip_operator(self.h, cp.ctypes.data, idst.ctypes.data,
-                                            iptr.ctypes.data, icol.ctypes.data, iw.ctypes.data,
+                                            iref.ctypes.data, srefs.ctypes.data, lptr.ctypes.data,
                                             zs.ctypes.data), "dgb_mesh_unzip_operator")
-        return {"copy_src": cp, "interp_dst": idst, "interp_ptr": iptr, "interp_col": icol,
-                "interp_w": iw, "zip_src": zs}
+        return {"copy_src": cp, "interp_dst": idst, "interp_ref": iref, "src_refs": srefs,
+                "level_ptr": lptr, "zip_src": zs}
 
     def close(self):
         if self.h:
@@ -356,11 +357,13 @@ class UnzipPlan:
         h = C.c_void_p()
         n = len(op["copy_src"])
         ni = len(op["interp_dst"])
+        nsrc = len(op["src_refs"]) // 343
+        nlev = max(len(op["level_ptr"]) - 1, 0)
         check(lib().dgb_unzip_plan_create(ndof, n, op["copy_src"].ctypes.data, ni,
                                           op["interp_dst"].ctypes.data,
-                                          op["interp_ptr"].ctypes.data,
-                                          op["interp_col"].ctypes.data,
-                                          op["interp_w"].ctypes.data, op["zip_src"].ctypes.data,
+                                          op["interp_ref"].ctypes.data, nsrc,
+                                          op["src_refs"].ctypes.data, nlev,
+                                          op["level_ptr"].ctypes.data, op["zip_src"].ctypes.data,
                                           C.byref(h)), "dgb_unzip_plan_create")
         self.h = h
 

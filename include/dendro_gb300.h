@@ -179,29 +179,38 @@ typedef struct {
 typedef struct dgb_mesh dgb_mesh;
 dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **mesh);
 dgb_status dgb_mesh_destroy(dgb_mesh *mesh);
-/* sizes[0..5]: leaves, independent nodes (zipped length), blocks, padded
- * points (unzipped length), interpolation rows, interpolation terms. */
+/* sizes[0..6]: leaves, independent nodes (zipped length), blocks, padded
+ * points (unzipped length), interpolation rows, source elements, source
+ * levels. */
 dgb_status dgb_mesh_sizes(const dgb_mesh *mesh, uint64_t *sizes);
 dgb_status dgb_mesh_blocks(const dgb_mesh *mesh, dgb_block_desc *blocks);
 dgb_status dgb_mesh_dof_coords(const dgb_mesh *mesh, double *xyz);
 dgb_status dgb_mesh_leaf_levels(const dgb_mesh *mesh, uint8_t *level, uint32_t *anchor);
-/* The mesh's unzip / zip operators in the generic form dgb_unzip_plan_create
- * takes (array lengths from dgb_mesh_sizes). */
+/* The mesh's unzip / zip operators in the form dgb_unzip_plan_create takes
+ * (array lengths from dgb_mesh_sizes; src_refs holds 343 per source). */
 dgb_status dgb_mesh_unzip_operator(const dgb_mesh *mesh, uint32_t *copy_src, uint64_t *interp_dst,
-                                   uint64_t *interp_ptr, uint32_t *interp_col, double *interp_w,
+                                   uint64_t *interp_ref, uint64_t *src_refs, uint64_t *level_ptr,
                                    uint64_t *zip_src);
 
-/* Device unzip / zip for any mesh, from the operator: padded point p copies
- * zipped node copy_src[p] (0xFFFFFFFF: not written), or, for the rows listed
- * in interp_dst, takes sum_t interp_w[t] * zipped[interp_col[t]] over the
- * CSR row interp_ptr[r]..interp_ptr[r+1]; zipped node d reads padded point
- * zip_src[d].  A host maintainer builds the operator once per mesh from
- * ot::Mesh's maps. */
+/* Device unzip / zip for any mesh, from its operator.  A node reference is
+ * a 64-bit word: bit 63 clear = the zipped node in the low 32 bits; bit 63
+ * set = the degree-6 Lagrange interpolant of source element (bits 12..42)
+ * at local position codes (bits 0..11, 4 bits per axis x,y,z, code = 2*xi,
+ * xi in [0,6] in node spacings).  Source elements are elements whose 343
+ * nodal values (src_refs, x fastest) some reference interpolates from, the
+ * way Mesh::getElementNodalValues (include/mesh.tcc:2467) rebuilds hanging
+ * nodes; they are grouped by refinement level, coarsest first
+ * (level_ptr[l]..level_ptr[l+1]), and a reference may only name a source of
+ * an earlier group.  Padded point p copies zipped node copy_src[p]
+ * (0xFFFFFFFF: not a copy), or, for the rows interp_dst[r], takes
+ * interp_ref[r]; zipped node d reads padded point zip_src[d].  A maintainer
+ * builds the operator once per mesh from ot::Mesh's maps. */
 typedef struct dgb_unzip_plan dgb_unzip_plan;
 dgb_status dgb_unzip_plan_create(uint64_t ndof, uint64_t unzipped_size, const uint32_t *copy_src,
                                  uint64_t ninterp, const uint64_t *interp_dst,
-                                 const uint64_t *interp_ptr, const uint32_t *interp_col,
-                                 const double *interp_w, const uint64_t *zip_src,
+                                 const uint64_t *interp_ref, uint64_t nsrc,
+                                 const uint64_t *src_refs, uint64_t nlevels,
+                                 const uint64_t *level_ptr, const uint64_t *zip_src,
                                  dgb_unzip_plan **plan);
 dgb_status dgb_unzip_plan_destroy(dgb_unzip_plan *plan);
 /* Replaces ot::Mesh::unzip(const T* in, T* out, unsigned dof) for nvars

@@ -15,18 +15,59 @@ def mesh(dgb):
     return dgb.Mesh(dgb.mesh_params(max_level=6, min_level=3, fine_radius=1.0))
 
 
+def _lagrange_table():
+    t = np.zeros((6, 7))
+    for r in range(6):
+        xi = r + 0.5
+        for i in range(7):
+            num = den = 1.0
+            for m in range(7):
+                if m != i:
+                    num *= xi - m
+                    den *= i - m
+            t[r, i] = num / den
+    return t
+
+
+LAG = _lagrange_table()
+
+
+def _ref_values(refs, z, dg):
+    """Values of 64-bit node references (copy or separable interpolation)."""
+    out = np.empty(len(refs))
+    interp = (refs >> np.uint64(63)) != 0
+    out[~interp] = z[(refs[~interp] & np.uint64(0xFFFFFFFF)).astype(np.int64)]
+    r = refs[interp]
+    if len(r):
+        src = ((r >> np.uint64(12)) & np.uint64(0x7FFFFFFF)).astype(np.int64)
+        W = []
+        for a in range(3):
+            code = ((r >> np.uint64(4 * a)) & np.uint64(0xF)).astype(np.int64)
+            w = np.zeros((len(r), 7))
+            even = code % 2 == 0
+            w[np.nonzero(even)[0], code[even] // 2] = 1.0
+            w[~even] = LAG[code[~even] // 2]
+            W.append(w)
+        E = dg[src].reshape(len(r), 7, 7, 7)  # [k][j][i]
+        out[interp] = np.einsum("nk,nj,ni,nkji->n", W[2], W[1], W[0], E)
+    return out
+
+
 def apply_unzip(op, z, n):
-    """Host application of the unzip operator (the oracle for the GPU kernels)."""
+    """Host application of the unzip operator (the oracle for the GPU kernels):
+    source elements level by level, then copies, then interpolated points."""
+    lp = op["level_ptr"].astype(np.int64)
+    nsrc = len(op["src_refs"]) // 343
+    dg = np.zeros((nsrc, 343))
+    for l in range(len(lp) - 1):
+        a, b = lp[l], lp[l + 1]
+        dg[a:b] = _ref_values(op["src_refs"][a * 343:b * 343], z, dg).reshape(b - a, 343)
     out = np.full(n, np.nan)
     cp = op["copy_src"]
     m = cp != 0xFFFFFFFF
     out[m] = z[cp[m]]
     if len(op["interp_dst"]):
-        ptr = op["interp_ptr"].astype(np.int64)
-        prod = op["interp_w"] * z[op["interp_col"]]
-        sums = np.add.reduceat(prod, ptr[:-1]) if len(prod) else np.zeros(0)
-        sums[ptr[1:] == ptr[:-1]] = 0.0
-        out[op["interp_dst"].astype(np.int64)] = sums
+        out[op["interp_dst"].astype(np.int64)] = _ref_values(op["interp_ref"], z, dg)
     return out
 
 
@@ -84,7 +125,8 @@ def test_blocks_cover_leaves(dgb, mesh):
     for b in mesh.blocks:
         h = (b.ptmax[0] - b.ptmin[0]) / (b.sz[0] - 1)
         vol += ((b.sz[0] - 7) * h) ** 3
-        assert (b.sz[0] - 7) % 6 == 0 and b.sz[0] in (13, 19, 31, 61)
+        # p * 2^k + 1 + 6 points per side for 2^k leaves (src/block.cpp:50)
+        assert b.sz[0] in (13, 19, 31, 55)
         assert b.sz[0] == b.sz[1] == b.sz[2]
     assert vol == pytest.approx(64.0 ** 3, rel=1e-12)
     # the synthetic fields are finite on every block and the layout is contiguous
@@ -127,8 +169,17 @@ def test_zip_of_unzip_is_identity(mesh):
     assert np.array_equal(u[op["zip_src"].astype(np.int64)], z)
 
 
-def test_operator_rows_are_partitions_of_unity(mesh):
+def test_operator_sources_read_only_coarser_levels(mesh):
     op = mesh.operator()
-    ptr = op["interp_ptr"].astype(np.int64)
-    sums = np.add.reduceat(op["interp_w"], ptr[:-1])
-    assert np.allclose(sums, 1.0, atol=1e-12)
+    lp = op["level_ptr"].astype(np.int64)
+    assert lp[0] == 0 and lp[-1] == len(op["src_refs"]) // 343
+    for l in range(len(lp) - 1):
+        refs = op["src_refs"][lp[l] * 343:lp[l + 1] * 343]
+        interp = (refs >> np.uint64(63)) != 0
+        src = (refs[interp] >> np.uint64(12)) & np.uint64(0x7FFFFFFF)
+        assert np.all(src < lp[l])
+        for a in range(3):
+            assert np.all(((refs[interp] >> np.uint64(4 * a)) & np.uint64(0xF)) <= 12)
+    # every padded interpolation names an existing source
+    src = (op["interp_ref"] >> np.uint64(12)) & np.uint64(0x7FFFFFFF)
+    assert np.all(src < lp[-1])
