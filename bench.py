@@ -167,7 +167,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--workload", default="uneven20k", choices=["uneven20k", "uniform512"])
+    ap.add_argument("--workload", default="uneven20k",
+                    choices=["uneven20k", "uniform512", "octree_rk4"])
+    ap.add_argument("--fine-radius", type=float, default=1.0,
+                    help="octree_rk4: radius of the finest level around each puncture")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", action="store_true")
@@ -177,6 +180,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dgb = load_dgb()
+    if args.workload == "octree_rk4":
+        return main_octree(args, dgb, rank, world, local)
     blocks, seed, sigma = workload(dgb, args.workload)
     npts = interior_points(blocks)
     units = npts * 24
@@ -298,6 +303,165 @@ def main():
                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                "gpu_launches": args.steps, "impl": "ours"}
         print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def octree_params(dgb, fine_radius):
+    """2:1-balanced octree on [-32,32]^3: level 10 within fine_radius of each
+    puncture, one level coarser per doubling of the distance, down to level 4;
+    blocks of up to 8^3 leaves."""
+    return dgb.mesh_params(max_level=10, min_level=4, fine_radius=fine_radius)
+
+
+def cpu_rk4_baseline(dgb, seed, sigma, steps=1):
+    """Oracle port of the reference RK4 step (unzip, bssnrhs per block with
+    OpenMP, zip, stage update + constraint closure) on a sample octree (levels
+    4-8, the same refinement rule) on all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    ora = oracle_py.Oracle()
+    cores = os.cpu_count() or 1
+    m = dgb.Mesh(dgb.mesh_params(max_level=8, min_level=4, fine_radius=1.0))
+    op = m.operator()
+    xyz = m.dof_coords()
+    state = [np.zeros(m.ndof) for _ in range(24)]
+    dgb.synth_fill_points(xyz, state, seed, 1e-6)
+    prm = dgb.params_vector(dgb.default_params(sigma))
+    dt = 0.25 * 64.0 / (2 ** 8 * 6)
+    vals = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        state = oracle_py.rk4_step_pipeline(ora, m.blocks, op, m.nunzipped, state, dt, prm,
+                                            nthreads=cores)
+        vals.append(m.ndof * 24 / (time.perf_counter() - t0))
+    return {"value": float(np.median(vals)), "unit": "grid-pts*vars/s", "cores": cores,
+            "kind": "port",
+            "sample": f"octree levels 4-8 ({m.num_leaves} leaves, {m.ndof} independent nodes, "
+                      f"{m.nblocks} blocks), one full RK4 step: host unzip, bssnrhs per block "
+                      f"(OpenMP), zip, stage updates"}, vals
+
+
+def main_octree(args, dgb, rank, world, local):
+    sigma, seed = 0.4, 20261203 + 3
+    t0 = time.perf_counter()
+    mesh = dgb.Mesh(octree_params(dgb, args.fine_radius))
+    t_mesh = time.perf_counter() - t0
+    n_int = sum((b.sz[0] - 6) * (b.sz[1] - 6) * (b.sz[2] - 6) for b in mesh.blocks)
+    units = mesh.ndof * 24
+    dx_min = 64.0 / (2 ** 10 * 6)
+    dt = 0.25 * dx_min
+    wl = {"workload": f"octree_rk4: 2:1-balanced octree on [-32,32]^3, level 10 within "
+                      f"r<{args.fine_radius} of each puncture, coarsening to level 4; "
+                      f"{mesh.num_leaves} leaves, {mesh.nblocks} blocks, "
+                      f"{mesh.ndof} independent nodes",
+          "step": "one RK4 step = 4 x (unzip -> bssnRHS+KO+BCs -> zip -> stage update), "
+                  "one CUDA graph",
+          "units": "independent nodes x 24 vars per RK4 step", "ko_sigma": sigma,
+          "dt": dt, "cfl": 0.25, "padded_points": mesh.nunzipped, "interior_points": n_int,
+          "mesh_build_s": round(t_mesh, 2), "precision": args.precision,
+          "l2": "fields (6.6 GB zipped, 18 GB unzipped per set) larger than L2"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        base, vals = cpu_rk4_baseline(dgb, seed, sigma, steps=max(1, args.steps))
+        v = base["value"]
+        print(json.dumps({"metric": METRIC, "value": v, "unit": "grid-pts*vars/s", "n_gpus": 1,
+                          "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": units / v * 1e3, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": wl, "impl": "reference",
+                          "cpu_baseline": base,
+                          "e2e": {"value": v, "unit": "grid-pts*vars/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    import torch
+    if world > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dgb.init(local)
+    prec = dgb.PREC_MIXED if args.precision == "mixed" else dgb.PREC_FP64
+    op = mesh.operator()
+    plan = dgb.Plan(mesh.blocks, dgb.default_params(sigma))
+    if args.autotune:
+        tu = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(24)]
+        tr = [torch.zeros_like(tu[0]) for _ in range(24)]
+        plan.synth_fill_device([t.data_ptr() for t in tu], seed, 1e-6)
+        plan.autotune([t.data_ptr() for t in tr], [t.data_ptr() for t in tu], prec)
+        wl["tile"] = plan.tile(prec)
+        del tu, tr
+        torch.cuda.empty_cache()
+    uz = dgb.UnzipPlan(op, mesh.ndof)
+    st = dgb.Stepper(plan, uz, prec)
+    xyz = mesh.dof_coords()
+    host = [np.empty(mesh.ndof) for _ in range(24)]
+    dgb.synth_fill_points(xyz, host, seed, 1e-6)
+    ds = [torch.from_numpy(a).to(dev) for a in host]
+    ptrs = [t.data_ptr() for t in ds]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    st.step(ptrs, dt, nsteps=args.warmup, stream=sh)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    st.step(ptrs, dt, nsteps=args.steps, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = units * world / (ms * 1e-3)
+    fp64_gflops, _ = dgb.measure_fp64_peak()
+    achieved = 4 * n_int * FLOP_PER_POINT / (ms * 1e-3) / 1e9
+    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
+            "frac": achieved / fp64_gflops, "traffic": None,
+            "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
+            "flop_per_point": FLOP_PER_POINT,
+            "note": "4 RHS evaluations per step over all block interior points; unzip, zip "
+                    "and the stage updates are not counted"}
+    e2e = None
+    if not args.no_e2e:
+        k = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(k):
+            for v in range(24):
+                ds[v].copy_(torch.from_numpy(host[v]))
+            st.step(ptrs, dt, nsteps=1, stream=sh)
+            for v in range(24):
+                host[v][:] = ds[v].cpu().numpy()
+        torch.cuda.synchronize(dev)
+        e2e_s = (time.perf_counter() - t0) / k
+        e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
+               "h2d_bytes_per_step": 24 * mesh.ndof * 8, "d2h_bytes_per_step": 24 * mesh.ndof * 8,
+               "ms_per_step": e2e_s * 1e3,
+               "path": "state in host arrays: H2D, dgb_rk4_step, D2H every step"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu, _ = cpu_rk4_baseline(dgb, seed, sigma)
+    launches_per_step = 4 * (mesh.nlevels + 2 + 1 + 1 + 1)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": "grid-pts*vars/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None,
+                          "dtype": "f64" if prec == dgb.PREC_FP64 else "f64 (FP32 stencils/KO)",
+                          "data": "synthetic (seeded Brill-Lindquist + 1e-6 noise)",
+                          "config": wl, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                          "clocks": clocks, "gpu_launches": launches_per_step * args.steps,
+                          "impl": "ours"}))
+    st.close()
+    uz.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

@@ -112,20 +112,62 @@ __global__ void __launch_bounds__(256) unzip_copy_kernel(const FieldPtrs f, cons
     }
 }
 
-struct InterpArgs {
+// Interpolated padded points grouped by source element: one CTA refines a
+// source element onto its 13^3 half-lattice (codes 0..12 per axis) with three
+// separable passes in shared memory (x, then y, then z: the same operations
+// in the same order as ref_value, so the values are bit-identical), then
+// scatters the rows of that source.
+struct GroupArgs {
     FieldPtrs f;
     const double *dg[NV];
-    const uint64_t *dst, *ref;
-    uint64_t nrows;
+    const uint64_t *gptr;   // nsrc + 1
+    const uint64_t *gdst;   // destinations grouped by source
+    const uint16_t *gcode;  // cx + 13 * (cy + 13 * cz)
+    uint64_t nsrc;
     LagTable T;
 };
 
-__global__ void __launch_bounds__(128) unzip_interp_kernel(const InterpArgs a)
+__device__ __forceinline__ double pass1(const double *in, int code, int stride, const LagTable &T)
 {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < a.nrows; r += stride) {
-        const uint64_t d = __ldg(a.dst + r), ref = __ldg(a.ref + r);
-        for (int v = 0; v < a.f.nvars; v++) a.f.out[v][d] = ref_value(ref, a.f.in[v], a.dg[v], a.T);
+    if ((code & 1) == 0) return in[(code >> 1) * stride];
+    const double *w = T.w[code >> 1];
+    double acc = 0.0;
+#pragma unroll
+    for (int a = 0; a < 7; a++) acc = fma(w[a], in[a * stride], acc);
+    return acc;
+}
+
+__global__ void __launch_bounds__(256) unzip_group_kernel(const GroupArgs a)
+{
+    __shared__ double e[kNpe];            // [k][j][i]
+    __shared__ double A[7 * 7 * 13];      // [k][j][cx]
+    __shared__ double B[7 * 13 * 13];     // [k][cy][cx]
+    __shared__ double Cc[13 * 13 * 13];   // [cz][cy][cx]
+    for (uint64_t s = blockIdx.x; s < a.nsrc; s += gridDim.x) {
+        const uint64_t r0 = a.gptr[s], r1 = a.gptr[s + 1];
+        if (r0 == r1) continue;
+        for (int v = 0; v < a.f.nvars; v++) {
+            __syncthreads();
+            for (int t = threadIdx.x; t < kNpe; t += blockDim.x) e[t] = a.dg[v][s * kNpe + t];
+            __syncthreads();
+            for (int t = threadIdx.x; t < 7 * 7 * 13; t += blockDim.x) {
+                const int cx = t % 13, jk = t / 13;
+                A[t] = pass1(e + 7 * jk, cx, 1, a.T);
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < 7 * 13 * 13; t += blockDim.x) {
+                const int cx = t % 13, cy = (t / 13) % 13, k = t / 169;
+                B[t] = pass1(A + (k * 7) * 13 + cx, cy, 13, a.T);
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < 13 * 13 * 13; t += blockDim.x) {
+                const int cxy = t % 169, cz = t / 169;
+                Cc[t] = pass1(B + cxy, cz, 169, a.T);
+            }
+            __syncthreads();
+            for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
+                a.f.out[v][a.gdst[r]] = Cc[a.gcode[r]];
+        }
     }
 }
 
@@ -180,7 +222,9 @@ struct dgb_unzip_plan {
     uint64_t ndof = 0, nunz = 0, ninterp = 0, nsrc = 0;
     std::vector<uint64_t> level_ptr;
     uint32_t *d_copy = nullptr;
-    uint64_t *d_idst = nullptr, *d_iref = nullptr, *d_srefs = nullptr, *d_zip = nullptr;
+    uint64_t *d_srefs = nullptr, *d_zip = nullptr;
+    uint64_t *d_gptr = nullptr, *d_gdst = nullptr;  // interpolated rows grouped by source
+    uint16_t *d_gcode = nullptr;
     double *d_dg = nullptr;  // nsrc * 343 * 24 source nodal values
     LagTable T;
 };
@@ -242,14 +286,19 @@ dgb_status do_unzip(dgb_unzip_plan *p, const double *const *zipped, double *cons
         DGB_CUDA(cudaGetLastError());
     }
     if (p->ninterp) {
-        InterpArgs a;
+        GroupArgs a;
         a.f = f;
         for (int v = 0; v < NV; v++) a.dg[v] = dg[v];
-        a.dst = p->d_idst;
-        a.ref = p->d_iref;
-        a.nrows = p->ninterp;
+        a.gptr = p->d_gptr;
+        a.gdst = p->d_gdst;
+        a.gcode = p->d_gcode;
+        a.nsrc = p->nsrc;
         a.T = p->T;
-        unzip_interp_kernel<<<grid_for(p->ninterp, 128), 128, 0, st>>>(a);
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        const uint64_t grid = p->nsrc < (uint64_t)nsm * 8 ? p->nsrc : (uint64_t)nsm * 8;
+        unzip_group_kernel<<<(unsigned)grid, 256, 0, st>>>(a);
         DGB_CUDA(cudaGetLastError());
     }
     return DGB_OK;
@@ -374,10 +423,26 @@ dgb_status dgb_unzip_plan_create(uint64_t ndof, uint64_t unzipped_size, const ui
     };
     up((void **)&p->d_copy, copy_src, unzipped_size * 4);
     up((void **)&p->d_zip, zip_src, ndof * 8);
-    up((void **)&p->d_idst, interp_dst, ninterp * 8);
-    up((void **)&p->d_iref, interp_ref, ninterp * 8);
     up((void **)&p->d_srefs, src_refs, nsrc * kNpe * 8);
     if (e == cudaSuccess && nsrc) e = cudaMalloc(&p->d_dg, nsrc * kNpe * NV * sizeof(double));
+    if (ninterp) {
+        // group the interpolated rows by source element (counting sort)
+        std::vector<uint64_t> gptr(nsrc + 1, 0), gdst(ninterp);
+        std::vector<uint16_t> gcode(ninterp);
+        for (uint64_t r = 0; r < ninterp; r++) gptr[((interp_ref[r] >> 12) & 0x7FFFFFFFull) + 1]++;
+        for (uint64_t s = 0; s < nsrc; s++) gptr[s + 1] += gptr[s];
+        std::vector<uint64_t> fill(gptr.begin(), gptr.end() - 1);
+        for (uint64_t r = 0; r < ninterp; r++) {
+            const uint64_t ref = interp_ref[r];
+            const uint64_t s = (ref >> 12) & 0x7FFFFFFFull;
+            const uint64_t q = fill[s]++;
+            gdst[q] = interp_dst[r];
+            gcode[q] = (uint16_t)((ref & 0xF) + 13 * (((ref >> 4) & 0xF) + 13 * ((ref >> 8) & 0xF)));
+        }
+        up((void **)&p->d_gptr, gptr.data(), gptr.size() * 8);
+        up((void **)&p->d_gdst, gdst.data(), gdst.size() * 8);
+        up((void **)&p->d_gcode, gcode.data(), gcode.size() * 2);
+    }
     if (e != cudaSuccess) {
         set_error(std::string("dgb_unzip_plan_create: ") + cudaGetErrorString(e));
         dgb_unzip_plan_destroy(p);
@@ -392,10 +457,11 @@ dgb_status dgb_unzip_plan_destroy(dgb_unzip_plan *p)
     if (!p) return DGB_OK;
     cudaFree(p->d_copy);
     cudaFree(p->d_zip);
-    cudaFree(p->d_idst);
-    cudaFree(p->d_iref);
     cudaFree(p->d_srefs);
     cudaFree(p->d_dg);
+    cudaFree(p->d_gptr);
+    cudaFree(p->d_gdst);
+    cudaFree(p->d_gcode);
     delete p;
     return DGB_OK;
 }

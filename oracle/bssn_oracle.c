@@ -641,3 +641,82 @@ void orc_rk4_stage(int s, double **dst, const double **prev, const double ***k,
         orc_enforce_bssn_constraints(dst, node, chi_floor);
     }
 }
+
+/* ---------------- Mesh::unzip / Mesh::zip from the operator ---------------- */
+/* The restatement of include/mesh.tcc:7436-8690 used by the checker and the
+ * CPU baseline: source elements' nodal values level by level (hanging nodes
+ * interpolated from coarser sources, getElementNodalValues mesh.tcc:2467),
+ * then copies and separable degree-6 interpolations of the padded points
+ * (parent2ChildInterpolation, FEM/include/refel.h:249-296).  Reference word:
+ * bit 63 clear = zipped node (low 32 bits); set = source (bits 12..42) at
+ * codes 2*xi (bits 0..11). */
+static double orc_lag[6][7];
+static void orc_lag_init(void)
+{
+    for (int r = 0; r < 6; r++)
+        for (int i = 0; i < 7; i++) {
+            double num = 1.0, den = 1.0;
+            for (int m = 0; m < 7; m++)
+                if (m != i) { num *= (r + 0.5) - m; den *= (double)(i - m); }
+            orc_lag[r][i] = num / den;
+        }
+}
+
+static double orc_ref_value(unsigned long long ref, const double *z, const double *dg)
+{
+    if (!(ref >> 63)) return z[(unsigned)(ref & 0xFFFFFFFFull)];
+    const unsigned long long src = (ref >> 12) & 0x7FFFFFFFull;
+    double w[3][7];
+    int idx[3][7], n[3];
+    for (int a = 0; a < 3; a++) {
+        const int code = (int)((ref >> (4 * a)) & 0xF);
+        if ((code & 1) == 0) { n[a] = 1; w[a][0] = 1.0; idx[a][0] = code >> 1; }
+        else { n[a] = 7; for (int i = 0; i < 7; i++) { w[a][i] = orc_lag[code >> 1][i]; idx[a][i] = i; } }
+    }
+    const double *e = dg + src * 343;
+    double acc = 0.0;
+    for (int c = 0; c < n[2]; c++) {
+        double accy = 0.0;
+        for (int b = 0; b < n[1]; b++) {
+            double accx = 0.0;
+            for (int q = 0; q < n[0]; q++) accx += w[0][q] * e[idx[0][q] + 7 * (idx[1][b] + 7 * idx[2][c])];
+            accy += w[1][b] * accx;
+        }
+        acc += w[2][c] * accy;
+    }
+    return acc;
+}
+
+/* zipped -> unzipped for one field; dg is scratch of nsrc*343 doubles.
+ * Padded points that are neither copies nor interpolation rows are left
+ * untouched. */
+void orc_unzip(const double *z, double *u, unsigned long long nunz, const unsigned *copy_src,
+               unsigned long long ninterp, const unsigned long long *interp_dst,
+               const unsigned long long *interp_ref, unsigned long long nlevels,
+               const unsigned long long *level_ptr, const unsigned long long *src_refs,
+               double *dg, int nthreads)
+{
+    static int init = 0;
+    if (!init) { orc_lag_init(); init = 1; }
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+    (void)nthreads;
+    for (unsigned long long l = 0; l < nlevels; l++) {
+        const long long a = (long long)(level_ptr[l] * 343), b = (long long)(level_ptr[l + 1] * 343);
+#pragma omp parallel for schedule(static)
+        for (long long t = a; t < b; t++) dg[t] = orc_ref_value(src_refs[t], z, dg);
+    }
+#pragma omp parallel for schedule(static)
+    for (long long p = 0; p < (long long)nunz; p++)
+        if (copy_src[p] != 0xFFFFFFFFu) u[p] = z[copy_src[p]];
+#pragma omp parallel for schedule(static)
+    for (long long r = 0; r < (long long)ninterp; r++)
+        u[interp_dst[r]] = orc_ref_value(interp_ref[r], z, dg);
+}
+
+void orc_zip(const double *u, double *z, unsigned long long ndof, const unsigned long long *zip_src)
+{
+#pragma omp parallel for schedule(static)
+    for (long long d = 0; d < (long long)ndof; d++) z[d] = u[zip_src[d]];
+}

@@ -53,6 +53,12 @@ class Oracle:
         L.orc_rk4_stage.restype = None
         L.orc_rk4_stage.argtypes = [C.c_int, _PP, _PP, C.POINTER(_PP), C.c_size_t, C.c_double,
                                     C.c_double]
+        L.orc_unzip.restype = None
+        L.orc_unzip.argtypes = [C.c_void_p, C.c_void_p, C.c_ulonglong, C.c_void_p, C.c_ulonglong,
+                                C.c_void_p, C.c_void_p, C.c_ulonglong, C.c_void_p, C.c_void_p,
+                                C.c_void_p, C.c_int]
+        L.orc_zip.restype = None
+        L.orc_zip.argtypes = [C.c_void_p, C.c_void_p, C.c_ulonglong, C.c_void_p]
         L.orc_enforce_bssn_constraints.restype = None
         L.orc_enforce_bssn_constraints.argtypes = [_PP, C.c_size_t, C.c_double]
         for nm in ("orc_deriv64", "orc_deriv64_2", "orc_ko42"):
@@ -153,3 +159,112 @@ class Reference:
     def enforce(self, fields, node, chi_floor):
         pp, k = _ptrs(fields)
         self.L.ref_enforce_bssn_constraints(pp, node, chi_floor)
+
+
+# ----------------------------------------------------------------------------
+# Host application of a mesh's unzip / zip operator and the RK4 step pipeline
+# (RK_BSSN::performSingleIteration's RK4 branch, BSSN_GR/src/rkBSSN.cpp:803-1012):
+# the checker for the GPU unzip, zip and graph-captured step.
+
+def _lagrange_table():
+    t = np.zeros((6, 7))
+    for r in range(6):
+        xi = r + 0.5
+        for i in range(7):
+            num = den = 1.0
+            for m in range(7):
+                if m != i:
+                    num *= xi - m
+                    den *= i - m
+            t[r, i] = num / den
+    return t
+
+
+LAG = _lagrange_table()
+
+
+def _ref_values(refs, z, dg, chunk=65536):
+    """Values of 64-bit node references: bit 63 clear = copy of zipped node
+    (low 32 bits); set = separable degree-6 interpolation of source element
+    (bits 12..42) at codes 2*xi (bits 0..11, 4 per axis)."""
+    out = np.empty(len(refs))
+    interp = (refs >> np.uint64(63)) != 0
+    out[~interp] = z[(refs[~interp] & np.uint64(0xFFFFFFFF)).astype(np.int64)]
+    idx = np.nonzero(interp)[0]
+    for c0 in range(0, len(idx), chunk):
+        sel = idx[c0:c0 + chunk]
+        r = refs[sel]
+        src = ((r >> np.uint64(12)) & np.uint64(0x7FFFFFFF)).astype(np.int64)
+        W = []
+        for a in range(3):
+            code = ((r >> np.uint64(4 * a)) & np.uint64(0xF)).astype(np.int64)
+            w = np.zeros((len(r), 7))
+            even = code % 2 == 0
+            w[np.nonzero(even)[0], code[even] // 2] = 1.0
+            w[~even] = LAG[code[~even] // 2]
+            W.append(w)
+        E = dg[src].reshape(len(r), 7, 7, 7)  # [k][j][i]
+        out[sel] = np.einsum("nk,nj,ni,nkji->n", W[2], W[1], W[0], E)
+    return out
+
+
+_ORC = None
+
+
+def _default_oracle():
+    global _ORC
+    if _ORC is None:
+        _ORC = Oracle()
+    return _ORC
+
+
+def unzip_apply(op, z, n, oracle=None, nthreads=0):
+    """Mesh::unzip on the host from the operator (oracle/bssn_oracle.c
+    orc_unzip); NaN where nothing is written (padding beyond domain faces)."""
+    ora = oracle or _default_oracle()
+    out = np.full(n, np.nan)
+    nsrc = len(op["src_refs"]) // 343
+    dg = np.zeros(max(nsrc * 343, 1))
+    nlev = max(len(op["level_ptr"]) - 1, 0)
+    ora.L.orc_unzip(np.ascontiguousarray(z).ctypes.data, out.ctypes.data, n,
+                    op["copy_src"].ctypes.data, len(op["interp_dst"]), op["interp_dst"].ctypes.data,
+                    op["interp_ref"].ctypes.data, nlev, op["level_ptr"].ctypes.data,
+                    op["src_refs"].ctypes.data, dg.ctypes.data, nthreads)
+    return out
+
+
+def unzip_apply_numpy(op, z, n):
+    """Same operator applied with numpy (an independent second restatement)."""
+    lp = op["level_ptr"].astype(np.int64)
+    nsrc = len(op["src_refs"]) // 343
+    dg = np.zeros((nsrc, 343))
+    for l in range(len(lp) - 1):
+        a, b = lp[l], lp[l + 1]
+        dg[a:b] = _ref_values(op["src_refs"][a * 343:b * 343], z, dg).reshape(b - a, 343)
+    out = np.full(n, np.nan)
+    cp = op["copy_src"]
+    m = cp != 0xFFFFFFFF
+    out[m] = z[cp[m]]
+    if len(op["interp_dst"]):
+        out[op["interp_dst"].astype(np.int64)] = _ref_values(op["interp_ref"], z, dg)
+    return out
+
+
+def rk4_step_pipeline(oracle, blocks, op, nunzipped, state, dt, prm, chi_floor=1e-4, nthreads=0):
+    """One RK4 step: for each stage unzip -> bssnrhs per block -> zip -> stage
+    update with enforce_bssn_constraints.  Returns the new state."""
+    prev = state
+    ks, im = [], prev
+    zs = op["zip_src"].astype(np.int64)
+    ndof = len(state[0])
+    for s in range(4):
+        src = prev if s == 0 else im
+        U = [np.nan_to_num(unzip_apply(op, src[v], nunzipped, oracle, nthreads), nan=0.0)
+             for v in range(24)]
+        R = [np.zeros(nunzipped) for _ in range(24)]
+        assert oracle.bssnrhs_blocks(R, U, blocks, prm, nthreads) == 0
+        ks.append([R[v][zs] for v in range(24)])
+        dst = [np.zeros(ndof) for _ in range(24)]
+        oracle.rk4_stage(s, dst, prev, ks, dt, chi_floor)
+        im = dst
+    return im

@@ -24,20 +24,9 @@ def mesh_state(dgb, mesh, seed=7):
 
 
 def oracle_step(dgb, oracle, mesh, op, state, dt, sigma):
+    import oracle_py
     prm = dgb.params_vector(dgb.default_params(sigma))
-    prev = state
-    ks, im = [], prev
-    zs = op["zip_src"].astype(np.int64)
-    for s in range(4):
-        src = prev if s == 0 else im
-        U = [np.nan_to_num(apply_unzip(op, src[v], mesh.nunzipped), nan=0.0) for v in range(24)]
-        R = [np.zeros(mesh.nunzipped) for _ in range(24)]
-        assert oracle.bssnrhs_blocks(R, U, mesh.blocks, prm) == 0
-        ks.append([R[v][zs] for v in range(24)])
-        dst = [np.zeros(mesh.ndof) for _ in range(24)]
-        oracle.rk4_stage(s, dst, prev, ks, dt, 1e-4)
-        im = dst
-    return im
+    return oracle_py.rk4_step_pipeline(oracle, mesh.blocks, op, mesh.nunzipped, state, dt, prm)
 
 
 def test_unzip_zip_match_host_operator(dgb, gpu, small_mesh):

@@ -15,60 +15,7 @@ def mesh(dgb):
     return dgb.Mesh(dgb.mesh_params(max_level=6, min_level=3, fine_radius=1.0))
 
 
-def _lagrange_table():
-    t = np.zeros((6, 7))
-    for r in range(6):
-        xi = r + 0.5
-        for i in range(7):
-            num = den = 1.0
-            for m in range(7):
-                if m != i:
-                    num *= xi - m
-                    den *= i - m
-            t[r, i] = num / den
-    return t
-
-
-LAG = _lagrange_table()
-
-
-def _ref_values(refs, z, dg):
-    """Values of 64-bit node references (copy or separable interpolation)."""
-    out = np.empty(len(refs))
-    interp = (refs >> np.uint64(63)) != 0
-    out[~interp] = z[(refs[~interp] & np.uint64(0xFFFFFFFF)).astype(np.int64)]
-    r = refs[interp]
-    if len(r):
-        src = ((r >> np.uint64(12)) & np.uint64(0x7FFFFFFF)).astype(np.int64)
-        W = []
-        for a in range(3):
-            code = ((r >> np.uint64(4 * a)) & np.uint64(0xF)).astype(np.int64)
-            w = np.zeros((len(r), 7))
-            even = code % 2 == 0
-            w[np.nonzero(even)[0], code[even] // 2] = 1.0
-            w[~even] = LAG[code[~even] // 2]
-            W.append(w)
-        E = dg[src].reshape(len(r), 7, 7, 7)  # [k][j][i]
-        out[interp] = np.einsum("nk,nj,ni,nkji->n", W[2], W[1], W[0], E)
-    return out
-
-
-def apply_unzip(op, z, n):
-    """Host application of the unzip operator (the oracle for the GPU kernels):
-    source elements level by level, then copies, then interpolated points."""
-    lp = op["level_ptr"].astype(np.int64)
-    nsrc = len(op["src_refs"]) // 343
-    dg = np.zeros((nsrc, 343))
-    for l in range(len(lp) - 1):
-        a, b = lp[l], lp[l + 1]
-        dg[a:b] = _ref_values(op["src_refs"][a * 343:b * 343], z, dg).reshape(b - a, 343)
-    out = np.full(n, np.nan)
-    cp = op["copy_src"]
-    m = cp != 0xFFFFFFFF
-    out[m] = z[cp[m]]
-    if len(op["interp_dst"]):
-        out[op["interp_dst"].astype(np.int64)] = _ref_values(op["interp_ref"], z, dg)
-    return out
+from oracle_py import unzip_apply as apply_unzip  # noqa: E402  (host unzip: the checker)
 
 
 def padded_coords(blocks):
