@@ -61,7 +61,12 @@ class Oracle:
         L.orc_zip.argtypes = [C.c_void_p, C.c_void_p, C.c_ulonglong, C.c_void_p]
         L.orc_enforce_bssn_constraints.restype = None
         L.orc_enforce_bssn_constraints.argtypes = [_PP, C.c_size_t, C.c_double]
-        for nm in ("orc_deriv64", "orc_deriv64_2", "orc_ko42"):
+        L.orc_physcon_block.restype = C.c_int
+        L.orc_physcon_block.argtypes = [_PP, _PP, C.c_ulong, _D, _D, C.POINTER(C.c_uint), C.c_uint]
+        L.orc_physcon_blocks.restype = C.c_int
+        L.orc_physcon_blocks.argtypes = [_PP, _PP, C.c_long, C.POINTER(C.c_ulong),
+                                         C.POINTER(C.c_uint), C.POINTER(C.c_uint), _D, _D, C.c_int]
+        for nm in ("orc_deriv64", "orc_deriv64_2", "orc_ko42", "orc_deriv42", "orc_deriv42_2"):
             f = getattr(L, nm)
             f.restype = None
             f.argtypes = [C.c_int, _D, _D, C.c_double, C.POINTER(C.c_uint), C.c_uint]
@@ -84,12 +89,36 @@ class Oracle:
     def stencil(self, kind, dirn, u3, h, bflag=0):
         """kind in {'d1','d2','ko'} on a 3-D array u3[z][y][x]; returns D (zeros
         where the reference leaves the output untouched)."""
-        fn = {"d1": self.L.orc_deriv64, "d2": self.L.orc_deriv64_2, "ko": self.L.orc_ko42}[kind]
+        fn = {"d1": self.L.orc_deriv64, "d2": self.L.orc_deriv64_2, "ko": self.L.orc_ko42,
+              "d1_4": self.L.orc_deriv42, "d2_4": self.L.orc_deriv42_2}[kind]
         u = np.ascontiguousarray(u3, dtype=np.float64)
         D = np.zeros_like(u)
         sz = (C.c_uint * 3)(u.shape[2], u.shape[1], u.shape[0])
         fn(dirn, D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz, bflag)
         return D
+
+    def physcon_block(self, cons, u, block):
+        """physical_constraints on one block: cons = 6 arrays (ham, mom0-2,
+        psi4_real, psi4_img), written at the block's interior points."""
+        c, k1 = _ptrs(cons)
+        uu, k2 = _ptrs(u)
+        pmin = np.array(list(block.ptmin), dtype=np.float64)
+        pmax = np.array(list(block.ptmax), dtype=np.float64)
+        sz = (C.c_uint * 3)(*block.sz)
+        return self.L.orc_physcon_block(c, uu, block.offset, pmin.ctypes.data_as(_D),
+                                        pmax.ctypes.data_as(_D), sz, block.bflag)
+
+    def physcon_blocks(self, cons, u, blocks, nthreads=0):
+        n = len(blocks)
+        off = (C.c_ulong * n)(*[b.offset for b in blocks])
+        sz = (C.c_uint * (3 * n))(*[s for b in blocks for s in b.sz])
+        bf = (C.c_uint * n)(*[b.bflag for b in blocks])
+        pmin = np.array([x for b in blocks for x in b.ptmin], dtype=np.float64)
+        pmax = np.array([x for b in blocks for x in b.ptmax], dtype=np.float64)
+        c, k1 = _ptrs(cons)
+        uu, k2 = _ptrs(u)
+        return self.L.orc_physcon_blocks(c, uu, n, off, sz, bf, pmin.ctypes.data_as(_D),
+                                         pmax.ctypes.data_as(_D), nthreads)
 
     def bssnrhs_block(self, rhs, u, block, prm, apply_bcs=True):
         r, k1 = _ptrs(rhs)
@@ -128,9 +157,13 @@ class Reference:
         L.ref_bssnrhs.argtypes = [_PP, _PP, C.c_uint, _D, _D, C.POINTER(C.c_uint), C.c_uint, _D]
         L.ref_enforce_bssn_constraints.restype = None
         L.ref_enforce_bssn_constraints.argtypes = [_PP, C.c_uint, C.c_double]
+        L.ref_physical_constraints.restype = C.c_int
+        L.ref_physical_constraints.argtypes = [_PP, _PP, C.c_uint, _D, _D, C.POINTER(C.c_uint),
+                                               C.c_uint]
         for nm in ("ref_deriv64_x", "ref_deriv64_y", "ref_deriv64_z", "ref_deriv64_xx",
                    "ref_deriv64_yy", "ref_deriv64_zz", "ref_ko_deriv42_x", "ref_ko_deriv42_y",
-                   "ref_ko_deriv42_z"):
+                   "ref_ko_deriv42_z", "ref_deriv42_x", "ref_deriv42_y", "ref_deriv42_z",
+                   "ref_deriv42_xx", "ref_deriv42_yy", "ref_deriv42_zz"):
             f = getattr(L, nm)
             f.restype = None
             f.argtypes = [_D, _D, C.c_double, C.POINTER(C.c_uint), C.c_uint]
@@ -149,12 +182,23 @@ class Reference:
     def stencil(self, kind, dirn, u3, h, bflag=0):
         nm = {"d1": ["ref_deriv64_x", "ref_deriv64_y", "ref_deriv64_z"],
               "d2": ["ref_deriv64_xx", "ref_deriv64_yy", "ref_deriv64_zz"],
-              "ko": ["ref_ko_deriv42_x", "ref_ko_deriv42_y", "ref_ko_deriv42_z"]}[kind][dirn]
+              "ko": ["ref_ko_deriv42_x", "ref_ko_deriv42_y", "ref_ko_deriv42_z"],
+              "d1_4": ["ref_deriv42_x", "ref_deriv42_y", "ref_deriv42_z"],
+              "d2_4": ["ref_deriv42_xx", "ref_deriv42_yy", "ref_deriv42_zz"]}[kind][dirn]
         u = np.ascontiguousarray(u3, dtype=np.float64)
         D = np.zeros_like(u)
         sz = (C.c_uint * 3)(u.shape[2], u.shape[1], u.shape[0])
         getattr(self.L, nm)(D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz, bflag)
         return D
+
+    def physical_constraints(self, cons, u, block):
+        c, k1 = _ptrs(cons)
+        uu, k2 = _ptrs(u)
+        pmin = np.array(list(block.ptmin), dtype=np.float64)
+        pmax = np.array(list(block.ptmax), dtype=np.float64)
+        sz = (C.c_uint * 3)(*block.sz)
+        return self.L.ref_physical_constraints(c, uu, block.offset, pmin.ctypes.data_as(_D),
+                                               pmax.ctypes.data_as(_D), sz, block.bflag)
 
     def enforce(self, fields, node, chi_floor):
         pp, k = _ptrs(fields)

@@ -5,7 +5,9 @@ Runs only where the reference tree exists: oracle/Makefile.ref compiles the
 reference's sources (QuadGrav/src/derivs.cpp, the generated
 BSSN_GR/scripts/bssnrhs_*.h drivers and
 BSSN_GR/src/bssneqs_eta_const_standard_gauge.cpp inside the bssnrhs harness
-oracle/ref_bssnrhs.cpp, and BSSN_GR/src/bssn_constraints.cpp).
+oracle/ref_bssnrhs.cpp, BSSN_GR/src/bssn_constraints.cpp, and the constraint
+diagnostics BSSN_GR/scripts/constraint_derivs.h + BSSN_GR/src/physconeqs.cpp
+inside oracle/ref_physcon.cpp).
 
 Inputs come from the library's seeded synthetic generator (host fill); their
 SHA-256 is stored so that a change of the generator is detected.
@@ -97,6 +99,52 @@ def main():
         stencil_h=np.array(h), **{f"stencil_{k}": v for k, v in st.items()},
         enforce_in=np.stack(cs), enforce_out=np.stack(out), enforce_chi_floor=np.array(1e-4))
     print("wrote", os.path.join(HERE, "bssn_reference.npz"))
+    constraint_goldens(dgb, ref)
+
+
+def axis_block(dgb, blocks):
+    """First uniform block with interior points on the z axis (x = y = 0)."""
+    for i, b in enumerate(blocks):
+        h = [(b.ptmax[d] - b.ptmin[d]) / (b.sz[d] - 1) for d in range(3)]
+        ok = [any(abs(b.ptmin[d] + k * h[d]) <= 1e-7 for k in range(3, b.sz[d] - 3))
+              for d in (0, 1)]
+        if all(ok):
+            return i
+    raise RuntimeError("no block on the axis")
+
+
+def constraint_goldens(dgb, ref):
+    """physical_constraints (BSSN_GR/src/physcon.cpp) of the reference on the
+    puncture block, a generic block, a block on the z axis (the Psi4 guard)
+    and a domain-boundary corner block (one-sided 4th-order closures)."""
+    allb = dgb.synth_blocks(1)
+    picks = [(288, 0), (100, 0), (axis_block(dgb, allb), 0), (0, 1 | 4 | 16), (511, 2 | 8 | 32)]
+    rows, off = [], 0
+    for i, f in picks:
+        b = allb[i]
+        rows.append((off, tuple(b.sz), f, tuple(b.ptmin), tuple(b.ptmax)))
+        off += b.sz[0] * b.sz[1] * b.sz[2]
+    blocks = dgb.blocks_array(rows)
+    n = dgb.unzipped_size(blocks)
+    u = [np.zeros(n) for _ in range(24)]
+    dgb.synth_fill_host(blocks, u, SEED1, 1e-6)
+    c = [np.zeros(n) for _ in range(6)]
+    for b in blocks:
+        assert ref.physical_constraints(c, u, b) == 0
+    mask = interior_mask(blocks, n)
+    b0 = blocks[0]
+    sz = tuple(b0.sz)
+    chi = u[1][:sz[0] * sz[1] * sz[2]].reshape(sz[2], sz[1], sz[0])
+    h = (b0.ptmax[0] - b0.ptmin[0]) / (sz[0] - 1)
+    st = {}
+    for kind in ("d1_4", "d2_4"):
+        for d in range(3):
+            st[f"stencil_{kind}_{d}"] = ref.stencil(kind, d, chi, h, 0)[3:-3, 3:-3, 3:-3].copy()
+    np.savez_compressed(
+        os.path.join(HERE, "constraints_reference.npz"),
+        picks=np.array(picks), seed=np.array(SEED1), input_sha256=np.array(sha(u)),
+        cons=np.stack([x[mask] for x in c]), stencil_h=np.array(h), **st)
+    print("wrote", os.path.join(HERE, "constraints_reference.npz"))
 
 
 if __name__ == "__main__":
