@@ -51,6 +51,7 @@ struct dgb_plan {
     double *d_scratch = nullptr;
     size_t scratch_doubles = 0;
     int occupancy[8][2] = {};  // resident CTAs per SM per (variant, precision)
+    int pc_occupancy = 0;      // constraint kernel, resident CTAs per SM (0 = not yet known)
     // device copies for the host-array entry point
     double *d_u = nullptr, *d_rhs = nullptr;
 };
@@ -305,6 +306,88 @@ dgb_status dgb_plan_set_tile_variant(dgb_plan *p, int precision, int variant)
         return DGB_ERR_INVALID;
     }
     p->variant[precision == DGB_PREC_MIXED ? 1 : 0] = variant;
+    return DGB_OK;
+}
+
+dgb_status dgb_physical_constraints(dgb_plan *p, double *const *cons, const double *const *u,
+                                   void *stream)
+{
+    if (!p || !cons || !u) {
+        set_error("dgb_physical_constraints: null argument");
+        return DGB_ERR_INVALID;
+    }
+    for (int v = 0; v < NV; v++)
+        if (!u[v]) {
+            set_error("dgb_physical_constraints: null field pointer");
+            return DGB_ERR_INVALID;
+        }
+    for (int c = 0; c < DGB_NUM_CONSTRAINTS; c++)
+        if (!cons[c]) {
+            set_error("dgb_physical_constraints: null output pointer");
+            return DGB_ERR_INVALID;
+        }
+    dgb_status s = build_items(p, 0);  // the 8x8x8 schedule
+    if (s != DGB_OK) return s;
+    if (p->nitems[0] == 0) return DGB_OK;
+    if (p->pc_occupancy == 0) {
+        p->pc_occupancy = physcon_max_ctas_per_sm();
+        if (p->pc_occupancy < 1) {
+            set_error("dgb_physical_constraints: kernel cannot be resident");
+            return DGB_ERR_CUDA;
+        }
+    }
+    DGB_CUDA(physcon_configure());
+    const size_t fit = p->scratch_doubles / physcon_scratch_per_cta();
+    const int grid = (int)std::min<size_t>((size_t)p->nsm * p->pc_occupancy, fit);
+    PcArgs a;
+    for (int v = 0; v < NV; v++) a.u[v] = u[v];
+    for (int c = 0; c < DGB_NUM_CONSTRAINTS; c++) a.cons[c] = cons[c];
+    a.blocks = p->d_blocks;
+    a.items = p->d_items[0];
+    a.nitems = p->nitems[0];
+    a.queue = p->d_queue;
+    a.scratch = p->d_scratch;
+    cudaStream_t st = (cudaStream_t)stream;
+    DGB_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned int), st));
+    DGB_CUDA(physcon_launch(a, grid, st));
+    return DGB_OK;
+}
+
+dgb_status dgb_constraint_l2(const double *const *fields, int nvars, const double *mask,
+                             double threshold, uint64_t ndof, double *out, void *stream)
+{
+    if (!fields || !out || nvars < 1 || nvars > DGB_NUM_CONSTRAINTS) {
+        set_error("dgb_constraint_l2: bad argument");
+        return DGB_ERR_INVALID;
+    }
+    for (int v = 0; v < nvars; v++)
+        if (!fields[v]) {
+            set_error("dgb_constraint_l2: null field pointer");
+            return DGB_ERR_INVALID;
+        }
+    cudaStream_t st = (cudaStream_t)stream;
+    NormArgs a{};
+    for (int v = 0; v < nvars; v++) a.f[v] = fields[v];
+    a.nvars = nvars;
+    a.mask = mask;
+    a.threshold = threshold;
+    a.ndof = ndof;
+    const size_t np = (size_t)norm_partials() * (DGB_NUM_CONSTRAINTS + 1);
+    double *buf = nullptr;
+    DGB_CUDA(cudaMallocAsync(&buf, (np + DGB_NUM_CONSTRAINTS + 1) * sizeof(double), st));
+    a.partial = buf;
+    double res[DGB_NUM_CONSTRAINTS + 1];
+    cudaError_t e = l2_norm_launch(a, buf + np, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(res, buf + np, sizeof(res), cudaMemcpyDeviceToHost, st);
+    cudaError_t e2 = cudaFreeAsync(buf, st);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        set_error(std::string("dgb_constraint_l2: ") + cudaGetErrorString(e));
+        return DGB_ERR_CUDA;
+    }
+    for (int v = 0; v < nvars; v++) out[v] = res[v];
     return DGB_OK;
 }
 

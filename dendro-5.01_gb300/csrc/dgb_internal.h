@@ -72,6 +72,34 @@ cudaError_t synth_fill_launch(const DevBlock *blocks, uint32_t nblk, const uint6
                               uint64_t total, double *const *u, uint64_t seed, double noise,
                               cudaStream_t stream);
 
+// Constraint diagnostics (physcon.cu).
+struct PcArgs {
+    const double *u[NV];
+    double *cons[DGB_NUM_CONSTRAINTS];
+    const DevBlock *blocks;
+    const WorkItem *items;   // the 8x8x8 schedule (tile variant 0)
+    uint32_t nitems;
+    unsigned int *queue;
+    double *scratch;
+};
+size_t physcon_smem_bytes();
+size_t physcon_scratch_per_cta();  // doubles
+int physcon_threads();
+cudaError_t physcon_configure();
+int physcon_max_ctas_per_sm();
+cudaError_t physcon_launch(const PcArgs &args, int grid, cudaStream_t stream);
+
+struct NormArgs {
+    const double *f[DGB_NUM_CONSTRAINTS];
+    int nvars;
+    const double *mask;      // may be null: every node counts
+    double threshold;
+    uint64_t ndof;
+    double *partial;         // norm_partials() x (DGB_NUM_CONSTRAINTS + 1) doubles
+};
+int norm_partials();
+cudaError_t l2_norm_launch(const NormArgs &a, double *out_dev, cudaStream_t stream);
+
 void set_error(const std::string &msg);
 
 }  // namespace dgb

@@ -84,6 +84,9 @@ _SIGS = {
                                             C.POINTER(C.c_double), C.POINTER(C.c_uint32),
                                             C.c_uint32, C.POINTER(BssnParams), C.c_void_p]),
     "dgb_plan_autotune": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
+    "dgb_physical_constraints": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_void_p]),
+    "dgb_constraint_l2": (C.c_int, [PtrArr, C.c_int, C.c_void_p, C.c_double, C.c_uint64,
+                                    C.POINTER(C.c_double), C.c_void_p]),
     "dgb_plan_tile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint32)]),
     "dgb_num_tile_variants": (C.c_int, []),
     "dgb_plan_set_tile_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
@@ -227,6 +230,13 @@ class Plan:
         u, k2 = host_ptrs(u_arrays)
         check(lib().dgb_bssn_rhs_host(self.h, r, u, precision), "dgb_bssn_rhs_host")
 
+    def physical_constraints(self, cons_ptrs, u_ptrs, stream=0):
+        """ham, mom0-2, psi4_real, psi4_img at every block interior point."""
+        c, k1 = ptr_array(cons_ptrs)
+        u, k2 = ptr_array(u_ptrs)
+        check(lib().dgb_physical_constraints(self.h, c, u, C.c_void_p(stream)),
+              "dgb_physical_constraints")
+
     def autotune(self, rhs_ptrs, u_ptrs, precision=PREC_FP64, stream=0):
         r, k1 = ptr_array(rhs_ptrs)
         u, k2 = ptr_array(u_ptrs)
@@ -257,6 +267,18 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def constraint_l2(field_ptrs, ndof, mask_ptr=None, threshold=0.0, stream=0):
+    """Masked RMS of zipped device vectors (computeConstraintL2Norm)."""
+    out = (C.c_double * len(field_ptrs))()
+    f, keep = ptr_array(field_ptrs)
+    check(lib().dgb_constraint_l2(f, len(field_ptrs), mask_ptr, threshold,
+                                  ndof, out, C.c_void_p(stream)), "dgb_constraint_l2")
+    return list(out)
+
+
+CONSTRAINT_NAMES = ("ham", "mom0", "mom1", "mom2", "psi4_real", "psi4_img")
 
 
 def rk4_stage(stage, dst_ptrs, prev_ptrs, k_ptrs, nnodes, dt, chi_floor=1e-4, stream=0):

@@ -24,6 +24,9 @@ extern "C" {
 #endif
 
 #define DGB_NUM_VARS 24
+/* constraint diagnostics, bssn::VAR_CONSTRAINT order (BSSN_GR/include/grDef.h):
+ * ham, mom0, mom1, mom2, psi4_real, psi4_img */
+#define DGB_NUM_CONSTRAINTS 6
 
 typedef enum {
     DGB_OK = 0,
@@ -135,6 +138,24 @@ dgb_status dgb_plan_tile(const dgb_plan *plan, int precision, uint32_t *tile3);
 /* Compiled tile schedules: count, and explicit choice (bypasses autotune). */
 int dgb_num_tile_variants(void);
 dgb_status dgb_plan_set_tile_variant(dgb_plan *plan, int precision, int variant);
+
+/* Constraint diagnostics over every block of a plan, device pointers:
+ * replaces the per-block loop over physical_constraints (BSSN_GR/src/physcon.cpp:12-96,
+ * called from BSSN_GR/src/bssnCtx.cpp:332-355 and rkBSSN.cpp:1659).
+ * cons[0..5] = ham, mom0, mom1, mom2, psi4_real, psi4_img are written at each
+ * block's interior points (padding untouched) from the 24 unzipped fields
+ * u; 4th-order stencils with one-sided closures on flagged faces, FP64.
+ * Asynchronous on `stream`; shares the plan's work queue and workspace with
+ * dgb_bssn_rhs, so calls on one plan must be ordered on one stream. */
+dgb_status dgb_physical_constraints(dgb_plan *plan, double *const *cons, const double *const *u,
+                                    void *stream);
+/* Masked RMS of nvars (<= DGB_NUM_CONSTRAINTS) zipped device vectors of
+ * ndof values: sqrt(sum c^2 / count) over the nodes whose mask value is not
+ * below threshold (mask may be NULL: every node counts).  Replaces
+ * computeConstraintL2Norm (BSSN_GR/include/grUtils.tcc:40-88) on one rank.
+ * Deterministic reduction order; synchronises `stream`; out is host memory. */
+dgb_status dgb_constraint_l2(const double *const *fields, int nvars, const double *mask,
+                             double threshold, uint64_t ndof, double *out, void *stream);
 
 /* RK4 stage update on zipped (CG) vectors with the per-node constraint
  * closure, device pointers.  stage 0..2: dst = prev + U[s+1] dt k[s];
