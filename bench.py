@@ -168,9 +168,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="uneven20k",
-                    choices=["uneven20k", "uniform512", "octree_rk4"])
+                    choices=["uneven20k", "uniform512", "octree_rk4", "drift"])
     ap.add_argument("--fine-radius", type=float, default=1.0,
                     help="octree_rk4: radius of the finest level around each puncture")
+    ap.add_argument("--drift-steps", type=int, default=100,
+                    help="drift: RK4 steps per precision")
+    ap.add_argument("--drift-level", type=int, default=10,
+                    help="drift: finest octree level")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", action="store_true")
@@ -182,6 +186,10 @@ def main():
     dgb = load_dgb()
     if args.workload == "octree_rk4":
         return main_octree(args, dgb, rank, world, local)
+    if args.workload == "drift":
+        if args.impl == "reference" or rank != 0:
+            return
+        return main_drift(args, dgb)
     blocks, seed, sigma = workload(dgb, args.workload)
     npts = interior_points(blocks)
     units = npts * 24
@@ -464,6 +472,108 @@ def main_octree(args, dgb, rank, world, local):
     uz.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def constraint_norms(dgb, plan, uz, state_ptrs, U, Cu, Cz, ndof, stream):
+    """Masked L2 of ham, mom0-2 as the reference's solver reports them."""
+    return dgb.constraint_report(plan, uz, state_ptrs, [t.data_ptr() for t in U],
+                                 [t.data_ptr() for t in Cu], [t.data_ptr() for t in Cz], ndof,
+                                 stream=stream)
+
+
+def main_drift(args, dgb):
+    """Mixed precision against FP64: (1) per-field normwise error of one
+    bssnRHS over the uneven 20,000-block batch; (2) per-field error of the
+    evolved state and the Hamiltonian / momentum constraint L2 drift after
+    --drift-steps RK4 steps on the octree."""
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    dgb.init(0)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    out = {"metric": "mixed-precision error and constraint drift vs FP64", "impl": "ours",
+           "data": "synthetic (seeded Brill-Lindquist + 1e-6 noise)"}
+
+    # (1) RHS error on the uneven batch; padding stays 0 in both outputs
+    blocks, seed, sigma = workload(dgb, "uneven20k")
+    plan = dgb.Plan(blocks, dgb.default_params(sigma))
+    n = plan.unzipped
+    u = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(24)]
+    plan.synth_fill_device([t.data_ptr() for t in u], seed, 1e-6, sh)
+    up = [t.data_ptr() for t in u]
+    r64 = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(24)]
+    plan.rhs_device([t.data_ptr() for t in r64], up, dgb.PREC_FP64, sh)
+    rerr = {}
+    rmx = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(24)]
+    plan.rhs_device([t.data_ptr() for t in rmx], up, dgb.PREC_MIXED, sh)
+    torch.cuda.synchronize(dev)
+    for v in range(24):
+        den = float(r64[v].abs().max())
+        rerr[dgb.VAR_NAMES[v]] = float((rmx[v] - r64[v]).abs().max()) / den if den > 0 else 0.0
+    out["rhs_error_uneven20k"] = {"per_field_normwise": rerr, "max": max(rerr.values()),
+                                  "definition": "max|rhs_mixed - rhs_fp64| / max|rhs_fp64| over "
+                                                "block interiors, one bssnRHS"}
+    del u, r64, rmx
+    plan.close()
+    torch.cuda.empty_cache()
+
+    # (2) evolution on the octree
+    seed = 20261203 + 3
+    mesh = dgb.Mesh(dgb.mesh_params(max_level=args.drift_level, min_level=4,
+                                    fine_radius=args.fine_radius))
+    dt = 0.25 * 64.0 / (2 ** args.drift_level * 6)
+    plan = dgb.Plan(mesh.blocks, dgb.default_params(0.4))
+    uz = dgb.UnzipPlan(mesh.operator(), mesh.ndof)
+    U = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(24)]
+    Cu = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(6)]
+    Cz = [torch.zeros(mesh.ndof, dtype=torch.float64, device=dev) for _ in range(6)]
+    host = [np.empty(mesh.ndof) for _ in range(24)]
+    dgb.synth_fill_points(mesh.dof_coords(), host, seed, 1e-6)
+    every = max(1, args.drift_steps // 10)
+    runs, finals = {}, {}
+    for name, prec in (("fp64", dgb.PREC_FP64), ("mixed", dgb.PREC_MIXED)):
+        st = dgb.Stepper(plan, uz, prec)
+        ds = [torch.from_numpy(a).to(dev) for a in host]
+        ptrs = [t.data_ptr() for t in ds]
+        hist = [[0] + constraint_norms(dgb, plan, uz, ptrs, U, Cu, Cz, mesh.ndof, sh)]
+        step, t_steps = 0, 0.0
+        while step < args.drift_steps:
+            k = min(every, args.drift_steps - step)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st.step(ptrs, dt, nsteps=k, stream=sh)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            t_steps += e0.elapsed_time(e1)
+            step += k
+            hist.append([step] + constraint_norms(dgb, plan, uz, ptrs, U, Cu, Cz, mesh.ndof, sh))
+        st.close()
+        runs[name] = {"l2_history": hist, "ms_per_step": t_steps / args.drift_steps}
+        finals[name] = ds
+    ferr = {}
+    for v in range(24):
+        den = float(finals["fp64"][v].abs().max())
+        ferr[dgb.VAR_NAMES[v]] = float((finals["mixed"][v] - finals["fp64"][v]).abs().max()) / den
+    cnames = ("ham", "mom0", "mom1", "mom2")
+    drift = {}
+    for q, cn in enumerate(cnames):
+        f0, f1 = runs["fp64"]["l2_history"][0][1 + q], runs["fp64"]["l2_history"][-1][1 + q]
+        m0, m1 = runs["mixed"]["l2_history"][0][1 + q], runs["mixed"]["l2_history"][-1][1 + q]
+        drift[cn] = {"fp64": f1 - f0, "mixed": m1 - m0,
+                     "ratio_abs": abs(m1 - m0) / abs(f1 - f0) if f1 != f0 else None,
+                     "final_rel_diff": abs(m1 - f1) / abs(f1) if f1 else None}
+    out["octree"] = {"leaves": mesh.num_leaves, "blocks": mesh.nblocks, "nodes": mesh.ndof,
+                     "levels": [4, args.drift_level], "fine_radius": args.fine_radius,
+                     "dt": dt, "cfl": 0.25, "ko_sigma": 0.4, "steps": args.drift_steps,
+                     "mask": "alpha >= 0.3"}
+    out["runs"] = runs
+    out["state_error_after_steps"] = {"per_field_normwise": ferr, "max": max(ferr.values())}
+    out["constraint_drift"] = drift
+    print(json.dumps(out))
+    uz.close()
+    plan.close()
 
 
 if __name__ == "__main__":

@@ -75,7 +75,7 @@ size_t rhs_smem_bytes(int variant, int precision)
     const TileShape t = kTileShapes[variant];
     const size_t fb = (size_t)(t.tx + 6) * (t.ty + 6) * (t.tz + 6);
     const size_t bx = (size_t)t.tx * (t.ty + 6) * (t.tz + 6) + (size_t)t.tx * t.ty * (t.tz + 6);
-    return precision == DGB_PREC_MIXED ? 2 * fb * 8 + 2 * fb * 4 + bx * 4 : 2 * fb * 8 + bx * 8;
+    return precision == DGB_PREC_MIXED ? 2 * fb * 8 + 2 * fb * 4 + 2 * bx * 4 : 2 * fb * 8 + bx * 8;
 }
 
 int rhs_threads(int) { return kThreads; }

@@ -26,11 +26,13 @@
 // Only interior (bflag == 0) blocks; the host rejects others.
 //
 // The mixed-precision variant (MIXED = true) splits each staged FP64 value
-// into an exact float pair hi + lo by integer bit operations (no FP64 pipe
-// work), evaluates every stencil in FP32 on symmetric differences
-// (u[+k] -/+ u[-k] - ..., exact by Sterbenz for smooth data) for the hi and
-// lo parts, and widens the float result to FP64 by integer bit operations.
-// The algebra, the KO accumulate and all field I/O stay FP64.
+// into a float pair hi + lo by integer bit operations (no FP64 pipe work)
+// and evaluates every stencil in FP32 on symmetric differences
+// (u[+k] - u[-k], (u[k] - u0) + (u[-k] - u0)): compensated (TwoSum /
+// FMA TwoProduct) on the hi part, plain on the lo part.  Each stencil's
+// float pair is widened to FP64 by integer bit operations, added and scaled
+// in FP64; the sums across stencil terms (KO over directions, the algebra),
+// the RK update and all field I/O stay FP64.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -264,6 +266,65 @@ __device__ __forceinline__ float nko_32(const float *u, int s)
     return fmaf(-15.0f, t1, fmaf(6.0f, t2, -t3));
 }
 
+// Compensated FP32 stencils for the hi plane.  A value is carried as s + e
+// (|e| <= ulp(s)/2) through error-free transformations: Knuth's TwoSum for
+// every difference and sum, the FMA TwoProduct for every tap product, all
+// in FP32 with explicit round-to-nearest intrinsics (no contraction, no
+// reassociation).  The numerator then reaches FP64 as widen(s) + widen(e),
+// so neither the differences of nearly equal hi values nor the final float
+// rounding of the sum limits the accuracy; the FP64 side is one add and the
+// scale multiply per stencil.
+struct FP2 {
+    float s, e;
+};
+__device__ __forceinline__ FP2 two_sum(float a, float b)
+{
+    FP2 r;
+    r.s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(r.s, a);
+    r.e = __fadd_rn(__fsub_rn(a, __fsub_rn(r.s, bb)), __fsub_rn(b, bb));
+    return r;
+}
+__device__ __forceinline__ FP2 add2(FP2 x, FP2 y)
+{
+    FP2 r = two_sum(x.s, y.s);
+    r.e = __fadd_rn(r.e, __fadd_rn(x.e, y.e));
+    return r;
+}
+__device__ __forceinline__ FP2 mulc2(float c, FP2 x)
+{
+    FP2 r;
+    r.s = __fmul_rn(c, x.s);
+    r.e = __fadd_rn(__fmaf_rn(c, x.s, -r.s), __fmul_rn(c, x.e));
+    return r;
+}
+// (u[k] - c) + (u[-k] - c)
+__device__ __forceinline__ FP2 sym2(const float *u, int k, float c)
+{
+    return add2(two_sum(u[k], -c), two_sum(u[-k], -c));
+}
+__device__ __forceinline__ FP2 n1_c(const float *u, int s)
+{
+    const FP2 a1 = two_sum(u[s], -u[-s]), a2 = two_sum(u[2 * s], -u[-2 * s]),
+              a3 = two_sum(u[3 * s], -u[-3 * s]);
+    return add2(add2(mulc2(45.0f, a1), mulc2(-9.0f, a2)), a3);
+}
+__device__ __forceinline__ FP2 n2_c(const float *u, int s)
+{
+    const float c = u[0];
+    return add2(add2(mulc2(270.0f, sym2(u, s, c)), mulc2(-27.0f, sym2(u, 2 * s, c))),
+                mulc2(2.0f, sym2(u, 3 * s, c)));
+}
+__device__ __forceinline__ FP2 nko_c(const float *u, int s)
+{
+    const float c = u[0];
+    FP2 t3 = sym2(u, 3 * s, c);
+    t3.s = -t3.s;
+    t3.e = -t3.e;
+    return add2(add2(mulc2(-15.0f, sym2(u, s, c)), mulc2(6.0f, sym2(u, 2 * s, c))), t3);
+}
+__device__ __forceinline__ double fp2_widen(FP2 h) { return __dadd_rn(widen(h.s), widen(h.e)); }
+
 // ---------------------------------------------------------------- cp.async
 __device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
 {
@@ -309,9 +370,9 @@ template <int TX, int TY, int TZ, bool MIXED>
 struct Smem {
     using G = Geo<TX, TY, TZ>;
     // FP64: two field buffers + d_x box + d_y box (doubles)
-    // MIXED: two field buffers (doubles) + hi/lo float planes + float boxes
+    // MIXED: two field buffers (doubles) + hi/lo float planes + float-pair boxes
     static constexpr size_t bytes = MIXED
-        ? (2 * G::FBUF * 8 + 2 * G::FBUF * 4 + (G::DXB + G::DYB) * 4)
+        ? (2 * G::FBUF * 8 + 2 * G::FBUF * 4 + 2 * (G::DXB + G::DYB) * 4)
         : (2 * G::FBUF * 8 + (G::DXB + G::DYB) * 8);
 };
 
@@ -328,11 +389,13 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
     // FP64 boxes
     double *dxb = fb1 + G::FBUF;
     double *dyb = dxb + G::DXB;
-    // FP32 planes (MIXED)
+    // FP32 planes (MIXED): split field, and the d_x / d_y boxes as s + e pairs
     float *fhi = reinterpret_cast<float *>(fb1 + G::FBUF);
     float *flo = fhi + G::FBUF;
-    float *dxf = flo + G::FBUF;
-    float *dyf = dxf + G::DXB;
+    float *dxs = flo + G::FBUF;
+    float *dxe = dxs + G::DXB;
+    float *dys = dxe + G::DXB;
+    float *dye = dys + G::DYB;
     const int tid = threadIdx.x;
 
     const int nx = blk.sz[0], ny = blk.sz[1];
@@ -511,31 +574,43 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 flo[q] = f2.lo;
             }
             __syncthreads();
-            const float s60[3] = {(float)c60[0], (float)c60[1], (float)c60[2]};
-            const float s180[3] = {(float)c180[0], (float)c180[1], (float)c180[2]};
-            const float sko[3] = {(float)ko[0], (float)ko[1], (float)ko[2]};
-            auto D1 = [&](int off, int s, float c) {
-                return (n1_32(fhi + off, s) + n1_32(flo + off, s)) * c;
+            // numerators: compensated on the hi plane, plain FP32 on the lo
+            // plane (its rounding is 2^-24 of a 2^-24 residue), as s + e
+            auto N1 = [&](int off, int s) {
+                FP2 h = n1_c(fhi + off, s);
+                h.e = __fadd_rn(h.e, n1_32(flo + off, s));
+                return h;
             };
-            auto D2 = [&](int off, int s, float c) {
-                return (n2_32(fhi + off, s) + n2_32(flo + off, s)) * c;
+            auto N2 = [&](int off, int s) {
+                FP2 h = n2_c(fhi + off, s);
+                h.e = __fadd_rn(h.e, n2_32(flo + off, s));
+                return h;
             };
-            auto KO = [&](int off, int s, float c) {
-                return (nko_32(fhi + off, s) + nko_32(flo + off, s)) * c;
+            auto NK = [&](int off, int s) {
+                FP2 h = nko_c(fhi + off, s);
+                h.e = __fadd_rn(h.e, nko_32(flo + off, s));
+                return h;
+            };
+            // KO sum across the three directions in FP64
+            auto KO3 = [&](int off) {
+                return __dadd_rn(__dadd_rn(__dmul_rn(fp2_widen(NK(off, 1)), ko[0]),
+                                           __dmul_rn(fp2_widen(NK(off, sy)), ko[1])),
+                                 __dmul_rn(fp2_widen(NK(off, sz)), ko[2]));
             };
             if (q2 < 0) {
                 for (int p = tid; p < P; p += kThreads) {
                     const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                    Sg[p] = widen(D1(off, 1, s60[0]));
-                    Sg[G::PMAX + p] = widen(D1(off, sy, s60[1]));
-                    Sg[2 * G::PMAX + p] = widen(D1(off, sz, s60[2]));
-                    Sko[p] = widen(KO(off, 1, sko[0]) + KO(off, sy, sko[1]) + KO(off, sz, sko[2]));
+                    Sg[p] = __dmul_rn(fp2_widen(N1(off, 1)), c60[0]);
+                    Sg[G::PMAX + p] = __dmul_rn(fp2_widen(N1(off, sy)), c60[1]);
+                    Sg[2 * G::PMAX + p] = __dmul_rn(fp2_widen(N1(off, sz)), c60[2]);
+                    Sko[p] = KO3(off);
                 }
             } else {
                 double *S2 = S + (size_t)(DGB_NUM_GRAD + 6 * q2) * G::PMAX;
                 const int bx_y = ey + 6;
                 const int nA = ex * bx_y * ez, nB = ex * ey * 6;
+                // (1a) x-numerators on the cross region, kept as s + e pairs
                 for (int q = tid; q < nA + nB; q += kThreads) {
                     int ti, tj, tk;
                     if (q < nA) {
@@ -546,32 +621,47 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                         const int kk = r / ey;
                         tk = kk < 3 ? kk : ez + kk;
                     }
-                    dxf[ti + ex * (tj + bx_y * tk)] = D1((ti + 3) + sy * tj + sz * tk, 1, s60[0]);
+                    const FP2 h = N1((ti + 3) + sy * tj + sz * tk, 1);
+                    const int b = ti + ex * (tj + bx_y * tk);
+                    dxs[b] = h.s;
+                    dxe[b] = h.e;
                 }
+                // (1b) y-numerators, z extended
                 const int nC = ex * ey * pz;
                 for (int q = tid; q < nC; q += kThreads) {
                     const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
-                    dyf[q] = D1((ti + 3) + sy * (tj + 3) + sz * tk, sy, s60[1]);
+                    const FP2 h = N1((ti + 3) + sy * (tj + 3) + sz * tk, sy);
+                    dys[q] = h.s;
+                    dye[q] = h.e;
                 }
                 for (int p = tid; p < P; p += kThreads) {
                     const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                    Sg[2 * G::PMAX + p] = widen(D1(off, sz, s60[2]));
-                    S2[0 * G::PMAX + p] = widen(D2(off, 1, s180[0]));
-                    S2[3 * G::PMAX + p] = widen(D2(off, sy, s180[1]));
-                    S2[5 * G::PMAX + p] = widen(D2(off, sz, s180[2]));
-                    Sko[p] = widen(KO(off, 1, sko[0]) + KO(off, sy, sko[1]) + KO(off, sz, sko[2]));
+                    Sg[2 * G::PMAX + p] = __dmul_rn(fp2_widen(N1(off, sz)), c60[2]);
+                    S2[0 * G::PMAX + p] = __dmul_rn(fp2_widen(N2(off, 1)), c180[0]);
+                    S2[3 * G::PMAX + p] = __dmul_rn(fp2_widen(N2(off, sy)), c180[1]);
+                    S2[5 * G::PMAX + p] = __dmul_rn(fp2_widen(N2(off, sz)), c180[2]);
+                    Sko[p] = KO3(off);
                 }
                 __syncthreads();
+                // (2) mixed: the pair boxes differentiated again (compensated on s,
+                // plain on e), both scales applied in FP64
+                const double cxy = c60[0] * c60[1], cxz = c60[0] * c60[2], cyz = c60[1] * c60[2];
                 for (int p = tid; p < P; p += kThreads) {
                     const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
-                    const float *cx = dxf + ti + ex * ((tj + 3) + bx_y * (tk + 3));
-                    const float *cy = dyf + ti + ex * (tj + ey * (tk + 3));
-                    Sg[p] = widen(cx[0]);
-                    Sg[G::PMAX + p] = widen(cy[0]);
-                    S2[1 * G::PMAX + p] = widen(n1_32(cx, ex) * s60[1]);
-                    S2[2 * G::PMAX + p] = widen(n1_32(cx, ex * bx_y) * s60[2]);
-                    S2[4 * G::PMAX + p] = widen(n1_32(cy, ex * ey) * s60[2]);
+                    const int bxi = ti + ex * ((tj + 3) + bx_y * (tk + 3));
+                    const int byi = ti + ex * (tj + ey * (tk + 3));
+                    Sg[p] = __dmul_rn(__dadd_rn(widen(dxs[bxi]), widen(dxe[bxi])), c60[0]);
+                    Sg[G::PMAX + p] = __dmul_rn(__dadd_rn(widen(dys[byi]), widen(dye[byi])), c60[1]);
+                    FP2 h = n1_c(dxs + bxi, ex);
+                    h.e = __fadd_rn(h.e, n1_32(dxe + bxi, ex));
+                    S2[1 * G::PMAX + p] = __dmul_rn(fp2_widen(h), cxy);
+                    h = n1_c(dxs + bxi, ex * bx_y);
+                    h.e = __fadd_rn(h.e, n1_32(dxe + bxi, ex * bx_y));
+                    S2[2 * G::PMAX + p] = __dmul_rn(fp2_widen(h), cxz);
+                    h = n1_c(dys + byi, ex * ey);
+                    h.e = __fadd_rn(h.e, n1_32(dye + byi, ex * ey));
+                    S2[4 * G::PMAX + p] = __dmul_rn(fp2_widen(h), cyz);
                 }
             }
         }

@@ -280,6 +280,22 @@ def constraint_l2(field_ptrs, ndof, mask_ptr=None, threshold=0.0, stream=0):
 
 CONSTRAINT_NAMES = ("ham", "mom0", "mom1", "mom2", "psi4_real", "psi4_img")
 
+# bssn:: defaults of the constraint report's mask (BSSN_GR/src/parameters.cpp:157-158)
+EXTRACTION_VAR_ID = 0  # alpha
+EXTRACTION_TOL = 0.3
+
+
+def constraint_report(plan, uz, state_ptrs, unzipped_ptrs, cons_unzipped_ptrs, cons_ptrs, ndof,
+                      threshold=EXTRACTION_TOL, stream=0):
+    """The solver's constraint output (BSSN_GR/src/bssnCtx.cpp:332-365) on
+    device buffers: unzip the 24 zipped state vectors, physical_constraints
+    on every block, zip the 6 outputs into cons_ptrs, and return the masked
+    L2 of ham, mom0-2 (mask: the alpha vector >= threshold)."""
+    uz.unzip(state_ptrs, unzipped_ptrs, stream)
+    plan.physical_constraints(cons_unzipped_ptrs, unzipped_ptrs, stream)
+    uz.zip(cons_unzipped_ptrs, cons_ptrs, stream)
+    return constraint_l2(cons_ptrs[:4], ndof, state_ptrs[EXTRACTION_VAR_ID], threshold, stream)
+
 
 def rk4_stage(stage, dst_ptrs, prev_ptrs, k_ptrs, nnodes, dt, chi_floor=1e-4, stream=0):
     d, k1 = ptr_array(dst_ptrs)

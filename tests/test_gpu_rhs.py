@@ -9,7 +9,7 @@ from workloads import SEED1, SEED2, host_fields, interior_mask, normwise, repack
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-12
-MIXED_RHS_TOL = 2e-4  # per-field normwise, FP32 stencils vs FP64
+MIXED_RHS_TOL = 1e-7  # per-field normwise, compensated FP32 stencils vs FP64
 
 
 def device_fields(torch, arrays):
