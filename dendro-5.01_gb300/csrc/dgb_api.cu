@@ -535,7 +535,18 @@ dgb_status dgb_synth_fill_device(dgb_plan *p, double *const *u, uint64_t seed, d
     if (!p || !u) return DGB_ERR_INVALID;
     if (p->blocks.empty()) return DGB_OK;
     DGB_CUDA(synth_fill_launch(p->d_blocks, (uint32_t)p->blocks.size(), p->d_first, p->unzipped, u,
-                               seed, noise, (cudaStream_t)stream));
+                               0, NV, seed, noise, (cudaStream_t)stream));
+    return DGB_OK;
+}
+
+dgb_status dgb_synth_fill_var_device(dgb_plan *p, int var, double *dst, uint64_t seed, double noise,
+                                     void *stream)
+{
+    if (!p || !dst || var < 0 || var > NV) return DGB_ERR_INVALID;
+    if (p->blocks.empty()) return DGB_OK;
+    double *u[1] = {dst};
+    DGB_CUDA(synth_fill_launch(p->d_blocks, (uint32_t)p->blocks.size(), p->d_first, p->unzipped, u,
+                               var, var + 1, seed, noise, (cudaStream_t)stream));
     return DGB_OK;
 }
 

@@ -68,9 +68,11 @@ cudaError_t rk4_launch(int stage, double *const *dst, const double *const *prev,
                        const double *const *k, uint64_t nnodes, double dt, double chi_floor,
                        unsigned int *status, cudaStream_t stream);
 
+// fills variables [v0, v1) (v1 <= 25; index 24 = theta_z4 of the CCZ4 set);
+// u[q] is the array of variable v0 + q
 cudaError_t synth_fill_launch(const DevBlock *blocks, uint32_t nblk, const uint64_t *first_pt,
-                              uint64_t total, double *const *u, uint64_t seed, double noise,
-                              cudaStream_t stream);
+                              uint64_t total, double *const *u, int v0, int v1, uint64_t seed,
+                              double noise, cudaStream_t stream);
 
 // Constraint diagnostics (physcon.cu).
 struct PcArgs {

@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(256) rk4_kernel(const Rk4Args a)
 }
 
 struct SynthArgs {
-    double *u[NV];
+    double *u[NV + 1];  // the 24 BSSN fields, or theta_z4 of the CCZ4 set at index 24
+    int v0, v1;         // variables [v0, v1) are filled
     const DevBlock *blocks;
     uint32_t nblk;
     uint64_t seed;
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(256) synth_kernel(const SynthArgs a)
     for (uint32_t b = blockIdx.x; b < a.nblk; b += gridDim.x) {
         const DevBlock d = a.blocks[b];
         const uint64_t n = (uint64_t)d.sz[0] * d.sz[1] * d.sz[2];
-        for (int v = 0; v < NV; v++) {
+        for (int v = a.v0; v < a.v1; v++) {
             const uint64_t key = dgb_noise_key(a.seed, b, (uint32_t)v);
             double *dst = a.u[v] + d.offset;
             for (uint64_t p = threadIdx.x; p < n; p += blockDim.x) {
@@ -128,11 +129,13 @@ cudaError_t rk4_launch(int stage, double *const *dst, const double *const *prev,
 }
 
 cudaError_t synth_fill_launch(const DevBlock *blocks, uint32_t nblk, const uint64_t *,
-                              uint64_t, double *const *u, uint64_t seed, double noise,
-                              cudaStream_t stream)
+                              uint64_t, double *const *u, int v0, int v1, uint64_t seed,
+                              double noise, cudaStream_t stream)
 {
     SynthArgs a;
-    for (int v = 0; v < NV; v++) a.u[v] = u[v];
+    for (int v = 0; v <= NV; v++) a.u[v] = (v >= v0 && v < v1) ? u[v - v0] : nullptr;
+    a.v0 = v0;
+    a.v1 = v1;
     a.blocks = blocks;
     a.nblk = nblk;
     a.seed = seed;

@@ -149,6 +149,33 @@ extern "C" dgb_status dgb_synth_fill_host(const dgb_block_desc *blocks, size_t n
     return DGB_OK;
 }
 
+extern "C" dgb_status dgb_synth_fill_var_host(const dgb_block_desc *blocks, size_t nblk, int var,
+                                              double *dst, uint64_t seed, double noise,
+                                              int nthreads)
+{
+    if (!blocks || !dst || var < 0 || var > DGB_NUM_VARS) return DGB_ERR_INVALID;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic)
+#endif
+    for (long b = 0; b < (long)nblk; b++) {
+        const dgb_block_desc &d = blocks[b];
+        const int nx = d.sz[0], ny = d.sz[1], nz = d.sz[2];
+        double h[3];
+        for (int a = 0; a < 3; a++) h[a] = (d.ptmax[a] - d.ptmin[a]) / (double)(d.sz[a] - 1);
+        const uint64_t key = dgb_noise_key(seed, (uint64_t)b, (uint32_t)var);
+        double *out = dst + d.offset;
+        for (int k = 0; k < nz; k++)
+            for (int j = 0; j < ny; j++)
+                for (int i = 0; i < nx; i++) {
+                    const uint64_t p = (uint64_t)i + (uint64_t)nx * (j + (uint64_t)ny * k);
+                    out[p] = dgb_synth_value(var, key, p, i, j, k, d.ptmin, h, noise);
+                }
+    }
+    (void)nthreads;
+    return DGB_OK;
+}
+
 extern "C" dgb_status dgb_synth_fill_points_host(const double *xyz, uint64_t n, double *const *u,
                                                  uint64_t seed, double noise, int nthreads)
 {

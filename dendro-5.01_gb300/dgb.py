@@ -52,6 +52,41 @@ def default_params(ko_sigma=0.1):
     return p
 
 
+CCZ4_VAR_NAMES = ["alpha", "psi", "K", "Gh0", "Gh1", "Gh2", "beta0", "beta1", "beta2",
+                  "B0", "B1", "B2", "gt0", "gt1", "gt2", "gt3", "gt4", "gt5",
+                  "At0", "At1", "At2", "At3", "At4", "At5", "theta_z4"]
+
+
+class Ccz4Params(C.Structure):
+    """The ccz4:: globals ccz4rhs reads (CCZ4_GR/include/parameters.h)."""
+    _fields_ = [("lambda_", C.c_double * 4), ("lambda_f", C.c_double * 2),
+                ("kappa", C.c_double * 2), ("p_expo", C.c_double), ("eta_const", C.c_double),
+                ("eta_r0", C.c_double), ("eta_damping_exp", C.c_double),
+                ("ko_sigma", C.c_double)]
+
+
+def default_ccz4_params(ko_sigma=0.4, kappa=(0.1, 0.0)):
+    """lambda = 1, lambda_f = (1, 0), p_expo = -1, eta = 2 within r0 = 30
+    (CCZ4_GR/pars/ccz4.par.json:90-115), damping kappa."""
+    p = Ccz4Params()
+    p.lambda_[:] = [1.0, 1.0, 1.0, 1.0]
+    p.lambda_f[:] = [1.0, 0.0]
+    p.kappa[:] = list(kappa)
+    p.p_expo = -1.0
+    p.eta_const = 2.0
+    p.eta_r0 = 30.0
+    p.eta_damping_exp = 1.0
+    p.ko_sigma = ko_sigma
+    return p
+
+
+def ccz4_params_vector(p):
+    """The 13-double vector the CCZ4 oracle and reference harness take."""
+    return np.array(list(p.lambda_) + list(p.lambda_f) + list(p.kappa)
+                    + [p.p_expo, p.eta_const, p.eta_r0, p.eta_damping_exp, p.ko_sigma],
+                    dtype=np.float64)
+
+
 def params_vector(p):
     """The 10-double vector the oracle and the reference harness take."""
     return np.array(list(p.lambda_) + list(p.lambda_f)
@@ -96,6 +131,11 @@ _SIGS = {
                                       C.c_double, C.c_int]),
     "dgb_synth_fill_device": (C.c_int, [C.c_void_p, PtrArr, C.c_uint64, C.c_double,
                                         C.c_void_p]),
+    "dgb_synth_fill_var_host": (C.c_int, [C.POINTER(BlockDesc), C.c_size_t, C.c_int,
+                                          C.POINTER(C.c_double), C.c_uint64, C.c_double,
+                                          C.c_int]),
+    "dgb_synth_fill_var_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_uint64,
+                                            C.c_double, C.c_void_p]),
     "dgb_synth_blocks": (C.c_int, [C.c_int, C.c_uint64, C.POINTER(BlockDesc),
                                    C.POINTER(C.c_size_t)]),
     "dgb_mesh_create": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
@@ -197,6 +237,10 @@ def synth_fill_host(blocks, fields, seed, noise=1e-6, nthreads=0):
     pa, keep = host_ptrs(fields)
     check(lib().dgb_synth_fill_host(blocks, len(blocks), pa, seed, noise, nthreads),
           "dgb_synth_fill_host")
+    if len(fields) > 24:  # the CCZ4 set: theta_z4 as variable 24
+        check(lib().dgb_synth_fill_var_host(blocks, len(blocks), 24,
+                                            fields[24].ctypes.data_as(C.POINTER(C.c_double)),
+                                            seed, noise, nthreads), "dgb_synth_fill_var_host")
 
 
 def init(device=0):
@@ -256,6 +300,10 @@ class Plan:
         u, k = ptr_array(u_ptrs)
         check(lib().dgb_synth_fill_device(self.h, u, seed, noise, C.c_void_p(stream)),
               "dgb_synth_fill_device")
+        if len(u_ptrs) > 24:  # the CCZ4 set: theta_z4 as variable 24
+            check(lib().dgb_synth_fill_var_device(self.h, 24, C.c_void_p(int(u_ptrs[24])), seed,
+                                                  noise, C.c_void_p(stream)),
+                  "dgb_synth_fill_var_device")
 
     def close(self):
         if self.h:

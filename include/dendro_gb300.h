@@ -174,6 +174,13 @@ dgb_status dgb_synth_fill_host(const dgb_block_desc *blocks, size_t nblk,
                                double *const *u, uint64_t seed, double noise, int nthreads);
 dgb_status dgb_synth_fill_device(dgb_plan *plan, double *const *u, uint64_t seed,
                                  double noise, void *stream);
+/* One variable of the synthetic set, var in [0, 24]: the 24 BSSN fields,
+ * or 24 = theta_z4 of the CCZ4 set (value 0 + noise).  The CCZ4 state is
+ * the 24 BSSN fields (psi takes chi's values, Gh takes Gt's) plus var 24. */
+dgb_status dgb_synth_fill_var_host(const dgb_block_desc *blocks, size_t nblk, int var,
+                                   double *dst, uint64_t seed, double noise, int nthreads);
+dgb_status dgb_synth_fill_var_device(dgb_plan *plan, int var, double *dst, uint64_t seed,
+                                     double noise, void *stream);
 /* Synthetic block lists.  which = 1: 512 uniform 13^3 blocks, dx = 0.05,
  * tiled 8x8x8 over [-1.2,1.2]^3; which = 2: 20,000 blocks, 70/20/8/2 % of
  * 13^3/19^3/31^3/61^3, levels 4-10 on [-32,32]^3.  Pass blocks == NULL to

@@ -199,9 +199,9 @@ void orc_ko42(int dir, double *D, const double *u, double h, const unsigned *sz,
 /* Outgoing-radiation condition on the flagged faces' boundary layer
  * (BSSN_GR/src/rhs.cpp:838-982):
  * rhs = -(1/r) (x f_x + y f_y + z f_z + falloff (f - asymptotic)). */
-static void orc_bssn_bcs(double *f_rhs, const double *f, const double *dxf, const double *dyf,
-                         const double *dzf, const double *pmin, const double *pmax,
-                         double falloff, double asym, const unsigned *sz, unsigned bflag)
+void orc_bssn_bcs(double *f_rhs, const double *f, const double *dxf, const double *dyf,
+                  const double *dzf, const double *pmin, const double *pmax,
+                  double falloff, double asym, const unsigned *sz, unsigned bflag)
 {
     const int nx = sz[0], ny = sz[1], nz = sz[2];
     const double hx = (pmax[0] - pmin[0]) / (nx - 1), hy = (pmax[1] - pmin[1]) / (ny - 1),

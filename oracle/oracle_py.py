@@ -12,6 +12,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libdendro_ref.so")
+CCZ4_REF_SO = os.path.join(HERE, "_ref", "libccz4_ref.so")
 
 _D = C.POINTER(C.c_double)
 _PP = C.POINTER(C.c_void_p)
@@ -66,7 +67,17 @@ class Oracle:
         L.orc_physcon_blocks.restype = C.c_int
         L.orc_physcon_blocks.argtypes = [_PP, _PP, C.c_long, C.POINTER(C.c_ulong),
                                          C.POINTER(C.c_uint), C.POINTER(C.c_uint), _D, _D, C.c_int]
-        for nm in ("orc_deriv64", "orc_deriv64_2", "orc_ko42", "orc_deriv42", "orc_deriv42_2"):
+        L.orc_ccz4rhs_ex.restype = C.c_int
+        L.orc_ccz4rhs_ex.argtypes = [_PP, _PP, C.c_ulong, _D, _D, C.POINTER(C.c_uint), C.c_uint,
+                                     _D, C.c_int]
+        L.orc_ccz4rhs_blocks.restype = C.c_int
+        L.orc_ccz4rhs_blocks.argtypes = [_PP, _PP, C.c_long, C.POINTER(C.c_ulong),
+                                         C.POINTER(C.c_uint), C.POINTER(C.c_uint), _D, _D, _D,
+                                         C.c_int, C.c_int]
+        L.orc_ccz4_adv42.restype = None
+        L.orc_ccz4_adv42.argtypes = [C.c_int, _D, _D, C.c_double, C.POINTER(C.c_uint), _D, C.c_uint]
+        for nm in ("orc_deriv64", "orc_deriv64_2", "orc_ko42", "orc_deriv42", "orc_deriv42_2",
+                   "orc_ccz4_ko42"):
             f = getattr(L, nm)
             f.restype = None
             f.argtypes = [C.c_int, _D, _D, C.c_double, C.POINTER(C.c_uint), C.c_uint]
@@ -90,12 +101,38 @@ class Oracle:
         """kind in {'d1','d2','ko'} on a 3-D array u3[z][y][x]; returns D (zeros
         where the reference leaves the output untouched)."""
         fn = {"d1": self.L.orc_deriv64, "d2": self.L.orc_deriv64_2, "ko": self.L.orc_ko42,
-              "d1_4": self.L.orc_deriv42, "d2_4": self.L.orc_deriv42_2}[kind]
+              "d1_4": self.L.orc_deriv42, "d2_4": self.L.orc_deriv42_2,
+              "ko_ccz4": self.L.orc_ccz4_ko42}[kind]
         u = np.ascontiguousarray(u3, dtype=np.float64)
         D = np.zeros_like(u)
         sz = (C.c_uint * 3)(u.shape[2], u.shape[1], u.shape[0])
         fn(dirn, D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz, bflag)
         return D
+
+    def adv_ccz4(self, dirn, u3, h, beta3, bflag=0):
+        """CCZ4 upwind advective derivative on u3[z][y][x] with shift component beta3."""
+        u = np.ascontiguousarray(u3, dtype=np.float64)
+        b = np.ascontiguousarray(beta3, dtype=np.float64)
+        D = np.zeros_like(u)
+        sz = (C.c_uint * 3)(u.shape[2], u.shape[1], u.shape[0])
+        self.L.orc_ccz4_adv42(dirn, D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz,
+                              b.ctypes.data_as(_D), bflag)
+        return D
+
+    def ccz4rhs_blocks(self, rhs, u, blocks, prm, apply_bcs=True, nthreads=0):
+        """ccz4rhs over a block list; rhs, u: 25 arrays in CCZ4 variable order."""
+        n = len(blocks)
+        off = (C.c_ulong * n)(*[b.offset for b in blocks])
+        sz = (C.c_uint * (3 * n))(*[s for b in blocks for s in b.sz])
+        bf = (C.c_uint * n)(*[b.bflag for b in blocks])
+        pmin = np.array([x for b in blocks for x in b.ptmin], dtype=np.float64)
+        pmax = np.array([x for b in blocks for x in b.ptmax], dtype=np.float64)
+        r, k1 = _ptrs(rhs)
+        uu, k2 = _ptrs(u)
+        p = np.ascontiguousarray(prm, dtype=np.float64)
+        return self.L.orc_ccz4rhs_blocks(r, uu, n, off, sz, bf, pmin.ctypes.data_as(_D),
+                                         pmax.ctypes.data_as(_D), p.ctypes.data_as(_D),
+                                         1 if apply_bcs else 0, nthreads)
 
     def physcon_block(self, cons, u, block):
         """physical_constraints on one block: cons = 6 arrays (ham, mom0-2,
@@ -146,6 +183,57 @@ class Oracle:
                 rows.append(C.cast(None, _PP))
         karr = (_PP * 4)(*rows)
         self.L.orc_rk4_stage(s, d, p, karr, n, dt, chi_floor)
+
+
+class CCZ4Reference:
+    """The reference's own CCZ4 code (CCZ4_GR/src/derivs.cpp + the ccz4rhs
+    harness), machines with the reference tree only."""
+
+    def __init__(self, path=CCZ4_REF_SO):
+        L = C.CDLL(path)
+        L.ref_ccz4rhs.restype = C.c_int
+        L.ref_ccz4rhs.argtypes = [_PP, _PP, C.c_uint, _D, _D, C.POINTER(C.c_uint), C.c_uint, _D]
+        for nm in ("ccz4_deriv42_x", "ccz4_deriv42_y", "ccz4_deriv42_z", "ccz4_deriv42_xx",
+                   "ccz4_deriv42_yy", "ccz4_deriv42_zz", "ccz4_ko_deriv42_x",
+                   "ccz4_ko_deriv42_y", "ccz4_ko_deriv42_z"):
+            f = getattr(L, nm)
+            f.restype = None
+            f.argtypes = [_D, _D, C.c_double, C.POINTER(C.c_uint), C.c_uint]
+        for nm in ("ccz4_deriv42adv_x", "ccz4_deriv42adv_y", "ccz4_deriv42adv_z"):
+            f = getattr(L, nm)
+            f.restype = None
+            f.argtypes = [_D, _D, C.c_double, C.POINTER(C.c_uint), _D, C.c_uint]
+        self.L = L
+
+    def ccz4rhs(self, rhs, u, block, prm):
+        r, k1 = _ptrs(rhs)
+        uu, k2 = _ptrs(u)
+        pmin = np.array(list(block.ptmin), dtype=np.float64)
+        pmax = np.array(list(block.ptmax), dtype=np.float64)
+        sz = (C.c_uint * 3)(*block.sz)
+        p = np.ascontiguousarray(prm, dtype=np.float64)
+        return self.L.ref_ccz4rhs(r, uu, block.offset, pmin.ctypes.data_as(_D),
+                                  pmax.ctypes.data_as(_D), sz, block.bflag, p.ctypes.data_as(_D))
+
+    def stencil(self, kind, dirn, u3, h, bflag=0):
+        nm = {"d1_4": ["ccz4_deriv42_x", "ccz4_deriv42_y", "ccz4_deriv42_z"],
+              "d2_4": ["ccz4_deriv42_xx", "ccz4_deriv42_yy", "ccz4_deriv42_zz"],
+              "ko_ccz4": ["ccz4_ko_deriv42_x", "ccz4_ko_deriv42_y", "ccz4_ko_deriv42_z"]}[kind][dirn]
+        u = np.ascontiguousarray(u3, dtype=np.float64)
+        D = np.zeros_like(u)
+        sz = (C.c_uint * 3)(u.shape[2], u.shape[1], u.shape[0])
+        getattr(self.L, nm)(D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz, bflag)
+        return D
+
+    def adv(self, dirn, u3, h, beta3, bflag=0):
+        nm = ["ccz4_deriv42adv_x", "ccz4_deriv42adv_y", "ccz4_deriv42adv_z"][dirn]
+        u = np.ascontiguousarray(u3, dtype=np.float64)
+        b = np.ascontiguousarray(beta3, dtype=np.float64)
+        D = np.zeros_like(u)
+        sz = (C.c_uint * 3)(u.shape[2], u.shape[1], u.shape[0])
+        getattr(self.L, nm)(D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz,
+                            b.ctypes.data_as(_D), bflag)
+        return D
 
 
 class Reference:

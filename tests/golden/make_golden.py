@@ -7,7 +7,9 @@ BSSN_GR/scripts/bssnrhs_*.h drivers and
 BSSN_GR/src/bssneqs_eta_const_standard_gauge.cpp inside the bssnrhs harness
 oracle/ref_bssnrhs.cpp, BSSN_GR/src/bssn_constraints.cpp, and the constraint
 diagnostics BSSN_GR/scripts/constraint_derivs.h + BSSN_GR/src/physconeqs.cpp
-inside oracle/ref_physcon.cpp).
+inside oracle/ref_physcon.cpp, and the CCZ4 right-hand side
+CCZ4_GR/src/derivs.cpp + the generated CCZ4_GR/scripts/ccz4rhs_*.h drivers +
+CCZ4_GR/src/ccz4eqs.cpp inside oracle/ref_ccz4rhs.cpp).
 
 Inputs come from the library's seeded synthetic generator (host fill); their
 SHA-256 is stored so that a change of the generator is detected.
@@ -100,6 +102,7 @@ def main():
         enforce_in=np.stack(cs), enforce_out=np.stack(out), enforce_chi_floor=np.array(1e-4))
     print("wrote", os.path.join(HERE, "bssn_reference.npz"))
     constraint_goldens(dgb, ref)
+    ccz4_goldens(dgb)
 
 
 def axis_block(dgb, blocks):
@@ -145,6 +148,45 @@ def constraint_goldens(dgb, ref):
         picks=np.array(picks), seed=np.array(SEED1), input_sha256=np.array(sha(u)),
         cons=np.stack([x[mask] for x in c]), stencil_h=np.array(h), **st)
     print("wrote", os.path.join(HERE, "constraints_reference.npz"))
+
+
+def ccz4_goldens(dgb):
+    """ccz4rhs (CCZ4_GR/src/rhs.cpp:12-298, stencils of CCZ4_GR/src/derivs.cpp)
+    of the reference on the puncture block, a generic block and two
+    domain-boundary corner blocks (one-sided stencils; the harness has no
+    ccz4_bcs), and its upwind / KO stencils on one field."""
+    cref = oracle_py.CCZ4Reference()
+    allb = dgb.synth_blocks(1)
+    picks = [(288, 0), (100, 0), (0, 1 | 4 | 16), (511, 2 | 8 | 32)]
+    rows, off = [], 0
+    for i, f in picks:
+        b = allb[i]
+        rows.append((off, tuple(b.sz), f, tuple(b.ptmin), tuple(b.ptmax)))
+        off += b.sz[0] * b.sz[1] * b.sz[2]
+    blocks = dgb.blocks_array(rows)
+    n = dgb.unzipped_size(blocks)
+    u = [np.zeros(n) for _ in range(25)]
+    dgb.synth_fill_host(blocks, u, SEED1, 1e-6)
+    prm = dgb.ccz4_params_vector(dgb.default_ccz4_params())
+    r = [np.zeros(n) for _ in range(25)]
+    for b in blocks:
+        assert cref.ccz4rhs(r, u, b, prm) == 0
+    mask = interior_mask(blocks, n)
+    b0 = blocks[0]
+    sz = tuple(b0.sz)
+    npt = sz[0] * sz[1] * sz[2]
+    gt1 = u[13][:npt].reshape(sz[2], sz[1], sz[0])
+    beta = [u[6 + d][:npt].reshape(sz[2], sz[1], sz[0]) for d in range(3)]
+    h = (b0.ptmax[0] - b0.ptmin[0]) / (sz[0] - 1)
+    st = {}
+    for d in range(3):
+        st[f"stencil_adv_{d}"] = cref.adv(d, gt1, h, beta[d], 0)[3:-3, 3:-3, 3:-3].copy()
+        st[f"stencil_ko_{d}"] = cref.stencil("ko_ccz4", d, gt1, h, 0)[3:-3, 3:-3, 3:-3].copy()
+    np.savez_compressed(
+        os.path.join(HERE, "ccz4_reference.npz"),
+        picks=np.array(picks), seed=np.array(SEED1), params=prm, input_sha256=np.array(sha(u)),
+        rhs=np.stack([x[mask] for x in r]), stencil_h=np.array(h), **st)
+    print("wrote", os.path.join(HERE, "ccz4_reference.npz"))
 
 
 if __name__ == "__main__":

@@ -1,0 +1,136 @@
+"""CPU tests of the CCZ4 oracle (ccz4rhs, CCZ4_GR/src/rhs.cpp:12-298): pinned
+to the reference's golden vectors (tests/golden/ccz4_reference.npz, made by
+tests/golden/make_golden.py from the reference's own compiled sources) and,
+where the reference tree exists, to the reference code itself on more
+blocks and every boundary flag."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from workloads import SEED2, interior_mask, normwise, repack, sample_uneven
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ccz4_reference.npz")
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN)
+
+
+@pytest.fixture(scope="session")
+def ccz4_reference():
+    import oracle_py
+    if not os.path.isdir("/root/reference") and not os.path.exists(oracle_py.CCZ4_REF_SO):
+        pytest.skip("reference tree not present on this machine")
+    try:
+        oracle_py.build_ref()
+        return oracle_py.CCZ4Reference()
+    except Exception as e:  # pragma: no cover
+        pytest.skip(f"reference build unavailable: {e}")
+
+
+def ccz4_fields(dgb, blocks, seed):
+    n = dgb.unzipped_size(blocks)
+    u = [np.zeros(n) for _ in range(25)]
+    dgb.synth_fill_host(blocks, u, seed, 1e-6)
+    return u
+
+
+def golden_blocks(dgb, g):
+    allb = dgb.synth_blocks(1)
+    rows, off = [], 0
+    for i, f in g["picks"]:
+        b = allb[int(i)]
+        rows.append((off, tuple(b.sz), int(f), tuple(b.ptmin), tuple(b.ptmax)))
+        off += b.sz[0] * b.sz[1] * b.sz[2]
+    blocks = dgb.blocks_array(rows)
+    return blocks, ccz4_fields(dgb, blocks, int(g["seed"]))
+
+
+def test_ccz4_golden_inputs_regenerate(dgb, golden):
+    blocks, u = golden_blocks(dgb, golden)
+    h = hashlib.sha256()
+    for a in u:
+        h.update(np.ascontiguousarray(a).tobytes())
+    assert h.hexdigest() == str(golden["input_sha256"])
+    # the first 24 fields are the BSSN synthetic set (psi = chi, Gh = Gt)
+    n = len(u[0])
+    b24 = [np.zeros(n) for _ in range(24)]
+    dgb.synth_fill_host(blocks, b24, int(golden["seed"]), 1e-6)
+    assert all(np.array_equal(a, b) for a, b in zip(u[:24], b24))
+
+
+def test_oracle_ccz4_matches_golden(dgb, oracle, golden):
+    blocks, u = golden_blocks(dgb, golden)
+    n = len(u[0])
+    r = [np.zeros(n) for _ in range(25)]
+    assert oracle.ccz4rhs_blocks(r, u, blocks, golden["params"], apply_bcs=False) == 0
+    mask = interior_mask(blocks, n)
+    err = normwise([x[mask] for x in r], list(golden["rhs"]), np.ones(int(mask.sum()), dtype=bool))
+    assert err.max() <= 1e-13, dict(zip(dgb.CCZ4_VAR_NAMES, err))
+
+
+def test_oracle_ccz4_stencils_bit_exact(dgb, oracle, golden):
+    blocks, u = golden_blocks(dgb, golden)
+    sz = tuple(blocks[0].sz)
+    npt = sz[0] * sz[1] * sz[2]
+    gt1 = u[13][:npt].reshape(sz[2], sz[1], sz[0])
+    h = float(golden["stencil_h"])
+    for d in range(3):
+        beta = u[6 + d][:npt].reshape(sz[2], sz[1], sz[0])
+        assert np.array_equal(oracle.adv_ccz4(d, gt1, h, beta)[3:-3, 3:-3, 3:-3],
+                              golden[f"stencil_adv_{d}"]), d
+        assert np.array_equal(oracle.stencil("ko_ccz4", d, gt1, h)[3:-3, 3:-3, 3:-3],
+                              golden[f"stencil_ko_{d}"]), d
+
+
+def test_oracle_ccz4_closures_bit_exact(oracle, ccz4_reference):
+    """Every boundary flag: 4th-order first/second, upwind advective (with a
+    zero shift value on the grid) and the CCZ4 KO stencils."""
+    rng = np.random.default_rng(2)
+    u3 = rng.normal(size=(17, 19, 21))
+    b3 = rng.normal(size=(17, 19, 21))
+    b3[5, 6, 7] = 0.0
+    for bflag in range(64):
+        for d in range(3):
+            for kind in ("d1_4", "d2_4", "ko_ccz4"):
+                a = oracle.stencil(kind, d, u3, 0.1, bflag)
+                b = ccz4_reference.stencil(kind, d, u3, 0.1, bflag)
+                assert np.array_equal(a, b), (kind, d, bflag)
+            a = oracle.adv_ccz4(d, u3, 0.1, b3, bflag)
+            b = ccz4_reference.adv(d, u3, 0.1, b3, bflag)
+            assert np.array_equal(a, b), ("adv", d, bflag)
+
+
+def test_oracle_ccz4_matches_reference_code(dgb, oracle, ccz4_reference):
+    allb = dgb.synth_blocks(2, SEED2)
+    blocks = repack(dgb, allb, sample_uneven(allb, (3, 2, 1, 0)))
+    u = ccz4_fields(dgb, blocks, SEED2)
+    prm = dgb.ccz4_params_vector(dgb.default_ccz4_params())
+    n = len(u[0])
+    r1 = [np.zeros(n) for _ in range(25)]
+    r2 = [np.zeros(n) for _ in range(25)]
+    assert oracle.ccz4rhs_blocks(r1, u, blocks, prm) == 0
+    for b in blocks:
+        assert ccz4_reference.ccz4rhs(r2, u, b, prm) == 0
+    err = normwise(r1, r2, interior_mask(blocks, n))
+    assert err.max() <= 1e-13, dict(zip(dgb.CCZ4_VAR_NAMES, err))
+
+
+def test_oracle_ccz4_theta_not_dissipated(dgb, oracle):
+    """The solver's KO loop leaves theta_z4 out (CCZ4_GR/src/rhs.cpp:241-283):
+    its right-hand side does not depend on sigma."""
+    allb = dgb.synth_blocks(1)
+    blocks = repack(dgb, allb, [100])
+    u = ccz4_fields(dgb, blocks, 5)
+    n = len(u[0])
+    out = []
+    for sigma in (0.0, 0.4):
+        prm = dgb.ccz4_params_vector(dgb.default_ccz4_params(ko_sigma=sigma))
+        r = [np.zeros(n) for _ in range(25)]
+        assert oracle.ccz4rhs_blocks(r, u, blocks, prm) == 0
+        out.append(r)
+    assert np.array_equal(out[0][24], out[1][24])
+    assert not np.array_equal(out[0][0], out[1][0])
