@@ -1,0 +1,308 @@
+// CCZ4 right-hand side on padded octant blocks (ccz4rhs,
+// CCZ4_GR/src/rhs.cpp:12-298): one persistent, work-queued launch over all
+// blocks of a plan, the structure of the BSSN kernel (rhs_item.cuh) with
+// the CCZ4 solver's 4th-order stencil family (stencil42.cuh).
+//
+// Per work item (a tile of <= 8x8x8 interior points of one block):
+//   the shift components at the tile points are staged once (the upwind
+//   direction of every advective derivative);
+//   phase D  for each of the 25 fields: stage tile + 3 in shared memory
+//            (cp.async, double buffered) and write to the CTA's workspace
+//            slice the first derivatives (deriv42), the upwind advective
+//            derivatives (deriv42adv), for alpha, psi, beta0-2, gt0-5 the
+//            second and mixed derivatives (mixed = d_y(d_x u), d_z(d_x u),
+//            d_z(d_y u) as CCZ4_GR/scripts/ccz4rhs_derivs.h composes them),
+//            and for every field but theta_z4 the KO sum kx + ky + kz;
+//   phase A  one thread per tile point: the generated algebra
+//            (ccz4_algebra.cuh), ccz4_bcs on flagged faces (every variable
+//            but theta_z4) and rhs += sigma * KO (every variable but
+//            theta_z4, CCZ4_GR/src/rhs.cpp:241-283).
+// The first derivatives of At0-5 and B0-2 feed only the boundary condition
+// and are formed on domain-boundary blocks only.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ccz4_algebra.cuh"
+#include "dgb_internal.h"
+#include "exact_mul.cuh"
+#include "stencil42.cuh"
+
+namespace dgb {
+namespace {
+
+constexpr int kC4Threads = 256;
+constexpr int kC4Theta = 24;
+// VAR -> second-derivative group (alpha, psi, beta0-2, gt0-5) or -1
+__constant__ int8_t c_c4d2[NV4] = {0, 1, -1, -1, -1, -1, 2, 3, 4, -1, -1, -1,
+                                   5, 6, 7, 8, 9, 10, -1, -1, -1, -1, -1, -1, -1};
+// ccz4_bcs falloff / asymptotic per variable (CCZ4_GR/src/rhs.cpp:168-231)
+__constant__ double c_c4fall[NV4] = {1, 1, 1, 2, 2, 2, 1, 1, 1, 1, 1, 1,
+                                     1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2, 0};
+__constant__ double c_c4asym[NV4] = {1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+                                     1, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0, 0, 0};
+
+__device__ __forceinline__ void c4_cp_async8(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void c4_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void c4_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+template <int TX, int TY, int TZ>
+struct C4Geo {
+    static constexpr int PX = TX + 6, PY = TY + 6, PZ = TZ + 6;
+    static constexpr int FBUF = PX * PY * PZ;
+    static constexpr int DXB = TX * (TY + 4) * (TZ + 4);  // d_x on the +-2 cross region
+    static constexpr int DYB = TX * TY * (TZ + 4);
+    static constexpr int PMAX = TX * TY * TZ;
+    static constexpr size_t bytes = (size_t)(2 * FBUF + DXB + DYB + 3 * PMAX) * 8;
+};
+
+struct C4AlgPrm {
+    double l1, l2, l3, l4, lf0, lf1, k1, k2, p;
+};
+
+struct C4IO {
+    const double *const *uu;
+    double *const *rr;
+    const double *S;
+    int pmax, p;
+    uint64_t gi;
+    double sigma;
+    bool face;            // on a flagged domain face: ccz4_bcs replaces the algebra
+    double x, y, z, ninv_r;
+    __device__ __forceinline__ double u(int v) const { return __ldg(uu[v] + gi); }
+    __device__ __forceinline__ double d(int s) const { return S[(size_t)s * pmax + p]; }
+    __device__ __forceinline__ void out(int v, double val) const
+    {
+        if (v == kC4Theta) {
+            rr[v][gi] = val;
+            return;
+        }
+        if (face) {
+            // -(1/r)(x f_x + y f_y + z f_z + falloff (f - asymptotic))
+            const double f = __ldg(uu[v] + gi);
+            double t = __dadd_rn(__dmul_rn(x, d(3 * v)), __dmul_rn(y, d(3 * v + 1)));
+            t = __dadd_rn(t, __dmul_rn(z, d(3 * v + 2)));
+            t = __dadd_rn(t, __dmul_rn(c_c4fall[v], __dsub_rn(f, c_c4asym[v])));
+            val = __dmul_rn(ninv_r, t);
+        }
+        rr[v][gi] = __dadd_rn(val, __dmul_rn(sigma, d(DGB_CCZ4_NUM_DERIV + v)));
+    }
+};
+
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, const DevBlock &blk,
+                                        double *S)
+{
+    using G = C4Geo<TX, TY, TZ>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *fb0 = reinterpret_cast<double *>(smem_raw);
+    double *fb1 = fb0 + G::FBUF;
+    double *dxb = fb1 + G::FBUF;
+    double *dyb = dxb + G::DXB;
+    double *bet = dyb + G::DYB;  // beta0..2 at the tile points
+    const int tid = threadIdx.x;
+    const int nx = blk.sz[0], ny = blk.sz[1], nz = blk.sz[2];
+    const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
+    const int px = ex + 6, py = ey + 6, pz = ez + 6;
+    const int npad = px * py * pz;
+    const int P = ex * ey * ez;
+    const int sy = px, sz = px * py;
+    const uint64_t rbase = blk.offset + (uint64_t)w.o[0]
+                         + (uint64_t)nx * ((uint64_t)w.o[1] + (uint64_t)ny * w.o[2]);
+    const uint32_t bflag = blk.bflag;
+    const bool lo[3] = {(bflag & 1u) != 0, (bflag & 4u) != 0, (bflag & 16u) != 0};
+    const bool hi[3] = {(bflag & 2u) != 0, (bflag & 8u) != 0, (bflag & 32u) != 0};
+    const Ax4 ax[3] = {ax4(blk.h[0]), ax4(blk.h[1]), ax4(blk.h[2])};
+    const int nn[3] = {nx, ny, nz};
+
+    for (int p = tid; p < P; p += kC4Threads) {
+        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        const uint64_t gi = blk.offset + (uint64_t)(w.o[0] + ti + 3)
+                          + (uint64_t)nx * ((uint64_t)(w.o[1] + tj + 3) + (uint64_t)ny * (w.o[2] + tk + 3));
+        bet[p] = __ldg(args.u[6] + gi);
+        bet[G::PMAX + p] = __ldg(args.u[7] + gi);
+        bet[2 * G::PMAX + p] = __ldg(args.u[8] + gi);
+    }
+
+    auto issue_load = [&](int v, double *dst) {
+        const double *src = args.u[v] + rbase;
+        for (int q = tid; q < npad; q += kC4Threads) {
+            const int i = q % px, r = q / px, j = r % py, k = r / py;
+            c4_cp_async8(dst + q, src + i + (uint64_t)nx * (j + (uint64_t)ny * k));
+        }
+        c4_commit();
+    };
+
+    issue_load(0, fb0);
+    for (int v = 0; v < NV4; v++) {
+        double *F = (v & 1) ? fb1 : fb0;
+        if (v + 1 < NV4) {
+            issue_load(v + 1, (v & 1) ? fb0 : fb1);
+            c4_wait<1>();
+        } else {
+            c4_wait<0>();
+        }
+        __syncthreads();
+        const int q2 = c_c4d2[v];
+        double *Sg = S + (size_t)(3 * v) * G::PMAX;
+        double *Sa = S + (size_t)(DGB_CCZ4_ADV0 + 3 * v) * G::PMAX;
+        double *Sko = S + (size_t)(DGB_CCZ4_NUM_DERIV + v) * G::PMAX;
+        // At0-5, B0-2: first derivatives only for the boundary condition
+        const bool want_grad = bflag != 0 || !((v >= 9 && v <= 11) || (v >= 18 && v <= 23));
+        if (q2 < 0) {
+            for (int p = tid; p < P; p += kC4Threads) {
+                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
+                const int st[3] = {1, sy, sz};
+                const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                double ko = 0.0;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    if (want_grad) Sg[d * G::PMAX + p] = d1_42_at(c, st[d], pos[d], nn[d], lo[d], hi[d], ax[d]);
+                    Sa[d * G::PMAX + p] = adv42_at(c, st[d], pos[d], nn[d], lo[d], hi[d],
+                                                   bet[d * G::PMAX + p], ax[d]);
+                    if (v != kC4Theta) {
+                        const double k = ko42c_at(c, st[d], pos[d], nn[d], lo[d], hi[d], ax[d]);
+                        ko = d == 0 ? k : __dadd_rn(ko, k);
+                    }
+                }
+                if (v != kC4Theta) Sko[p] = ko;
+            }
+        } else {
+            double *S2 = S + (size_t)(DGB_CCZ4_D20 + 6 * q2) * G::PMAX;
+            // (1a) d_x on x in tile and (y in tile +- 2, z in tile) or (y in tile, z halo of 2)
+            const int by = ey + 4;
+            const int nA = ex * by * ez, nB = ex * ey * 4;
+            for (int q = tid; q < nA + nB; q += kC4Threads) {
+                int ti, tj, tk;  // box coordinates: tj in [0, ey+4), tk in [0, ez+4)
+                if (q < nA) {
+                    ti = q % ex; const int r = q / ex; tj = r % by; tk = r / by + 2;
+                } else {
+                    const int q3 = q - nA;
+                    ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 2;
+                    const int kk = r / ey;  // 0..3
+                    tk = kk < 2 ? kk : ez + kk;
+                }
+                const double *c = F + (ti + 3) + sy * (tj + 1) + sz * (tk + 1);
+                dxb[ti + ex * (tj + by * tk)] = d1_42_at(c, 1, w.o[0] + ti + 3, nx, lo[0], hi[0], ax[0]);
+            }
+            // (1b) d_y on x, y in tile, z in tile +- 2
+            const int nC = ex * ey * (ez + 4);
+            for (int q = tid; q < nC; q += kC4Threads) {
+                const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
+                const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 1);
+                dyb[q] = d1_42_at(c, sy, w.o[1] + tj + 3, ny, lo[1], hi[1], ax[1]);
+            }
+            // (1c) pointwise: d_z, xx, yy, zz, advective, KO
+            for (int p = tid; p < P; p += kC4Threads) {
+                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
+                const int st[3] = {1, sy, sz};
+                const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                Sg[2 * G::PMAX + p] = d1_42_at(c, sz, pos[2], nz, lo[2], hi[2], ax[2]);
+                S2[0 * G::PMAX + p] = d2_42_at(c, 1, pos[0], nx, lo[0], hi[0], ax[0]);
+                S2[3 * G::PMAX + p] = d2_42_at(c, sy, pos[1], ny, lo[1], hi[1], ax[1]);
+                S2[5 * G::PMAX + p] = d2_42_at(c, sz, pos[2], nz, lo[2], hi[2], ax[2]);
+                double ko = 0.0;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    Sa[d * G::PMAX + p] = adv42_at(c, st[d], pos[d], nn[d], lo[d], hi[d],
+                                                   bet[d * G::PMAX + p], ax[d]);
+                    const double k = ko42c_at(c, st[d], pos[d], nn[d], lo[d], hi[d], ax[d]);
+                    ko = d == 0 ? k : __dadd_rn(ko, k);
+                }
+                Sko[p] = ko;
+            }
+            __syncthreads();
+            // (2) mixed from the boxes; d_x, d_y at the tile points
+            for (int p = tid; p < P; p += kC4Threads) {
+                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                const int pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
+                const double *cx = dxb + ti + ex * ((tj + 2) + by * (tk + 2));
+                const double *cy = dyb + ti + ex * (tj + ey * (tk + 2));
+                Sg[p] = cx[0];
+                Sg[G::PMAX + p] = cy[0];
+                S2[1 * G::PMAX + p] = d1_42_at(cx, ex, pj, ny, lo[1], hi[1], ax[1]);
+                S2[2 * G::PMAX + p] = d1_42_at(cx, ex * by, pk, nz, lo[2], hi[2], ax[2]);
+                S2[4 * G::PMAX + p] = d1_42_at(cy, ex * ey, pk, nz, lo[2], hi[2], ax[2]);
+            }
+        }
+        __syncthreads();  // F and the boxes are reused
+    }
+
+    const C4AlgPrm aprm{args.prm.l1, args.prm.l2, args.prm.l3, args.prm.l4, args.prm.lf0,
+                        args.prm.lf1, args.prm.k1, args.prm.k2, args.prm.p};
+    for (int p = tid; p < P; p += kC4Threads) {
+        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        const int i = w.o[0] + ti + 3, j = w.o[1] + tj + 3, k = w.o[2] + tk + 3;
+        const uint64_t gi = blk.offset + (uint64_t)i + (uint64_t)nx * ((uint64_t)j + (uint64_t)ny * k);
+        // coordinates and radius with the reference's roundings (rhs.cpp:147-160)
+        const double x = __dadd_rn(blk.pmin[0], __dmul_rn((double)i, blk.h[0]));
+        const double y = __dadd_rn(blk.pmin[1], __dmul_rn((double)j, blk.h[1]));
+        const double z = __dadd_rn(blk.pmin[2], __dmul_rn((double)k, blk.h[2]));
+        const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+        const double rr = __dsqrt_rn(r2);
+        double eta = args.prm.eta_const;
+        if (rr >= args.prm.eta_r0) {
+            const double q = args.prm.eta_r0 / rr;
+            eta *= (args.prm.eta_exp == 1.0) ? q : pow(q, args.prm.eta_exp);
+        }
+        const bool face = bflag != 0 && ((lo[0] && i == 3) || (hi[0] && i == nx - 4) ||
+                                         (lo[1] && j == 3) || (hi[1] && j == ny - 4) ||
+                                         (lo[2] && k == 3) || (hi[2] && k == nz - 4));
+        const double ninv_r = face ? -__ddiv_rn(1.0, rr) : 0.0;
+        C4IO io{args.u, args.rhs, S, G::PMAX, p, gi, args.prm.sigma, face, x, y, z, ninv_r};
+        dgb_ccz4_algebra(io, aprm, eta);
+    }
+}
+
+template <int TX, int TY, int TZ>
+__global__ void __launch_bounds__(kC4Threads, 1) c4_kernel(const C4Args args)
+{
+    using G = C4Geo<TX, TY, TZ>;
+    __shared__ int s_item;
+    double *S = args.scratch + (size_t)blockIdx.x * DGB_CCZ4_NUM_SLOTS * G::PMAX;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(args.queue, 1u);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= (int)args.nitems) break;
+        const WorkItem w = args.items[it];
+        const DevBlock blk = args.blocks[w.blk];
+        c4_item<TX, TY, TZ>(args, w, blk, S);
+    }
+}
+
+}  // namespace
+
+size_t c4_smem_bytes() { return C4Geo<8, 8, 8>::bytes; }
+size_t c4_scratch_per_cta() { return (size_t)DGB_CCZ4_NUM_SLOTS * C4Geo<8, 8, 8>::PMAX; }
+
+cudaError_t c4_configure()
+{
+    return cudaFuncSetAttribute(c4_kernel<8, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)C4Geo<8, 8, 8>::bytes);
+}
+
+int c4_max_ctas_per_sm()
+{
+    int n = 0;
+    if (c4_configure() != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, c4_kernel<8, 8, 8>, kC4Threads,
+                                                      C4Geo<8, 8, 8>::bytes) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+cudaError_t c4_launch(const C4Args &args, int grid, cudaStream_t stream)
+{
+    c4_kernel<8, 8, 8><<<grid, kC4Threads, C4Geo<8, 8, 8>::bytes, stream>>>(args);
+    return cudaGetLastError();
+}
+
+}  // namespace dgb

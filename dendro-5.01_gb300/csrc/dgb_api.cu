@@ -52,6 +52,10 @@ struct dgb_plan {
     size_t scratch_doubles = 0;
     int occupancy[8][2] = {};  // resident CTAs per SM per (variant, precision)
     int pc_occupancy = 0;      // constraint kernel, resident CTAs per SM (0 = not yet known)
+    // CCZ4 kernel: its own workspace (241 slots per point), allocated at first use
+    int c4_occupancy = 0;
+    double *d_scratch4 = nullptr;
+    size_t scratch4_doubles = 0;
     // device copies for the host-array entry point
     double *d_u = nullptr, *d_rhs = nullptr;
 };
@@ -280,6 +284,7 @@ dgb_status dgb_plan_destroy(dgb_plan *p)
     for (auto d : p->d_items) cudaFree(d);
     cudaFree(p->d_queue);
     cudaFree(p->d_scratch);
+    cudaFree(p->d_scratch4);
     cudaFree(p->d_u);
     cudaFree(p->d_rhs);
     delete p;
@@ -350,6 +355,57 @@ dgb_status dgb_physical_constraints(dgb_plan *p, double *const *cons, const doub
     cudaStream_t st = (cudaStream_t)stream;
     DGB_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned int), st));
     DGB_CUDA(physcon_launch(a, grid, st));
+    return DGB_OK;
+}
+
+dgb_status dgb_ccz4_rhs(dgb_plan *p, const dgb_ccz4_params *prm, double *const *rhs,
+                        const double *const *u, int precision, void *stream)
+{
+    if (!p || !prm || !rhs || !u) {
+        set_error("dgb_ccz4_rhs: null argument");
+        return DGB_ERR_INVALID;
+    }
+    for (int v = 0; v < NV4; v++)
+        if (!rhs[v] || !u[v]) {
+            set_error("dgb_ccz4_rhs: null field pointer");
+            return DGB_ERR_INVALID;
+        }
+    if (precision != DGB_PREC_FP64) {
+        set_error("dgb_ccz4_rhs: only DGB_PREC_FP64 is built for CCZ4");
+        return DGB_ERR_UNSUPPORTED;
+    }
+    dgb_status s = build_items(p, 0);  // the 8x8x8 schedule
+    if (s != DGB_OK) return s;
+    if (p->nitems[0] == 0) return DGB_OK;
+    if (p->c4_occupancy == 0) {
+        const int occ = c4_max_ctas_per_sm();
+        if (occ < 1) {
+            set_error("dgb_ccz4_rhs: kernel cannot be resident");
+            return DGB_ERR_CUDA;
+        }
+        const size_t need = c4_scratch_per_cta() * (size_t)occ * (size_t)p->nsm;
+        DGB_CUDA(cudaMalloc(&p->d_scratch4, need * sizeof(double)));
+        p->scratch4_doubles = need;
+        p->c4_occupancy = occ;
+    }
+    DGB_CUDA(c4_configure());
+    C4Args a;
+    for (int v = 0; v < NV4; v++) {
+        a.u[v] = u[v];
+        a.rhs[v] = rhs[v];
+    }
+    a.blocks = p->d_blocks;
+    a.items = p->d_items[0];
+    a.nitems = p->nitems[0];
+    a.queue = p->d_queue;
+    a.scratch = p->d_scratch4;
+    a.prm = C4Params{prm->lambda[0], prm->lambda[1], prm->lambda[2], prm->lambda[3],
+                     prm->lambda_f[0], prm->lambda_f[1], prm->kappa[0], prm->kappa[1],
+                     prm->p_expo, prm->eta_const, prm->eta_r0, prm->eta_damping_exp,
+                     prm->ko_sigma};
+    cudaStream_t st = (cudaStream_t)stream;
+    DGB_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned int), st));
+    DGB_CUDA(c4_launch(a, p->nsm * p->c4_occupancy, st));
     return DGB_OK;
 }
 

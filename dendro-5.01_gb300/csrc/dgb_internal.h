@@ -74,6 +74,28 @@ cudaError_t synth_fill_launch(const DevBlock *blocks, uint32_t nblk, const uint6
                               uint64_t total, double *const *u, int v0, int v1, uint64_t seed,
                               double noise, cudaStream_t stream);
 
+// CCZ4 right-hand side (ccz4_rhs.cu): 25 variables, CCZ4_GR/include/grUtils.h:46.
+constexpr int NV4 = 25;
+struct C4Params {
+    double l1, l2, l3, l4, lf0, lf1, k1, k2, p;
+    double eta_const, eta_r0, eta_exp, sigma;
+};
+struct C4Args {
+    const double *u[NV4];
+    double *rhs[NV4];
+    const DevBlock *blocks;
+    const WorkItem *items;   // the 8x8x8 schedule (tile variant 0)
+    uint32_t nitems;
+    unsigned int *queue;
+    double *scratch;
+    C4Params prm;
+};
+size_t c4_smem_bytes();
+size_t c4_scratch_per_cta();  // doubles
+cudaError_t c4_configure();
+int c4_max_ctas_per_sm();
+cudaError_t c4_launch(const C4Args &args, int grid, cudaStream_t stream);
+
 // Constraint diagnostics (physcon.cu).
 struct PcArgs {
     const double *u[NV];

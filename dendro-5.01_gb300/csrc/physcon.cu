@@ -24,6 +24,7 @@
 
 #include "dgb_internal.h"
 #include "exact_mul.cuh"
+#include "stencil42.cuh"
 
 namespace dgb {
 namespace {
@@ -43,80 +44,6 @@ enum { Q_CHI = 0, Q_GT = 1, Q_K = 4, Q_G = 5, Q_A = 11 };
 __host__ __device__ constexpr int sy(int a, int b)
 {
     return (a < b ? a : b) == 0 ? (a < b ? b : a) : ((a < b ? a : b) == 1 ? 2 + (a < b ? b : a) : 5);
-}
-
-// ---------------------------------------------------------------- stencils
-// deriv42: (u[-2] - 8u[-1] + 8u[1] - u[2]) * ((1/h)/12), left to right, one
-// rounding per operation (products by 8 and 16 are exact, by 3, 5 and 30
-// are formed exactly on the integer pipes, exact_mul.cuh).
-struct Ax4 {
-    double c12, half, c12sq, sq;  // (1/h)/12, 0.5/h, (1/h^2)/12, 1/h^2
-};
-__device__ __forceinline__ Ax4 ax4(double h)
-{
-    Ax4 a;
-    const double ih = 1.0 / h, ih2 = 1.0 / (h * h);
-    a.c12 = ih / 12.0;
-    a.half = 0.5 * ih;
-    a.c12sq = ih2 / 12.0;
-    a.sq = ih2;
-    return a;
-}
-
-__device__ __forceinline__ double d1_42(const double *u, int s, double c12)
-{
-    double t = __dsub_rn(u[-2 * s], 8.0 * u[-s]);
-    t = __dadd_rn(t, 8.0 * u[s]);
-    t = __dsub_rn(t, u[2 * s]);
-    return __dmul_rn(t, c12);
-}
-__device__ __forceinline__ double d2_42(const double *u, int s, double c12sq)
-{
-    double t = __dadd_rn(-u[-2 * s], 16.0 * u[-s]);
-    t = __dsub_rn(t, dgb_mul_const<30>(u[0]));
-    t = __dadd_rn(t, 16.0 * u[s]);
-    t = __dsub_rn(t, u[2 * s]);
-    return __dmul_rn(t, c12sq);
-}
-
-// at index pos of an axis of n points (c points at that value, stride s)
-__device__ __forceinline__ double d1_42_at(const double *c, int s, int pos, int n, bool lo, bool hi,
-                                           const Ax4 &a)
-{
-    if (lo && pos == 3) {
-        double t = __dadd_rn(-dgb_mul_const<3>(c[0]), 4.0 * c[s]);
-        return __dmul_rn(__dsub_rn(t, c[2 * s]), a.half);
-    }
-    if (lo && pos == 4) return __dmul_rn(__dadd_rn(-c[-s], c[s]), a.half);
-    if (hi && pos == n - 5) return __dmul_rn(__dadd_rn(-c[-s], c[s]), a.half);
-    if (hi && pos == n - 4) {
-        double t = __dsub_rn(c[-2 * s], 4.0 * c[-s]);
-        return __dmul_rn(__dadd_rn(t, dgb_mul_const<3>(c[0])), a.half);
-    }
-    return d1_42(c, s, a.c12);
-}
-__device__ __forceinline__ double d2_42_at(const double *c, int s, int pos, int n, bool lo, bool hi,
-                                           const Ax4 &a)
-{
-    if (lo && pos == 3) {
-        double t = __dsub_rn(2.0 * c[0], dgb_mul_const<5>(c[s]));
-        t = __dadd_rn(t, 4.0 * c[2 * s]);
-        return __dmul_rn(__dsub_rn(t, c[3 * s]), a.sq);
-    }
-    if (lo && pos == 4) {
-        double t = __dsub_rn(c[-s], 2.0 * c[0]);
-        return __dmul_rn(__dadd_rn(t, c[s]), a.sq);
-    }
-    if (hi && pos == n - 5) {
-        double t = __dsub_rn(c[-s], 2.0 * c[0]);
-        return __dmul_rn(__dadd_rn(t, c[s]), a.sq);
-    }
-    if (hi && pos == n - 4) {
-        double t = __dadd_rn(-c[-3 * s], 4.0 * c[-2 * s]);
-        t = __dsub_rn(t, dgb_mul_const<5>(c[-s]));
-        return __dmul_rn(__dadd_rn(t, 2.0 * c[0]), a.sq);
-    }
-    return d2_42(c, s, a.c12sq);
 }
 
 __device__ __forceinline__ void cp_async8(void *smem, const void *gmem)

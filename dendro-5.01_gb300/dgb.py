@@ -119,6 +119,7 @@ _SIGS = {
                                             C.POINTER(C.c_double), C.POINTER(C.c_uint32),
                                             C.c_uint32, C.POINTER(BssnParams), C.c_void_p]),
     "dgb_plan_autotune": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
+    "dgb_ccz4_rhs": (C.c_int, [C.c_void_p, C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
     "dgb_physical_constraints": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_void_p]),
     "dgb_constraint_l2": (C.c_int, [PtrArr, C.c_int, C.c_void_p, C.c_double, C.c_uint64,
                                     C.POINTER(C.c_double), C.c_void_p]),
@@ -273,6 +274,13 @@ class Plan:
         r, k1 = host_ptrs(rhs_arrays)
         u, k2 = host_ptrs(u_arrays)
         check(lib().dgb_bssn_rhs_host(self.h, r, u, precision), "dgb_bssn_rhs_host")
+
+    def ccz4_rhs(self, params, rhs_ptrs, u_ptrs, precision=PREC_FP64, stream=0):
+        """CCZ4 right-hand side (25 device arrays each) over the plan's blocks."""
+        r, k1 = ptr_array(rhs_ptrs)
+        u, k2 = ptr_array(u_ptrs)
+        check(lib().dgb_ccz4_rhs(self.h, C.byref(params), r, u, precision, C.c_void_p(stream)),
+              "dgb_ccz4_rhs")
 
     def physical_constraints(self, cons_ptrs, u_ptrs, stream=0):
         """ham, mom0-2, psi4_real, psi4_img at every block interior point."""

@@ -139,6 +139,33 @@ dgb_status dgb_plan_tile(const dgb_plan *plan, int precision, uint32_t *tile3);
 int dgb_num_tile_variants(void);
 dgb_status dgb_plan_set_tile_variant(dgb_plan *plan, int precision, int variant);
 
+/* The ccz4:: globals ccz4rhs reads (CCZ4_GR/include/parameters.h):
+ * CCZ4_LAMBDA, CCZ4_LAMBDA_F, CCZ4_KAPPA, P_EXPO, ETA_*, KO_DISS_SIGMA. */
+typedef struct {
+    double lambda[4];
+    double lambda_f[2];
+    double kappa[2];
+    double p_expo;
+    double eta_const;
+    double eta_r0;
+    double eta_damping_exp;
+    double ko_sigma;
+} dgb_ccz4_params;
+#define DGB_CCZ4_NUM_VARS 25
+
+/* CCZ4 right-hand side over every block of a plan, device pointers:
+ * replaces the per-block loop over ccz4rhs (CCZ4_GR/src/rhs.cpp:12-298,
+ * called from CCZ4_GR/src/rk4CCZ4.cpp:498/584).  rhs and u are 25 arrays in
+ * CCZ4 variable order (alpha, psi, K, Gh0-2, beta0-2, B0-2, gt0-5, At0-5,
+ * theta_z4, CCZ4_GR/include/grUtils.h:46); interior points are written,
+ * padding untouched.  The CCZ4 solver's 4th-order stencils (upwind advective
+ * derivatives, its KO form), ccz4_bcs on flagged faces, KO on every variable
+ * but theta_z4.  FP64 (DGB_PREC_MIXED returns DGB_ERR_UNSUPPORTED).  The
+ * plan's block list is used; its BSSN parameters are not.  Asynchronous on
+ * `stream`; calls on one plan must be ordered on one stream. */
+dgb_status dgb_ccz4_rhs(dgb_plan *plan, const dgb_ccz4_params *prm, double *const *rhs,
+                        const double *const *u, int precision, void *stream);
+
 /* Constraint diagnostics over every block of a plan, device pointers:
  * replaces the per-block loop over physical_constraints (BSSN_GR/src/physcon.cpp:12-96,
  * called from BSSN_GR/src/bssnCtx.cpp:332-355 and rkBSSN.cpp:1659).

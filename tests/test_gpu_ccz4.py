@@ -1,0 +1,141 @@
+"""Parity of the CUDA CCZ4 right-hand side (through the C ABI) with the CCZ4
+oracle and the reference's golden vectors: ccz4rhs (CCZ4_GR/src/rhs.cpp:12-298)
+within 1e-12 normwise per field, padding untouched, the boundary condition on
+flagged faces, theta_z4 left out of KO."""
+import os
+
+import numpy as np
+import pytest
+
+from workloads import SEED1, SEED2, interior_mask, normwise, repack, sample_uneven
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "ccz4_reference.npz")
+
+
+def ccz4_fields(dgb, blocks, seed):
+    n = dgb.unzipped_size(blocks)
+    u = [np.zeros(n) for _ in range(25)]
+    dgb.synth_fill_host(blocks, u, seed, 1e-6)
+    return u
+
+
+def gpu_ccz4(dgb, torch, blocks, u, params, fill=7.0):
+    plan = dgb.Plan(blocks, dgb.default_params(0.1))
+    du = [torch.from_numpy(a).cuda() for a in u]
+    n = len(u[0])
+    dr = [torch.full((n,), fill, dtype=torch.float64, device="cuda") for _ in range(25)]
+    plan.ccz4_rhs(params, [t.data_ptr() for t in dr], [t.data_ptr() for t in du])
+    torch.cuda.synchronize()
+    out = [t.cpu().numpy() for t in dr]
+    plan.close()
+    return out
+
+
+def oracle_ccz4(dgb, oracle, blocks, u, params):
+    n = len(u[0])
+    r = [np.zeros(n) for _ in range(25)]
+    assert oracle.ccz4rhs_blocks(r, u, blocks, dgb.ccz4_params_vector(params)) == 0
+    return r
+
+
+@pytest.mark.parametrize("which", ["uniform512", "uneven_sample"])
+def test_ccz4_matches_oracle(dgb, gpu, oracle, which):
+    torch = gpu
+    if which == "uniform512":
+        blocks, seed = dgb.synth_blocks(1), SEED1
+    else:
+        allb = dgb.synth_blocks(2, SEED2)
+        blocks, seed = repack(dgb, allb, sample_uneven(allb)), SEED2
+    u = ccz4_fields(dgb, blocks, seed)
+    prm = dgb.default_ccz4_params()
+    got = gpu_ccz4(dgb, torch, blocks, u, prm)
+    want = oracle_ccz4(dgb, oracle, blocks, u, prm)
+    mask = interior_mask(blocks, len(u[0]))
+    err = normwise(got, want, mask)
+    assert np.all(err <= FP64_TOL), dict(zip(dgb.CCZ4_VAR_NAMES, err))
+    for v in range(25):
+        assert np.all(got[v][~mask] == 7.0)
+
+
+def face_mask(blocks, n):
+    """Interior points minus the boundary layer of each flagged face."""
+    m = np.zeros(n, dtype=bool)
+    for b in blocks:
+        nx, ny, nz = b.sz
+        sel = np.zeros((nz, ny, nx), dtype=bool)
+        sel[3:nz - 3, 3:ny - 3, 3:nx - 3] = True
+        f = b.bflag
+        if f & 1: sel[:, :, 3] = False
+        if f & 2: sel[:, :, nx - 4] = False
+        if f & 4: sel[:, 3, :] = False
+        if f & 8: sel[:, ny - 4, :] = False
+        if f & 16: sel[3, :, :] = False
+        if f & 32: sel[nz - 4, :, :] = False
+        m[b.offset + np.flatnonzero(sel.ravel())] = True
+    return m
+
+
+def test_ccz4_matches_reference_golden(dgb, gpu):
+    """Against the reference's own outputs (the harness has no ccz4_bcs, so
+    the boundary layer of flagged faces is left out of the comparison)."""
+    torch = gpu
+    g = np.load(GOLDEN)
+    allb = dgb.synth_blocks(1)
+    rows, off = [], 0
+    for i, f in g["picks"]:
+        b = allb[int(i)]
+        rows.append((off, tuple(b.sz), int(f), tuple(b.ptmin), tuple(b.ptmax)))
+        off += b.sz[0] * b.sz[1] * b.sz[2]
+    blocks = dgb.blocks_array(rows)
+    u = ccz4_fields(dgb, blocks, int(g["seed"]))
+    got = gpu_ccz4(dgb, torch, blocks, u, dgb.default_ccz4_params())
+    n = len(u[0])
+    mask = interior_mask(blocks, n)
+    keep = face_mask(blocks, n)[mask]
+    err = normwise([x[mask][keep] for x in got], [w[keep] for w in g["rhs"]],
+                   np.ones(int(keep.sum()), dtype=bool))
+    assert np.all(err <= FP64_TOL), dict(zip(dgb.CCZ4_VAR_NAMES, err))
+
+
+def test_ccz4_boundary_blocks(dgb, gpu, oracle):
+    """Closures and ccz4_bcs on every face class; NaN beyond flagged faces."""
+    from test_oracle import boundary_blocks
+    torch = gpu
+    blocks = boundary_blocks(dgb)
+    u = ccz4_fields(dgb, blocks, SEED1)
+    for b in blocks:
+        nx, ny, nz = b.sz
+        for v in range(25):
+            a = u[v][b.offset:b.offset + nx * ny * nz].reshape(nz, ny, nx)
+            if b.bflag & 1: a[:, :, :3] = np.nan
+            if b.bflag & 2: a[:, :, nx - 3:] = np.nan
+            if b.bflag & 4: a[:, :3, :] = np.nan
+            if b.bflag & 8: a[:, ny - 3:, :] = np.nan
+            if b.bflag & 16: a[:3, :, :] = np.nan
+            if b.bflag & 32: a[nz - 3:, :, :] = np.nan
+    prm = dgb.default_ccz4_params()
+    got = gpu_ccz4(dgb, torch, blocks, u, prm)
+    want = oracle_ccz4(dgb, oracle, blocks, u, prm)
+    mask = interior_mask(blocks, len(u[0]))
+    assert all(np.isfinite(x[mask]).all() for x in got)
+    err = normwise(got, want, mask)
+    assert np.all(err <= FP64_TOL), dict(zip(dgb.CCZ4_VAR_NAMES, err))
+
+
+def test_ccz4_theta_not_dissipated_and_fp64_only(dgb, gpu):
+    torch = gpu
+    blocks = repack(dgb, dgb.synth_blocks(1), [100, 101])
+    u = ccz4_fields(dgb, blocks, 5)
+    r0 = gpu_ccz4(dgb, torch, blocks, u, dgb.default_ccz4_params(ko_sigma=0.0))
+    r1 = gpu_ccz4(dgb, torch, blocks, u, dgb.default_ccz4_params(ko_sigma=0.4))
+    assert np.array_equal(r0[24], r1[24])
+    assert not np.array_equal(r0[0], r1[0])
+    plan = dgb.Plan(blocks, dgb.default_params(0.1))
+    du = [torch.from_numpy(a).cuda() for a in u]
+    with pytest.raises(dgb.DgbError):
+        plan.ccz4_rhs(dgb.default_ccz4_params(), [t.data_ptr() for t in du],
+                      [t.data_ptr() for t in du], dgb.PREC_MIXED)
+    plan.close()
