@@ -98,3 +98,10 @@ def test_generated_algebra_up_to_date():
     out = subprocess.run([sys.executable, gen], capture_output=True, text=True, check=True).stdout
     cur = open(os.path.join(ROOT, "dendro-5.01_gb300", "csrc", "bssn_algebra.cuh")).read()
     assert out == cur, "csrc/bssn_algebra.cuh is stale: rerun codegen/gen_bssn_algebra.py"
+
+
+def test_generated_ccz4_algebra_up_to_date():
+    gen = os.path.join(ROOT, "dendro-5.01_gb300", "codegen", "gen_ccz4_algebra.py")
+    out = subprocess.run([sys.executable, gen], capture_output=True, text=True, check=True).stdout
+    cur = open(os.path.join(ROOT, "dendro-5.01_gb300", "csrc", "ccz4_algebra.cuh")).read()
+    assert out == cur, "csrc/ccz4_algebra.cuh is stale: rerun codegen/gen_ccz4_algebra.py"
