@@ -36,6 +36,10 @@ METRIC = ("BSSN RK4 grid-pts×vars/s on 1 GB300 (FP64 vs mixed), % roofline, vs 
 # Algorithmic FP64 operations per interior point per RHS, 6th order with
 # the reference binding (centred advective, 7-point KO): 8,223.
 FLOP_PER_POINT = 8223.0
+# CCZ4 (4th order, the reference's set: 75 first + 36 mixed + 36 second +
+# 75 upwind + 75 KO stencils, "reduced ops 4633" algebra, KO accumulate):
+# 75*8 + 36*16 + 36*10 + 75*10 + 75*14 + 4633 + 24*4 = 8,065.
+FLOP_PER_POINT_CCZ4 = 8065.0
 SEED2 = 20261203 + 2
 SEED1 = 20261203 + 1
 
@@ -124,26 +128,37 @@ def cpu_sample(blocks, fraction):
     return sorted(idx)
 
 
-def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1):
-    """Times the oracle port of the reference CPU path on all host cores."""
+def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="bssn"):
+    """Times the oracle port of the reference CPU path on all host cores
+    (system "bssn": bssnrhs; "ccz4": ccz4rhs with its 25 variables)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from workloads import repack
     ora = oracle_py.Oracle()
     cores = os.cpu_count() or 1
-    prm = dgb.params_vector(dgb.default_params(sigma))
+    nv = 25 if system == "ccz4" else 24
+    if system == "ccz4":
+        prm = dgb.ccz4_params_vector(dgb.default_ccz4_params(ko_sigma=sigma))
+
+        def call(r, u, sub):
+            return ora.ccz4rhs_blocks(r, u, sub, prm, True, cores)
+    else:
+        prm = dgb.params_vector(dgb.default_params(sigma))
+
+        def call(r, u, sub):
+            return ora.bssnrhs_blocks(r, u, sub, prm, cores)
     # calibrate on a small sample, then size the sample to ~target_s
     frac = 1.0 / 400
     times = []
     for attempt in range(3):
         idx = cpu_sample(blocks, frac)
         sub = repack(dgb, blocks, idx)
-        u = [np.zeros(dgb.unzipped_size(sub)) for _ in range(24)]
+        u = [np.zeros(dgb.unzipped_size(sub)) for _ in range(nv)]
         dgb.synth_fill_host(sub, u, seed, 1e-6)
-        r = [np.zeros_like(u[0]) for _ in range(24)]
+        r = [np.zeros_like(u[0]) for _ in range(nv)]
         t0 = time.perf_counter()
-        assert ora.bssnrhs_blocks(r, u, sub, prm, cores) == 0
+        assert call(r, u, sub) == 0
         dt = time.perf_counter() - t0
         if dt > 0.25 * target_s or frac >= 1.0:
             break
@@ -152,12 +167,13 @@ def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1):
     vals = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        assert ora.bssnrhs_blocks(r, u, sub, prm, cores) == 0
-        vals.append(pts * 24 / (time.perf_counter() - t0))
+        assert call(r, u, sub) == 0
+        vals.append(pts * nv / (time.perf_counter() - t0))
     return {"value": float(np.median(vals)), "unit": "grid-pts*vars/s", "cores": cores,
             "kind": "port",
             "sample": f"{len(sub)} of {len(blocks)} blocks (stratified by size, "
-                      f"{pts} interior points), FP64, OpenMP over blocks"}, vals
+                      f"{pts} interior points), FP64, OpenMP over blocks, "
+                      f"{'ccz4rhs' if system == 'ccz4' else 'bssnrhs'}"}, vals
 
 
 def main():
@@ -168,7 +184,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="uneven20k",
-                    choices=["uneven20k", "uniform512", "octree_rk4", "drift"])
+                    choices=["uneven20k", "uniform512", "octree_rk4", "drift", "ccz4_uneven20k"])
     ap.add_argument("--fine-radius", type=float, default=1.0,
                     help="octree_rk4: radius of the finest level around each puncture")
     ap.add_argument("--drift-steps", type=int, default=100,
@@ -190,6 +206,8 @@ def main():
         if args.impl == "reference" or rank != 0:
             return
         return main_drift(args, dgb)
+    if args.workload == "ccz4_uneven20k":
+        return main_ccz4(args, dgb, rank, world, local)
     blocks, seed, sigma = workload(dgb, args.workload)
     npts = interior_points(blocks)
     units = npts * 24
@@ -313,6 +331,109 @@ def main():
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def main_ccz4(args, dgb, rank, world, local):
+    """CCZ4 right-hand side (25 variables, kappa = (0.1, 0), KO sigma 0.4) over
+    the uneven 20,000-block batch, one persistent launch per step."""
+    blocks = dgb.synth_blocks(2, SEED2)
+    seed, sigma = 20261203 + 5, 0.4
+    npts = interior_points(blocks)
+    units = npts * 25
+    wl = {"workload": f"ccz4_uneven20k: CCZ4 on {len(blocks)} padded blocks "
+                      "(14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)",
+          "interior_points": npts, "vars": 25, "fd_order": 4, "ko_sigma": sigma,
+          "kappa": [0.1, 0.0], "p_expo": -1,
+          "step": "one ccz4rhs (+KO, theta_z4 not dissipated) over all blocks, one persistent launch",
+          "l2": "inputs (39.3 GB of fields) larger than L2", "precision": args.precision}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        base, vals = run_cpu_baseline(dgb, blocks, seed, sigma, steps=args.steps + args.warmup,
+                                      system="ccz4")
+        v = float(np.median(vals[args.warmup:])) if len(vals) > args.warmup else base["value"]
+        print(json.dumps({"metric": METRIC, "value": v, "unit": "grid-pts*vars/s", "n_gpus": 1,
+                          "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": units / v * 1e3, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": wl, "impl": "reference",
+                          "cpu_baseline": dict(base, value=v),
+                          "e2e": {"value": v, "unit": "grid-pts*vars/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dgb.init(local)
+    prec = dgb.PREC_MIXED if args.precision == "mixed" else dgb.PREC_FP64
+    prm = dgb.default_ccz4_params(ko_sigma=sigma)
+    plan = dgb.Plan(blocks, dgb.default_params(0.1))
+    n = plan.unzipped
+    du = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(25)]
+    dr = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(25)]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    plan.synth_fill_device([t.data_ptr() for t in du], seed, 1e-6, sh)
+    up = [t.data_ptr() for t in du]
+    rp = [t.data_ptr() for t in dr]
+    for _ in range(args.warmup):
+        plan.ccz4_rhs(prm, rp, up, prec, sh)
+    torch.cuda.synchronize(dev)
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.ccz4_rhs(prm, rp, up, prec, sh)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    value = units * world / (ms * 1e-3)
+    fp64_gflops, _ = dgb.measure_fp64_peak()
+    achieved = npts * FLOP_PER_POINT_CCZ4 / (ms * 1e-3) / 1e9
+    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
+            "frac": achieved / fp64_gflops, "traffic": None,
+            "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
+            "flop_per_point": FLOP_PER_POINT_CCZ4,
+            "hbm_gbs_algorithmic": 25 * 8 * (n + npts) / (ms * 1e-3) / 1e9}
+    e2e = None
+    if not args.no_e2e:
+        hu = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(25)]
+        hr = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(25)]
+        for v in range(25):
+            hu[v].copy_(du[v])
+        k = max(1, min(args.steps, 3))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(k):
+            for v in range(25):
+                du[v].copy_(hu[v], non_blocking=True)
+            plan.ccz4_rhs(prm, rp, up, prec, sh)
+            for v in range(25):
+                hr[v].copy_(dr[v], non_blocking=True)
+            torch.cuda.synchronize(dev)
+        e2e_s = (time.perf_counter() - t0) / k
+        e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
+               "h2d_bytes_per_step": 25 * n * 8, "d2h_bytes_per_step": 25 * n * 8,
+               "ms_per_step": e2e_s * 1e3,
+               "path": "pinned host arrays: H2D of the fields, dgb_ccz4_rhs, D2H of the rhs"}
+        del hu, hr
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu, _ = run_cpu_baseline(dgb, blocks, seed, sigma, system="ccz4")
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": "grid-pts*vars/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None,
+                          "dtype": "f64" if prec == dgb.PREC_FP64 else "f64 (FP32 stencils/KO)",
+                          "data": "synthetic (seeded Brill-Lindquist + 1e-6 noise, theta_z4 = noise)",
+                          "config": wl, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                          "clocks": clocks, "gpu_launches": args.steps, "impl": "ours"}))
+    plan.close()
 
 
 def octree_params(dgb, fine_radius):
