@@ -19,12 +19,19 @@
 //            theta_z4, CCZ4_GR/src/rhs.cpp:241-283).
 // The first derivatives of At0-5 and B0-2 feed only the boundary condition
 // and are formed on domain-boundary blocks only.
+//
+// Mixed precision (MIXED = true, interior blocks): every stencil runs in
+// FP32 on the split doubles (fp32split.cuh), compensated on the hi part and
+// plain on the lo part, and is widened, added and scaled in FP64; the
+// algebra, the KO sum across directions, the boundary condition and all
+// field I/O stay FP64.  Domain-boundary blocks take the FP64 stencils.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "ccz4_algebra.cuh"
 #include "dgb_internal.h"
 #include "exact_mul.cuh"
+#include "fp32split.cuh"
 #include "stencil42.cuh"
 
 namespace dgb {
@@ -50,6 +57,60 @@ __device__ __forceinline__ void c4_commit() { asm volatile("cp.async.commit_grou
 template <int N>
 __device__ __forceinline__ void c4_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
+// ---- 4th-order numerators on float lines (hi: compensated, lo: plain)
+__device__ __forceinline__ FP2 neg2(FP2 x)
+{
+    x.s = -x.s;
+    x.e = -x.e;
+    return x;
+}
+// first derivative: 8 (u1 - u-1) - (u2 - u-2)
+__device__ __forceinline__ FP2 n1_4c(const float *u, int s)
+{
+    return add2(mulc2(8.0f, two_sum(u[s], -u[-s])), neg2(two_sum(u[2 * s], -u[-2 * s])));
+}
+__device__ __forceinline__ float n1_4(const float *u, int s)
+{
+    return fmaf(8.0f, u[s] - u[-s], -(u[2 * s] - u[-2 * s]));
+}
+// second derivative: 16 s1 - s2, s_k = (u_k - u0) + (u_-k - u0)
+__device__ __forceinline__ FP2 n2_4c(const float *u, int s)
+{
+    const float c = u[0];
+    return add2(mulc2(16.0f, sym2(u, s, c)), neg2(sym2(u, 2 * s, c)));
+}
+__device__ __forceinline__ float n2_4(const float *u, int s)
+{
+    const float c = u[0];
+    return fmaf(16.0f, (u[s] - c) + (u[-s] - c), -((u[2 * s] - c) + (u[-2 * s] - c)));
+}
+// upwind, beta > 0: -3 d_-1 + 18 d_1 - 6 d_2 + d_3 with d_k = u_k - u0
+__device__ __forceinline__ FP2 nadvp_c(const float *u, int s)
+{
+    const float c = u[0];
+    FP2 t = add2(mulc2(-3.0f, two_sum(u[-s], -c)), mulc2(18.0f, two_sum(u[s], -c)));
+    t = add2(t, mulc2(-6.0f, two_sum(u[2 * s], -c)));
+    return add2(t, two_sum(u[3 * s], -c));
+}
+__device__ __forceinline__ float nadvp(const float *u, int s)
+{
+    const float c = u[0];
+    return fmaf(-3.0f, u[-s] - c, fmaf(18.0f, u[s] - c, fmaf(-6.0f, u[2 * s] - c, u[3 * s] - c)));
+}
+// upwind, beta <= 0: -d_-3 + 6 d_-2 - 18 d_-1 + 3 d_1
+__device__ __forceinline__ FP2 nadvn_c(const float *u, int s)
+{
+    const float c = u[0];
+    FP2 t = add2(neg2(two_sum(u[-3 * s], -c)), mulc2(6.0f, two_sum(u[-2 * s], -c)));
+    t = add2(t, mulc2(-18.0f, two_sum(u[-s], -c)));
+    return add2(t, mulc2(3.0f, two_sum(u[s], -c)));
+}
+__device__ __forceinline__ float nadvn(const float *u, int s)
+{
+    const float c = u[0];
+    return fmaf(6.0f, u[-2 * s] - c, fmaf(-18.0f, u[-s] - c, fmaf(3.0f, u[s] - c, -(u[-3 * s] - c))));
+}
+
 template <int TX, int TY, int TZ>
 struct C4Geo {
     static constexpr int PX = TX + 6, PY = TY + 6, PZ = TZ + 6;
@@ -58,6 +119,8 @@ struct C4Geo {
     static constexpr int DYB = TX * TY * (TZ + 4);
     static constexpr int PMAX = TX * TY * TZ;
     static constexpr size_t bytes = (size_t)(2 * FBUF + DXB + DYB + 3 * PMAX) * 8;
+    // + hi/lo planes of the staged field and the s + e pair boxes (floats)
+    static constexpr size_t bytes_mixed = bytes + (size_t)(2 * FBUF + 2 * DXB + 2 * DYB) * 4;
 };
 
 struct C4AlgPrm {
@@ -93,7 +156,7 @@ struct C4IO {
     }
 };
 
-template <int TX, int TY, int TZ>
+template <int TX, int TY, int TZ, bool MIXED>
 __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, const DevBlock &blk,
                                         double *S)
 {
@@ -104,6 +167,12 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
     double *dxb = fb1 + G::FBUF;
     double *dyb = dxb + G::DXB;
     double *bet = dyb + G::DYB;  // beta0..2 at the tile points
+    float *fhi = reinterpret_cast<float *>(bet + 3 * G::PMAX);  // MIXED only
+    float *flo = fhi + G::FBUF;
+    float *dxs = flo + G::FBUF;
+    float *dxe = dxs + G::DXB;
+    float *dys = dxe + G::DXB;
+    float *dye = dys + G::DYB;
     const int tid = threadIdx.x;
     const int nx = blk.sz[0], ny = blk.sz[1], nz = blk.sz[2];
     const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
@@ -153,7 +222,110 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
         double *Sko = S + (size_t)(DGB_CCZ4_NUM_DERIV + v) * G::PMAX;
         // At0-5, B0-2: first derivatives only for the boundary condition
         const bool want_grad = bflag != 0 || !((v >= 9 && v <= 11) || (v >= 18 && v <= 23));
-        if (q2 < 0) {
+        if (MIXED && bflag == 0) {
+            for (int q = tid; q < npad; q += kC4Threads) {
+                const F2 f2 = split_double(F[q]);
+                fhi[q] = f2.hi;
+                flo[q] = f2.lo;
+            }
+            __syncthreads();
+            auto N1 = [&](const float *h, const float *l, int s) {
+                FP2 r = n1_4c(h, s);
+                r.e = __fadd_rn(r.e, n1_4(l, s));
+                return r;
+            };
+            auto to64 = [](FP2 r, double scale) { return __dmul_rn(fp2_widen(r), scale); };
+            // one point: advective and (theta excluded) KO in FP32, scaled in FP64
+            auto adv_ko = [&](int p, int off, const int *pos) {
+                const int st[3] = {1, sy, sz};
+                double ko = 0.0;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const bool up = bet[d * G::PMAX + p] > 0.0;
+                    FP2 a = up ? nadvp_c(fhi + off, st[d]) : nadvn_c(fhi + off, st[d]);
+                    a.e = __fadd_rn(a.e, up ? nadvp(flo + off, st[d]) : nadvn(flo + off, st[d]));
+                    Sa[d * G::PMAX + p] = to64(a, ax[d].c12);
+                    if (v != kC4Theta) {
+                        // the first / last interior point takes its neighbour's stencil
+                        const int sh = pos[d] == 3 ? st[d] : (pos[d] == nn[d] - 4 ? -st[d] : 0);
+                        FP2 k = nko_c(fhi + off + sh, st[d]);
+                        k.e = __fadd_rn(k.e, nko_32(flo + off + sh, st[d]));
+                        const double kd = to64(k, ax[d].pre);
+                        ko = d == 0 ? kd : __dadd_rn(ko, kd);
+                    }
+                }
+                if (v != kC4Theta) Sko[p] = ko;
+            };
+            if (q2 < 0) {
+                for (int p = tid; p < P; p += kC4Threads) {
+                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
+                    const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                    if (want_grad) {
+                        Sg[p] = to64(N1(fhi + off, flo + off, 1), ax[0].c12);
+                        Sg[G::PMAX + p] = to64(N1(fhi + off, flo + off, sy), ax[1].c12);
+                        Sg[2 * G::PMAX + p] = to64(N1(fhi + off, flo + off, sz), ax[2].c12);
+                    }
+                    adv_ko(p, off, pos);
+                }
+            } else {
+                double *S2 = S + (size_t)(DGB_CCZ4_D20 + 6 * q2) * G::PMAX;
+                const int by = ey + 4;
+                const int nA = ex * by * ez, nB = ex * ey * 4;
+                for (int q = tid; q < nA + nB; q += kC4Threads) {
+                    int ti, tj, tk;
+                    if (q < nA) {
+                        ti = q % ex; const int r = q / ex; tj = r % by; tk = r / by + 2;
+                    } else {
+                        const int q3 = q - nA;
+                        ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 2;
+                        const int kk = r / ey;
+                        tk = kk < 2 ? kk : ez + kk;
+                    }
+                    const int off = (ti + 3) + sy * (tj + 1) + sz * (tk + 1);
+                    const FP2 h = N1(fhi + off, flo + off, 1);
+                    const int b = ti + ex * (tj + by * tk);
+                    dxs[b] = h.s;
+                    dxe[b] = h.e;
+                }
+                const int nC = ex * ey * (ez + 4);
+                for (int q = tid; q < nC; q += kC4Threads) {
+                    const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
+                    const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 1);
+                    const FP2 h = N1(fhi + off, flo + off, sy);
+                    dys[q] = h.s;
+                    dye[q] = h.e;
+                }
+                for (int p = tid; p < P; p += kC4Threads) {
+                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
+                    const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                    Sg[2 * G::PMAX + p] = to64(N1(fhi + off, flo + off, sz), ax[2].c12);
+                    const int st[3] = {1, sy, sz};
+                    const int slot[3] = {0, 3, 5};
+#pragma unroll
+                    for (int d = 0; d < 3; d++) {
+                        FP2 h = n2_4c(fhi + off, st[d]);
+                        h.e = __fadd_rn(h.e, n2_4(flo + off, st[d]));
+                        S2[slot[d] * G::PMAX + p] = to64(h, ax[d].c12sq);
+                    }
+                    adv_ko(p, off, pos);
+                }
+                __syncthreads();
+                const double cxy = ax[0].c12 * ax[1].c12, cxz = ax[0].c12 * ax[2].c12,
+                             cyz = ax[1].c12 * ax[2].c12;
+                for (int p = tid; p < P; p += kC4Threads) {
+                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    const int bxi = ti + ex * ((tj + 2) + by * (tk + 2));
+                    const int byi = ti + ex * (tj + ey * (tk + 2));
+                    Sg[p] = __dmul_rn(__dadd_rn(widen(dxs[bxi]), widen(dxe[bxi])), ax[0].c12);
+                    Sg[G::PMAX + p] = __dmul_rn(__dadd_rn(widen(dys[byi]), widen(dye[byi])), ax[1].c12);
+                    S2[1 * G::PMAX + p] = to64(N1(dxs + bxi, dxe + bxi, ex), cxy);
+                    S2[2 * G::PMAX + p] = to64(N1(dxs + bxi, dxe + bxi, ex * by), cxz);
+                    S2[4 * G::PMAX + p] = to64(N1(dys + byi, dye + byi, ex * ey), cyz);
+                }
+            }
+        } else if (q2 < 0) {
             for (int p = tid; p < P; p += kC4Threads) {
                 const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
                 const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
@@ -260,7 +432,7 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
     }
 }
 
-template <int TX, int TY, int TZ>
+template <int TX, int TY, int TZ, bool MIXED>
 __global__ void __launch_bounds__(kC4Threads, 1) c4_kernel(const C4Args args)
 {
     using G = C4Geo<TX, TY, TZ>;
@@ -274,34 +446,46 @@ __global__ void __launch_bounds__(kC4Threads, 1) c4_kernel(const C4Args args)
         if (it >= (int)args.nitems) break;
         const WorkItem w = args.items[it];
         const DevBlock blk = args.blocks[w.blk];
-        c4_item<TX, TY, TZ>(args, w, blk, S);
+        c4_item<TX, TY, TZ, MIXED>(args, w, blk, S);
     }
 }
 
 }  // namespace
 
-size_t c4_smem_bytes() { return C4Geo<8, 8, 8>::bytes; }
+size_t c4_smem_bytes(int precision)
+{
+    return precision == DGB_PREC_MIXED ? C4Geo<8, 8, 8>::bytes_mixed : C4Geo<8, 8, 8>::bytes;
+}
 size_t c4_scratch_per_cta() { return (size_t)DGB_CCZ4_NUM_SLOTS * C4Geo<8, 8, 8>::PMAX; }
 
-cudaError_t c4_configure()
+cudaError_t c4_configure(int precision)
 {
-    return cudaFuncSetAttribute(c4_kernel<8, 8, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (precision == DGB_PREC_MIXED)
+        return cudaFuncSetAttribute(c4_kernel<8, 8, 8, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)C4Geo<8, 8, 8>::bytes_mixed);
+    return cudaFuncSetAttribute(c4_kernel<8, 8, 8, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)C4Geo<8, 8, 8>::bytes);
 }
 
-int c4_max_ctas_per_sm()
+int c4_max_ctas_per_sm(int precision)
 {
     int n = 0;
-    if (c4_configure() != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, c4_kernel<8, 8, 8>, kC4Threads,
-                                                      C4Geo<8, 8, 8>::bytes) != cudaSuccess)
-        return 0;
-    return n;
+    if (c4_configure(precision) != cudaSuccess) return 0;
+    cudaError_t e = precision == DGB_PREC_MIXED
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, c4_kernel<8, 8, 8, true>, kC4Threads,
+                                                        C4Geo<8, 8, 8>::bytes_mixed)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, c4_kernel<8, 8, 8, false>, kC4Threads,
+                                                        C4Geo<8, 8, 8>::bytes);
+    return e == cudaSuccess ? n : 0;
 }
 
-cudaError_t c4_launch(const C4Args &args, int grid, cudaStream_t stream)
+cudaError_t c4_launch(int precision, const C4Args &args, int grid, cudaStream_t stream)
 {
-    c4_kernel<8, 8, 8><<<grid, kC4Threads, C4Geo<8, 8, 8>::bytes, stream>>>(args);
+    if (precision == DGB_PREC_MIXED)
+        c4_kernel<8, 8, 8, true><<<grid, kC4Threads, C4Geo<8, 8, 8>::bytes_mixed, stream>>>(args);
+    else
+        c4_kernel<8, 8, 8, false><<<grid, kC4Threads, C4Geo<8, 8, 8>::bytes, stream>>>(args);
     return cudaGetLastError();
 }
 

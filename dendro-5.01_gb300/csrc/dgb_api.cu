@@ -53,7 +53,7 @@ struct dgb_plan {
     int occupancy[8][2] = {};  // resident CTAs per SM per (variant, precision)
     int pc_occupancy = 0;      // constraint kernel, resident CTAs per SM (0 = not yet known)
     // CCZ4 kernel: its own workspace (241 slots per point), allocated at first use
-    int c4_occupancy = 0;
+    int c4_occupancy[2] = {0, 0};  // per precision
     double *d_scratch4 = nullptr;
     size_t scratch4_doubles = 0;
     // device copies for the host-array entry point
@@ -370,25 +370,31 @@ dgb_status dgb_ccz4_rhs(dgb_plan *p, const dgb_ccz4_params *prm, double *const *
             set_error("dgb_ccz4_rhs: null field pointer");
             return DGB_ERR_INVALID;
         }
-    if (precision != DGB_PREC_FP64) {
-        set_error("dgb_ccz4_rhs: only DGB_PREC_FP64 is built for CCZ4");
-        return DGB_ERR_UNSUPPORTED;
+    if (precision != DGB_PREC_FP64 && precision != DGB_PREC_MIXED) {
+        set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
+        return DGB_ERR_INVALID;
     }
+    const int pq = precision == DGB_PREC_MIXED ? 1 : 0;
     dgb_status s = build_items(p, 0);  // the 8x8x8 schedule
     if (s != DGB_OK) return s;
     if (p->nitems[0] == 0) return DGB_OK;
-    if (p->c4_occupancy == 0) {
-        const int occ = c4_max_ctas_per_sm();
+    if (p->c4_occupancy[pq] == 0) {
+        const int occ = c4_max_ctas_per_sm(precision);
         if (occ < 1) {
             set_error("dgb_ccz4_rhs: kernel cannot be resident");
             return DGB_ERR_CUDA;
         }
         const size_t need = c4_scratch_per_cta() * (size_t)occ * (size_t)p->nsm;
-        DGB_CUDA(cudaMalloc(&p->d_scratch4, need * sizeof(double)));
-        p->scratch4_doubles = need;
-        p->c4_occupancy = occ;
+        if (need > p->scratch4_doubles) {
+            cudaFree(p->d_scratch4);
+            p->d_scratch4 = nullptr;
+            p->scratch4_doubles = 0;
+            DGB_CUDA(cudaMalloc(&p->d_scratch4, need * sizeof(double)));
+            p->scratch4_doubles = need;
+        }
+        p->c4_occupancy[pq] = occ;
     }
-    DGB_CUDA(c4_configure());
+    DGB_CUDA(c4_configure(precision));
     C4Args a;
     for (int v = 0; v < NV4; v++) {
         a.u[v] = u[v];
@@ -405,7 +411,7 @@ dgb_status dgb_ccz4_rhs(dgb_plan *p, const dgb_ccz4_params *prm, double *const *
                      prm->ko_sigma};
     cudaStream_t st = (cudaStream_t)stream;
     DGB_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned int), st));
-    DGB_CUDA(c4_launch(a, p->nsm * p->c4_occupancy, st));
+    DGB_CUDA(c4_launch(precision, a, p->nsm * p->c4_occupancy[pq], st));
     return DGB_OK;
 }
 

@@ -90,11 +90,11 @@ struct C4Args {
     double *scratch;
     C4Params prm;
 };
-size_t c4_smem_bytes();
+size_t c4_smem_bytes(int precision);
 size_t c4_scratch_per_cta();  // doubles
-cudaError_t c4_configure();
-int c4_max_ctas_per_sm();
-cudaError_t c4_launch(const C4Args &args, int grid, cudaStream_t stream);
+cudaError_t c4_configure(int precision);
+int c4_max_ctas_per_sm(int precision);
+cudaError_t c4_launch(int precision, const C4Args &args, int grid, cudaStream_t stream);
 
 // Constraint diagnostics (physcon.cu).
 struct PcArgs {

@@ -160,8 +160,9 @@ typedef struct {
  * theta_z4, CCZ4_GR/include/grUtils.h:46); interior points are written,
  * padding untouched.  The CCZ4 solver's 4th-order stencils (upwind advective
  * derivatives, its KO form), ccz4_bcs on flagged faces, KO on every variable
- * but theta_z4.  FP64 (DGB_PREC_MIXED returns DGB_ERR_UNSUPPORTED).  The
- * plan's block list is used; its BSSN parameters are not.  Asynchronous on
+ * but theta_z4.  DGB_PREC_MIXED: FP32 (compensated) stencils on interior
+ * blocks, FP64 everywhere else.  The plan's block list is used; its BSSN
+ * parameters are not.  Asynchronous on
  * `stream`; calls on one plan must be ordered on one stream. */
 dgb_status dgb_ccz4_rhs(dgb_plan *plan, const dgb_ccz4_params *prm, double *const *rhs,
                         const double *const *u, int precision, void *stream);

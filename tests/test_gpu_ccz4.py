@@ -125,7 +125,7 @@ def test_ccz4_boundary_blocks(dgb, gpu, oracle):
     assert np.all(err <= FP64_TOL), dict(zip(dgb.CCZ4_VAR_NAMES, err))
 
 
-def test_ccz4_theta_not_dissipated_and_fp64_only(dgb, gpu):
+def test_ccz4_theta_not_dissipated(dgb, gpu):
     torch = gpu
     blocks = repack(dgb, dgb.synth_blocks(1), [100, 101])
     u = ccz4_fields(dgb, blocks, 5)
@@ -133,9 +133,42 @@ def test_ccz4_theta_not_dissipated_and_fp64_only(dgb, gpu):
     r1 = gpu_ccz4(dgb, torch, blocks, u, dgb.default_ccz4_params(ko_sigma=0.4))
     assert np.array_equal(r0[24], r1[24])
     assert not np.array_equal(r0[0], r1[0])
+
+
+MIXED_TOL = 1e-7  # per-field normwise, compensated FP32 stencils vs FP64
+
+
+@pytest.mark.parametrize("which", ["uniform512", "uneven_sample", "boundary"])
+def test_ccz4_mixed_precision(dgb, gpu, oracle, which):
+    """FP32 stencils on interior blocks within MIXED_TOL of the FP64 oracle;
+    domain-boundary blocks take the FP64 path (1e-12)."""
+    from test_oracle import boundary_blocks
+    torch = gpu
+    if which == "uniform512":
+        blocks, seed = dgb.synth_blocks(1), SEED1
+    elif which == "uneven_sample":
+        allb = dgb.synth_blocks(2, SEED2)
+        blocks, seed = repack(dgb, allb, sample_uneven(allb)), SEED2
+    else:
+        blocks, seed = boundary_blocks(dgb), SEED1
+    u = ccz4_fields(dgb, blocks, seed)
+    prm = dgb.default_ccz4_params()
     plan = dgb.Plan(blocks, dgb.default_params(0.1))
     du = [torch.from_numpy(a).cuda() for a in u]
-    with pytest.raises(dgb.DgbError):
-        plan.ccz4_rhs(dgb.default_ccz4_params(), [t.data_ptr() for t in du],
-                      [t.data_ptr() for t in du], dgb.PREC_MIXED)
+    n = len(u[0])
+    dr = [torch.full((n,), 7.0, dtype=torch.float64, device="cuda") for _ in range(25)]
+    plan.ccz4_rhs(prm, [t.data_ptr() for t in dr], [t.data_ptr() for t in du], dgb.PREC_MIXED)
+    torch.cuda.synchronize()
+    got = [t.cpu().numpy() for t in dr]
     plan.close()
+    want = oracle_ccz4(dgb, oracle, blocks, u, prm)
+    mask = interior_mask(blocks, n)
+    err = normwise(got, want, mask)
+    assert np.all(err <= MIXED_TOL), dict(zip(dgb.CCZ4_VAR_NAMES, err))
+    for v in range(25):
+        assert np.all(got[v][~mask] == 7.0)
+    flagged = [b for b in blocks if b.bflag != 0]
+    if flagged:
+        fmask = interior_mask(flagged, n)
+        err = normwise(got, want, fmask)
+        assert np.all(err <= FP64_TOL), dict(zip(dgb.CCZ4_VAR_NAMES, err))
