@@ -49,8 +49,12 @@ def build(verbose=False):
                   if f.endswith((".cu", ".cpp")))
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(HERE, "..", "include", "dendro_gb300.h"))
+    # a change of compiler flags rebuilds everything
+    stamp = os.path.join(OUT, "flags.txt")
+    flags = " ".join(NVCC_FLAGS + CXX_FLAGS)
+    same_flags = os.path.exists(stamp) and open(stamp).read() == flags
     todo = [s for s in srcs
-            if newer(os.path.join(OUT, os.path.basename(s) + ".o"), [s] + headers)]
+            if not same_flags or newer(os.path.join(OUT, os.path.basename(s) + ".o"), [s] + headers)]
     logs = {}
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(todo), os.cpu_count() or 4))) as ex:
         for src, obj, rc, log in ex.map(compile_one, todo):
@@ -59,6 +63,8 @@ def build(verbose=False):
                 sys.stderr.write(log)
             if rc != 0:
                 raise RuntimeError(f"compile failed: {src}")
+    with open(stamp, "w") as f:
+        f.write(flags)
     objs = [os.path.join(OUT, os.path.basename(s) + ".o") for s in srcs]
     if todo or not os.path.exists(LIB):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lgomp"]

@@ -38,6 +38,11 @@ namespace dgb {
 namespace {
 
 constexpr int kC4Threads = 256;
+#ifndef DGB_C4_MIN_CTAS
+#define DGB_C4_MIN_CTAS 2
+#endif
+// CTAs per SM the register budget is sized for (255 registers at 1, 128 at 2)
+constexpr int kC4MinBlocks = DGB_C4_MIN_CTAS;
 constexpr int kC4Theta = 24;
 // VAR -> second-derivative group (alpha, psi, beta0-2, gt0-5) or -1
 __constant__ int8_t c_c4d2[NV4] = {0, 1, -1, -1, -1, -1, 2, 3, 4, -1, -1, -1,
@@ -433,7 +438,7 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
 }
 
 template <int TX, int TY, int TZ, bool MIXED>
-__global__ void __launch_bounds__(kC4Threads, 1) c4_kernel(const C4Args args)
+__global__ void __launch_bounds__(kC4Threads, kC4MinBlocks) c4_kernel(const C4Args args)
 {
     using G = C4Geo<TX, TY, TZ>;
     __shared__ int s_item;

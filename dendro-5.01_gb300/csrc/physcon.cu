@@ -30,6 +30,11 @@ namespace dgb {
 namespace {
 
 constexpr int kPcThreads = 256;
+#ifndef DGB_PC_MIN_CTAS
+#define DGB_PC_MIN_CTAS 2
+#endif
+// CTAs per SM the register budget is sized for (255 registers at 1, 128 at 2)
+constexpr int kPcMinBlocks = DGB_PC_MIN_CTAS;
 constexpr int kNumCFields = 17;
 constexpr int kGradSlots = 3 * kNumCFields;            // 51
 constexpr int kPcSlots = kGradSlots + 7 * 6;           // + chi, gt0-5 second derivatives
@@ -437,7 +442,7 @@ __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem 
 }
 
 template <int TX, int TY, int TZ>
-__global__ void __launch_bounds__(kPcThreads, 1) physcon_kernel(const PcArgs args)
+__global__ void __launch_bounds__(kPcThreads, kPcMinBlocks) physcon_kernel(const PcArgs args)
 {
     using G = PcGeo<TX, TY, TZ>;
     __shared__ int s_item;
