@@ -40,6 +40,9 @@ FLOP_PER_POINT = 8223.0
 # 75 upwind + 75 KO stencils, "reduced ops 4633" algebra, KO accumulate):
 # 75*8 + 36*16 + 36*10 + 75*10 + 75*14 + 4633 + 24*4 = 8,065.
 FLOP_PER_POINT_CCZ4 = 8065.0
+# constraint diagnostics (4th order: 51 first, 21 second, 21 mixed stencils,
+# "reduced ops 4599" algebra): 51*8 + 21*10 + 21*16 + 4599 = 5,553.
+FLOP_PER_POINT_PHYSCON = 5553.0
 SEED2 = 20261203 + 2
 SEED1 = 20261203 + 1
 
@@ -184,7 +187,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="uneven20k",
-                    choices=["uneven20k", "uniform512", "octree_rk4", "drift", "ccz4_uneven20k"])
+                    choices=["uneven20k", "uniform512", "octree_rk4", "drift", "ccz4_uneven20k",
+                             "constraints_uneven20k"])
     ap.add_argument("--fine-radius", type=float, default=1.0,
                     help="octree_rk4: radius of the finest level around each puncture")
     ap.add_argument("--drift-steps", type=int, default=100,
@@ -208,6 +212,8 @@ def main():
         return main_drift(args, dgb)
     if args.workload == "ccz4_uneven20k":
         return main_ccz4(args, dgb, rank, world, local)
+    if args.workload == "constraints_uneven20k":
+        return main_constraints(args, dgb, rank, world, local)
     blocks, seed, sigma = workload(dgb, args.workload)
     npts = interior_points(blocks)
     units = npts * 24
@@ -432,6 +438,110 @@ def main_ccz4(args, dgb, rank, world, local):
                           "dtype": "f64" if prec == dgb.PREC_FP64 else "f64 (FP32 stencils/KO)",
                           "data": "synthetic (seeded Brill-Lindquist + 1e-6 noise, theta_z4 = noise)",
                           "config": wl, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                          "clocks": clocks, "gpu_launches": args.steps, "impl": "ours"}))
+    plan.close()
+
+
+def cpu_constraints_baseline(dgb, blocks, seed, target_s=12.0, steps=1):
+    """Oracle port of physical_constraints on all host cores, stratified sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from workloads import repack
+    ora = oracle_py.Oracle()
+    cores = os.cpu_count() or 1
+    frac = 1.0 / 400
+    for attempt in range(3):
+        sub = repack(dgb, blocks, cpu_sample(blocks, frac))
+        u = [np.zeros(dgb.unzipped_size(sub)) for _ in range(24)]
+        dgb.synth_fill_host(sub, u, seed, 1e-6)
+        c = [np.zeros_like(u[0]) for _ in range(6)]
+        t0 = time.perf_counter()
+        assert ora.physcon_blocks(c, u, sub, cores) == 0
+        dt = time.perf_counter() - t0
+        if dt > 0.25 * target_s or frac >= 1.0:
+            break
+        frac = min(1.0, frac * max(2.0, min(50.0, target_s / max(dt, 1e-3))))
+    pts = interior_points(sub)
+    vals = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        assert ora.physcon_blocks(c, u, sub, cores) == 0
+        vals.append(pts / (time.perf_counter() - t0))
+    return {"value": float(np.median(vals)), "unit": "grid-pts/s", "cores": cores, "kind": "port",
+            "sample": f"{len(sub)} of {len(blocks)} blocks (stratified by size, {pts} interior "
+                      f"points), FP64, OpenMP over blocks, physical_constraints"}, vals
+
+
+def main_constraints(args, dgb, rank, world, local):
+    """Constraint diagnostics (Hamiltonian, momentum, Psi4; physical_constraints)
+    over the uneven 20,000-block batch; units = interior points per second."""
+    blocks, seed, _ = workload(dgb, "uneven20k")
+    npts = interior_points(blocks)
+    wl = {"workload": f"constraints_uneven20k: physical_constraints on {len(blocks)} padded "
+                      "blocks (14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)",
+          "interior_points": npts, "outputs": 6, "fd_order": 4,
+          "step": "one physical_constraints over all blocks, one persistent launch",
+          "l2": "inputs (37.8 GB of fields) larger than L2"}
+    metric = "constraint diagnostics grid-pts/s on 1 GB300 (FP64)"
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        base, vals = cpu_constraints_baseline(dgb, blocks, seed, steps=args.steps + args.warmup)
+        v = float(np.median(vals[args.warmup:])) if len(vals) > args.warmup else base["value"]
+        print(json.dumps({"metric": metric, "value": v, "unit": "grid-pts/s", "n_gpus": 1,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": npts / v * 1e3,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64", "data": "synthetic", "config": wl, "impl": "reference",
+                          "cpu_baseline": dict(base, value=v),
+                          "e2e": {"value": v, "unit": "grid-pts/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dgb.init(local)
+    plan = dgb.Plan(blocks, dgb.default_params(0.1))
+    n = plan.unzipped
+    du = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(24)]
+    dc = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(6)]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    plan.synth_fill_device([t.data_ptr() for t in du], seed, 1e-6, sh)
+    up, cp = [t.data_ptr() for t in du], [t.data_ptr() for t in dc]
+    for _ in range(args.warmup):
+        plan.physical_constraints(cp, up, sh)
+    torch.cuda.synchronize(dev)
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.physical_constraints(cp, up, sh)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    value = npts * world / (ms * 1e-3)
+    fp64_gflops, _ = dgb.measure_fp64_peak()
+    achieved = npts * FLOP_PER_POINT_PHYSCON / (ms * 1e-3) / 1e9
+    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
+            "frac": achieved / fp64_gflops, "traffic": None,
+            "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
+            "flop_per_point": FLOP_PER_POINT_PHYSCON,
+            "hbm_gbs_algorithmic": (17 * n + 6 * npts) * 8 / (ms * 1e-3) / 1e9}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu, _ = cpu_constraints_baseline(dgb, blocks, seed)
+    if rank == 0:
+        print(json.dumps({"metric": metric, "value": value, "unit": "grid-pts/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic (seeded Brill-Lindquist + 1e-6 noise)",
+                          "config": wl, "roofline": roof, "cpu_baseline": cpu, "e2e": None,
                           "clocks": clocks, "gpu_launches": args.steps, "impl": "ours"}))
     plan.close()
 
