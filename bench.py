@@ -119,6 +119,30 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_max_ms(ms, world, device):
+    """Job time of a replica run: the max over ranks of the per-rank step time.
+    The one collective of the run; it carries timing only, never field data."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank, world, ms):
+    """Whole-job throughput: every rank processed units_per_rank in ms (max)."""
+    return units_per_rank * world / (ms * 1e-3)
+
+
+def init_replicas(world, local):
+    """One process per GPU; a process group only when there is more than one."""
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1 and not torch.distributed.is_initialized():
+        torch.distributed.init_process_group("nccl")
+
+
 def cpu_sample(blocks, fraction):
     """Stratified block sample: every k-th block of each size class."""
     by = {}
@@ -278,13 +302,10 @@ def main():
     e1.record(stream)
     torch.cuda.synchronize(dev)
     clocks = clk.stop()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = replica_max_ms(e0.elapsed_time(e1) / args.steps, world, dev)
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
         torch.distributed.barrier()
-    value = units * world / (ms * 1e-3)
+    value = replica_value(units, world, ms)
 
     fp64_gflops, _ = dgb.measure_fp64_peak()
     achieved = npts * FLOP_PER_POINT / (ms * 1e-3) / 1e9
@@ -368,8 +389,8 @@ def main_ccz4(args, dgb, rank, world, local):
                                   "d2h_bytes_per_step": 0}}))
         return
     import torch
+    init_replicas(world, local)
     dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
     dgb.init(local)
     prec = dgb.PREC_MIXED if args.precision == "mixed" else dgb.PREC_FP64
     prm = dgb.default_ccz4_params(ko_sigma=sigma)
@@ -385,6 +406,8 @@ def main_ccz4(args, dgb, rank, world, local):
     for _ in range(args.warmup):
         plan.ccz4_rhs(prm, rp, up, prec, sh)
     torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
     clk = ClockSampler(local)
     clk.start()
     time.sleep(0.3)
@@ -396,8 +419,8 @@ def main_ccz4(args, dgb, rank, world, local):
     e1.record(stream)
     torch.cuda.synchronize(dev)
     clocks = clk.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    value = units * world / (ms * 1e-3)
+    ms = replica_max_ms(e0.elapsed_time(e1) / args.steps, world, dev)
+    value = replica_value(units, world, ms)
     fp64_gflops, _ = dgb.measure_fp64_peak()
     achieved = npts * FLOP_PER_POINT_CCZ4 / (ms * 1e-3) / 1e9
     roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
@@ -440,6 +463,8 @@ def main_ccz4(args, dgb, rank, world, local):
                           "config": wl, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                           "clocks": clocks, "gpu_launches": args.steps, "impl": "ours"}))
     plan.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def cpu_constraints_baseline(dgb, blocks, seed, target_s=12.0, steps=1):
@@ -498,8 +523,8 @@ def main_constraints(args, dgb, rank, world, local):
                                   "d2h_bytes_per_step": 0}}))
         return
     import torch
+    init_replicas(world, local)
     dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
     dgb.init(local)
     plan = dgb.Plan(blocks, dgb.default_params(0.1))
     n = plan.unzipped
@@ -512,6 +537,8 @@ def main_constraints(args, dgb, rank, world, local):
     for _ in range(args.warmup):
         plan.physical_constraints(cp, up, sh)
     torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
     clk = ClockSampler(local)
     clk.start()
     time.sleep(0.3)
@@ -523,8 +550,8 @@ def main_constraints(args, dgb, rank, world, local):
     e1.record(stream)
     torch.cuda.synchronize(dev)
     clocks = clk.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    value = npts * world / (ms * 1e-3)
+    ms = replica_max_ms(e0.elapsed_time(e1) / args.steps, world, dev)
+    value = replica_value(npts, world, ms)
     fp64_gflops, _ = dgb.measure_fp64_peak()
     achieved = npts * FLOP_PER_POINT_PHYSCON / (ms * 1e-3) / 1e9
     roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
@@ -544,6 +571,8 @@ def main_constraints(args, dgb, rank, world, local):
                           "config": wl, "roofline": roof, "cpu_baseline": cpu, "e2e": None,
                           "clocks": clocks, "gpu_launches": args.steps, "impl": "ours"}))
     plan.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def octree_params(dgb, fine_radius):
@@ -655,12 +684,8 @@ def main_octree(args, dgb, rank, world, local):
     e1.record(stream)
     torch.cuda.synchronize(dev)
     clocks = clk.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = units * world / (ms * 1e-3)
+    ms = replica_max_ms(e0.elapsed_time(e1) / args.steps, world, dev)
+    value = replica_value(units, world, ms)
     fp64_gflops, _ = dgb.measure_fp64_peak()
     achieved = 4 * n_int * FLOP_PER_POINT / (ms * 1e-3) / 1e9
     roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
