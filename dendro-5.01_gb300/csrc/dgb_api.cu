@@ -2,6 +2,7 @@
 // and host arrays), the RK4 stage update and the synthetic fill.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -56,9 +57,57 @@ struct dgb_plan {
     int c4_occupancy[2] = {0, 0};  // per precision
     double *d_scratch4 = nullptr;
     size_t scratch4_doubles = 0;
-    // device copies for the host-array entry point
-    double *d_u = nullptr, *d_rhs = nullptr;
+    // host-array entry point: chunked pipeline, built at first use
+    struct HostPipe *pipe = nullptr;
+    bool borrowed_scratch = false;  // a chunk sub-plan using its parent's workspace
 };
+
+void destroy_pipe(struct HostPipe *h);
+
+namespace dgb {
+void host_gather(double *dst, size_t slot_pts, const double *const *u, int nv, uint64_t start,
+                 uint64_t span);
+void host_scatter_interior(double *const *rhs, const double *src, size_t slot_pts, int nv,
+                           const dgb_block_desc *blocks, const uint32_t *members, size_t nmem,
+                           uint64_t start);
+}  // namespace dgb
+
+// The host-array entry point as a pipeline over chunks of blocks (contiguous
+// in the caller's unzipped arrays): host threads copy chunk a's fields into
+// pinned staging while the GPU uploads chunk a-1... in order per chunk
+//   gather (host) -> H2D -> RHS -> D2H -> scatter of interior points (host)
+// with three device slots, two pinned staging buffers each way and separate
+// upload / compute / download streams, so transfers overlap the kernel.
+// Only interior points are written back, so the caller's rhs padding is
+// untouched without uploading rhs.
+struct HostPipe {
+    size_t slot_pts = 0;
+    std::vector<uint64_t> start, span;
+    std::vector<std::vector<uint32_t>> members;
+    std::vector<dgb_plan *> sub;
+    double *d_slots = nullptr;          // 3 u slots, then 3 rhs slots, NV * slot_pts each
+    double *h_in[2] = {nullptr, nullptr}, *h_out[2] = {nullptr, nullptr};  // pinned
+    cudaStream_t s_h2d = nullptr, s_comp = nullptr, s_d2h = nullptr;
+    std::vector<cudaEvent_t> ev_h2d, ev_comp, ev_d2h;
+};
+
+void destroy_pipe(HostPipe *h)
+{
+    if (!h) return;
+    for (dgb_plan *sp : h->sub) dgb_plan_destroy(sp);
+    cudaFree(h->d_slots);
+    for (int q = 0; q < 2; q++) {
+        cudaFreeHost(h->h_in[q]);
+        cudaFreeHost(h->h_out[q]);
+    }
+    for (auto e : h->ev_h2d) if (e) cudaEventDestroy(e);
+    for (auto e : h->ev_comp) if (e) cudaEventDestroy(e);
+    for (auto e : h->ev_d2h) if (e) cudaEventDestroy(e);
+    if (h->s_h2d) cudaStreamDestroy(h->s_h2d);
+    if (h->s_comp) cudaStreamDestroy(h->s_comp);
+    if (h->s_d2h) cudaStreamDestroy(h->s_d2h);
+    delete h;
+}
 
 namespace {
 
@@ -283,10 +332,9 @@ dgb_status dgb_plan_destroy(dgb_plan *p)
     cudaFree(p->d_first);
     for (auto d : p->d_items) cudaFree(d);
     cudaFree(p->d_queue);
-    cudaFree(p->d_scratch);
+    if (!p->borrowed_scratch) cudaFree(p->d_scratch);
     cudaFree(p->d_scratch4);
-    cudaFree(p->d_u);
-    cudaFree(p->d_rhs);
+    destroy_pipe(p->pipe);
     delete p;
     return DGB_OK;
 }
@@ -501,38 +549,179 @@ dgb_status dgb_plan_autotune(dgb_plan *p, double *const *rhs, const double *cons
     return DGB_OK;
 }
 
+namespace {
+
+// Padded points per chunk: ~1.2 GB of fields each way per chunk, small next to
+// the 20k-block batch (~40 chunks) and large next to any block.
+constexpr uint64_t kChunkPts = 6u << 20;
+
+dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
+{
+    uint64_t chunk_pts = kChunkPts;
+    if (const char *env = getenv("DGB_HOST_CHUNK_PTS")) {  // tests: force many chunks
+        const long long v = atoll(env);
+        if (v > 0) chunk_pts = (uint64_t)v;
+    }
+    std::vector<uint32_t> order(p->blocks.size());
+    for (size_t b = 0; b < order.size(); b++) order[b] = (uint32_t)b;
+    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        return p->blocks[a].offset < p->blocks[b].offset;
+    });
+    auto npts = [&](uint32_t b) {
+        const dgb_block_desc &d = p->blocks[b];
+        return (uint64_t)d.sz[0] * d.sz[1] * d.sz[2];
+    };
+    for (size_t q = 0; q < order.size();) {
+        const uint64_t s0 = p->blocks[order[q]].offset;
+        uint64_t end = s0 + npts(order[q]);
+        std::vector<uint32_t> mem{order[q]};
+        size_t r = q + 1;
+        while (r < order.size()) {
+            const uint64_t e2 = std::max(end, p->blocks[order[r]].offset + npts(order[r]));
+            if (e2 - s0 > chunk_pts) break;
+            end = e2;
+            mem.push_back(order[r]);
+            r++;
+        }
+        h->start.push_back(s0);
+        h->span.push_back(end - s0);
+        h->slot_pts = std::max<size_t>(h->slot_pts, end - s0);
+        h->members.push_back(std::move(mem));
+        q = r;
+    }
+    // one sub-plan per chunk, offsets relative to the chunk start, sharing
+    // the parent's derivative workspace (chunks run one after another)
+    for (size_t c = 0; c < h->members.size(); c++) {
+        std::vector<dgb_block_desc> d;
+        for (uint32_t b : h->members[c]) {
+            dgb_block_desc x = p->blocks[b];
+            x.offset -= h->start[c];
+            d.push_back(x);
+        }
+        dgb_plan *sp = nullptr;
+        dgb_status s = dgb_plan_create(d.data(), d.size(), &p->prm, &sp);
+        if (s != DGB_OK) return s;
+        h->sub.push_back(sp);
+        cudaFree(sp->d_scratch);
+        sp->d_scratch = p->d_scratch;
+        sp->borrowed_scratch = true;
+        for (int q = 0; q < 2; q++) sp->variant[q] = p->variant[q];
+    }
+    const size_t slot = (size_t)NV * h->slot_pts;
+    DGB_CUDA(cudaMalloc(&h->d_slots, 6 * slot * sizeof(double)));
+    for (int q = 0; q < 2; q++) {
+        DGB_CUDA(cudaMallocHost(&h->h_in[q], slot * sizeof(double)));
+        DGB_CUDA(cudaMallocHost(&h->h_out[q], slot * sizeof(double)));
+    }
+    DGB_CUDA(cudaStreamCreateWithFlags(&h->s_h2d, cudaStreamNonBlocking));
+    DGB_CUDA(cudaStreamCreateWithFlags(&h->s_comp, cudaStreamNonBlocking));
+    DGB_CUDA(cudaStreamCreateWithFlags(&h->s_d2h, cudaStreamNonBlocking));
+    const size_t nch = h->members.size();
+    h->ev_h2d.resize(nch);
+    h->ev_comp.resize(nch);
+    h->ev_d2h.resize(nch);
+    for (size_t c = 0; c < nch; c++) {
+        DGB_CUDA(cudaEventCreateWithFlags(&h->ev_h2d[c], cudaEventDisableTiming));
+        DGB_CUDA(cudaEventCreateWithFlags(&h->ev_comp[c], cudaEventDisableTiming));
+        DGB_CUDA(cudaEventCreateWithFlags(&h->ev_d2h[c], cudaEventDisableTiming));
+    }
+    return DGB_OK;
+}
+
+dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int precision)
+{
+    HostPipe *h = p->pipe;
+    const long nch = (long)h->members.size();
+    const size_t slot = (size_t)NV * h->slot_pts;
+    const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
+    auto ptrs = [&](int kind, long c, double **out) {  // kind 0: u slot, 1: rhs slot
+        double *base = h->d_slots + (size_t)(3 * kind + (int)(c % 3)) * slot;
+        for (int v = 0; v < NV; v++) out[v] = base + (size_t)v * h->slot_pts;
+    };
+    for (long step = 0; step < nch + 3; step++) {
+        const long c = step - 1, d = step - 2, a = step, e = step - 3;
+        if (c >= 0 && c < nch) {  // compute chunk c once its upload is done
+            DGB_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_h2d[c], 0));
+            if (c >= 3) DGB_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_d2h[c - 3], 0));
+            double *du[NV], *dr[NV];
+            ptrs(0, c, du);
+            ptrs(1, c, dr);
+            dgb_status s = run_rhs(h->sub[c], dr, du, precision, p->variant[prec], h->s_comp);
+            if (s != DGB_OK) return s;
+            DGB_CUDA(cudaEventRecord(h->ev_comp[c], h->s_comp));
+        }
+        if (d >= 0 && d < nch) {  // download chunk d once computed
+            DGB_CUDA(cudaStreamWaitEvent(h->s_d2h, h->ev_comp[d], 0));
+            double *dr[NV];
+            ptrs(1, d, dr);
+            for (int v = 0; v < NV; v++)
+                DGB_CUDA(cudaMemcpyAsync(h->h_out[d % 2] + (size_t)v * h->slot_pts, dr[v],
+                                         h->span[d] * sizeof(double), cudaMemcpyDeviceToHost,
+                                         h->s_d2h));
+            DGB_CUDA(cudaEventRecord(h->ev_d2h[d], h->s_d2h));
+        }
+        if (a < nch) {  // gather and upload chunk a
+            if (a >= 2) DGB_CUDA(cudaEventSynchronize(h->ev_h2d[a - 2]));
+            host_gather(h->h_in[a % 2], h->slot_pts, u, NV, h->start[a], h->span[a]);
+            if (a >= 3) DGB_CUDA(cudaStreamWaitEvent(h->s_h2d, h->ev_comp[a - 3], 0));
+            double *du[NV];
+            ptrs(0, a, du);
+            for (int v = 0; v < NV; v++)
+                DGB_CUDA(cudaMemcpyAsync(du[v], h->h_in[a % 2] + (size_t)v * h->slot_pts,
+                                         h->span[a] * sizeof(double), cudaMemcpyHostToDevice,
+                                         h->s_h2d));
+            DGB_CUDA(cudaEventRecord(h->ev_h2d[a], h->s_h2d));
+        }
+        if (e >= 0 && e < nch) {  // scatter chunk e's interior points back
+            DGB_CUDA(cudaEventSynchronize(h->ev_d2h[e]));
+            host_scatter_interior(rhs, h->h_out[e % 2], h->slot_pts, NV, p->blocks.data(),
+                                  h->members[e].data(), h->members[e].size(), h->start[e]);
+        }
+    }
+    return DGB_OK;
+}
+
+}  // namespace
+
 dgb_status dgb_bssn_rhs_host(dgb_plan *p, double *const *rhs, const double *const *u, int precision)
 {
     if (!p || !rhs || !u) {
         set_error("dgb_bssn_rhs_host: null argument");
         return DGB_ERR_INVALID;
     }
-    const size_t n = p->unzipped;
-    if (n == 0) return DGB_OK;
-    if (!p->d_u) {
-        cudaError_t e = cudaMalloc(&p->d_u, (size_t)NV * n * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&p->d_rhs, (size_t)NV * n * sizeof(double));
-        if (e != cudaSuccess) {
-            cudaFree(p->d_u);
-            p->d_u = nullptr;
-            set_error(std::string("dgb_bssn_rhs_host: ") + cudaGetErrorString(e));
-            return DGB_ERR_ALLOC;
-        }
-    }
-    double *du[NV], *dr[NV];
-    for (int v = 0; v < NV; v++) {
-        du[v] = p->d_u + (size_t)v * n;
-        dr[v] = p->d_rhs + (size_t)v * n;
-        DGB_CUDA(cudaMemcpyAsync(du[v], u[v], n * sizeof(double), cudaMemcpyHostToDevice, 0));
-        // the reference leaves the padding of rhs untouched: carry it through
-        DGB_CUDA(cudaMemcpyAsync(dr[v], rhs[v], n * sizeof(double), cudaMemcpyHostToDevice, 0));
-    }
-    const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
-    dgb_status s = run_rhs(p, dr, du, precision, p->variant[prec], 0);
-    if (s != DGB_OK) return s;
     for (int v = 0; v < NV; v++)
-        DGB_CUDA(cudaMemcpyAsync(rhs[v], dr[v], n * sizeof(double), cudaMemcpyDeviceToHost, 0));
-    DGB_CUDA(cudaStreamSynchronize(0));
+        if (!rhs[v] || !u[v]) {
+            set_error("dgb_bssn_rhs_host: null field pointer");
+            return DGB_ERR_INVALID;
+        }
+    if (precision != DGB_PREC_FP64 && precision != DGB_PREC_MIXED) {
+        set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
+        return DGB_ERR_INVALID;
+    }
+    if (p->blocks.empty()) return DGB_OK;
+    if (!p->pipe) {
+        HostPipe *h = new HostPipe();
+        dgb_status s = build_pipe_into(p, h);
+        if (s != DGB_OK) {
+            destroy_pipe(h);
+            return s;
+        }
+        p->pipe = h;
+    }
+    HostPipe *h = p->pipe;
+    for (size_t c = 0; c < h->sub.size(); c++)  // the parent's schedule choice
+        for (int q = 0; q < 2; q++) h->sub[c]->variant[q] = p->variant[q];
+    dgb_status s = run_pipe(p, rhs, u, precision);
+    // whatever happened, nothing may still be copying into the staging buffers
+    cudaError_t e1 = cudaStreamSynchronize(h->s_h2d);
+    cudaError_t e2 = cudaStreamSynchronize(h->s_comp);
+    cudaError_t e3 = cudaStreamSynchronize(h->s_d2h);
+    if (s != DGB_OK) return s;
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+        set_error(std::string("dgb_bssn_rhs_host: ") +
+                  cudaGetErrorString(e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3));
+        return DGB_ERR_CUDA;
+    }
     return DGB_OK;
 }
 

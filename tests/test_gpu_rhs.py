@@ -89,6 +89,28 @@ def test_rhs_host_entry_matches_device(dgb, gpu):
         assert np.array_equal(dev[v], host[v])
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_rhs_host_pipeline_many_chunks(dgb, gpu, precision, monkeypatch):
+    """The host-array entry as a pipeline over many chunks, with the block
+    list not in offset order: the same bits as the device entry, and the
+    caller's rhs padding untouched."""
+    torch = gpu
+    monkeypatch.setenv("DGB_HOST_CHUNK_PTS", "30000")
+    allb = dgb.synth_blocks(2, SEED2)
+    blocks = repack(dgb, allb, sample_uneven(allb, (6, 3, 2, 0)))
+    rows = [(b.offset, tuple(b.sz), b.bflag, tuple(b.ptmin), tuple(b.ptmax)) for b in blocks]
+    shuffled = dgb.blocks_array(rows[::-1])  # same layout, list in reverse order
+    u = host_fields(dgb, blocks, SEED2)
+    plan = dgb.Plan(shuffled, dgb.default_params(0.1))
+    dev = run_device(dgb, torch, plan, u, precision, rhs_init=[np.full(len(u[0]), 7.0)] * 24)
+    for rep in range(2):  # second call reuses the pipeline
+        host = [np.full(len(u[0]), 7.0) for _ in range(24)]
+        plan.rhs_host(host, u, precision)
+        for v in range(24):
+            assert np.array_equal(dev[v], host[v]), (rep, v)
+    plan.close()
+
+
 def test_block_entry_matches_oracle(dgb, gpu, oracle):
     """dgb_bssnrhs_block_host: the bssnrhs(...) drop-in for one block at an offset."""
     allb = dgb.synth_blocks(2, SEED2)
