@@ -55,9 +55,24 @@ def load_dgb():
     return m
 
 
+def first_blocks(dgb, blocks, nmax):
+    """The first nmax blocks of a list, laid out contiguously from offset 0
+    (the small cases of the profiling captures)."""
+    if not nmax or nmax >= len(blocks):
+        return blocks
+    rows, off = [], 0
+    for b in list(blocks)[:nmax]:
+        rows.append((off, tuple(b.sz), b.bflag, tuple(b.ptmin), tuple(b.ptmax)))
+        off += b.sz[0] * b.sz[1] * b.sz[2]
+    return dgb.blocks_array(rows)
+
+
+MAX_BLOCKS = 0  # --max-blocks
+
+
 def workload(dgb, name):
     if name == "uneven20k":
-        return dgb.synth_blocks(2, SEED2), SEED2, 0.1
+        return first_blocks(dgb, dgb.synth_blocks(2, SEED2), MAX_BLOCKS), SEED2, 0.1
     if name == "uniform512":
         return dgb.synth_blocks(1), SEED1, 0.1
     raise SystemExit(f"unknown workload {name}")
@@ -219,10 +234,14 @@ def main():
                     help="drift: RK4 steps per precision")
     ap.add_argument("--drift-level", type=int, default=10,
                     help="drift: finest octree level")
+    ap.add_argument("--max-blocks", type=int, default=0,
+                    help="use only the first N blocks of the batch (profiling captures)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", action="store_true")
     args = ap.parse_args()
+    global MAX_BLOCKS
+    MAX_BLOCKS = args.max_blocks
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -242,7 +261,8 @@ def main():
     npts = interior_points(blocks)
     units = npts * 24
     wl = {"workload": f"{args.workload}: {len(blocks)} padded blocks "
-                      "(14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)" if args.workload == "uneven20k"
+                      + ("(14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)" if len(blocks) == 20000
+                         else "(first blocks of the uneven batch)") if args.workload == "uneven20k"
           else f"{args.workload}: 512 blocks 13^3, dx 0.05",
           "interior_points": npts, "vars": 24, "fd_order": 6, "ko_sigma": sigma,
           "step": "one bssnRHS (+KO) over all blocks, one persistent launch",
@@ -365,12 +385,13 @@ def main():
 def main_ccz4(args, dgb, rank, world, local):
     """CCZ4 right-hand side (25 variables, kappa = (0.1, 0), KO sigma 0.4) over
     the uneven 20,000-block batch, one persistent launch per step."""
-    blocks = dgb.synth_blocks(2, SEED2)
+    blocks = first_blocks(dgb, dgb.synth_blocks(2, SEED2), MAX_BLOCKS)
     seed, sigma = 20261203 + 5, 0.4
     npts = interior_points(blocks)
     units = npts * 25
     wl = {"workload": f"ccz4_uneven20k: CCZ4 on {len(blocks)} padded blocks "
-                      "(14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)",
+                      + ("(14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)" if len(blocks) == 20000
+                         else "(first blocks of the uneven batch)"),
           "interior_points": npts, "vars": 25, "fd_order": 4, "ko_sigma": sigma,
           "kappa": [0.1, 0.0], "p_expo": -1,
           "step": "one ccz4rhs (+KO, theta_z4 not dissipated) over all blocks, one persistent launch",
@@ -506,7 +527,8 @@ def main_constraints(args, dgb, rank, world, local):
     blocks, seed, _ = workload(dgb, "uneven20k")
     npts = interior_points(blocks)
     wl = {"workload": f"constraints_uneven20k: physical_constraints on {len(blocks)} padded "
-                      "blocks (14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)",
+                      + ("blocks (14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)" if len(blocks) == 20000
+                         else "blocks (first blocks of the uneven batch)"),
           "interior_points": npts, "outputs": 6, "fd_order": 4,
           "step": "one physical_constraints over all blocks, one persistent launch",
           "l2": "inputs (37.8 GB of fields) larger than L2"}
@@ -699,19 +721,21 @@ def main_octree(args, dgb, rank, world, local):
     e2e = None
     if not args.no_e2e:
         k = max(1, min(args.steps, 3))
+        hp = [torch.from_numpy(a).pin_memory() for a in host]  # the caller's state, pinned
+        torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         for _ in range(k):
             for v in range(24):
-                ds[v].copy_(torch.from_numpy(host[v]))
+                ds[v].copy_(hp[v], non_blocking=True)
             st.step(ptrs, dt, nsteps=1, stream=sh)
             for v in range(24):
-                host[v][:] = ds[v].cpu().numpy()
-        torch.cuda.synchronize(dev)
+                hp[v].copy_(ds[v], non_blocking=True)
+            torch.cuda.synchronize(dev)
         e2e_s = (time.perf_counter() - t0) / k
         e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
                "h2d_bytes_per_step": 24 * mesh.ndof * 8, "d2h_bytes_per_step": 24 * mesh.ndof * 8,
                "ms_per_step": e2e_s * 1e3,
-               "path": "state in host arrays: H2D, dgb_rk4_step, D2H every step"}
+               "path": "state in pinned host arrays: H2D, dgb_rk4_step, D2H every step"}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu, _ = cpu_rk4_baseline(dgb, seed, sigma)
