@@ -134,6 +134,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def measured_traffic(key, blocks):
+    """DRAM bytes of one launch (dram__bytes_read + write) from the ncu
+    summaries (profiles/traffic.json), for the full 20,000-block workloads."""
+    if len(blocks) != 20000:
+        return None
+    try:
+        tj = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        return tj[key]["bytes_per_launch"] if key in tj else None
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 def replica_max_ms(ms, world, device):
     """Job time of a replica run: the max over ranks of the per-rank step time.
     The one collective of the run; it carries timing only, never field data."""
@@ -334,15 +346,7 @@ def main():
             "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
             "flop_per_point": FLOP_PER_POINT,
             "hbm_gbs_algorithmic": 24 * 8 * (n + npts) / (ms * 1e-3) / 1e9}
-    traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(traffic_file):
-        try:
-            tj = json.load(open(traffic_file))
-            key = f"{args.workload}:{args.precision}"
-            if key in tj:
-                roof["traffic"] = tj[key]["bytes_per_launch"]
-        except (ValueError, KeyError):
-            pass
+    roof["traffic"] = measured_traffic(f"{args.workload}:{args.precision}", blocks)
 
     e2e = None
     if not args.no_e2e:
@@ -447,7 +451,7 @@ def main_ccz4(args, dgb, rank, world, local):
     fp64_gflops, _ = dgb.measure_fp64_peak()
     achieved = npts * FLOP_PER_POINT_CCZ4 / (ms * 1e-3) / 1e9
     roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
-            "frac": achieved / fp64_gflops, "traffic": None,
+            "frac": achieved / fp64_gflops, "traffic": measured_traffic(f"ccz4_uneven20k:{args.precision}", blocks),
             "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
             "flop_per_point": FLOP_PER_POINT_CCZ4,
             "hbm_gbs_algorithmic": 25 * 8 * (n + npts) / (ms * 1e-3) / 1e9}
@@ -579,7 +583,7 @@ def main_constraints(args, dgb, rank, world, local):
     fp64_gflops, _ = dgb.measure_fp64_peak()
     achieved = npts * FLOP_PER_POINT_PHYSCON / (ms * 1e-3) / 1e9
     roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
-            "frac": achieved / fp64_gflops, "traffic": None,
+            "frac": achieved / fp64_gflops, "traffic": measured_traffic("constraints_uneven20k:fp64", blocks),
             "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
             "flop_per_point": FLOP_PER_POINT_PHYSCON,
             "hbm_gbs_algorithmic": (17 * n + 6 * npts) * 8 / (ms * 1e-3) / 1e9}
