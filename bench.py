@@ -250,7 +250,10 @@ def main():
                     help="use only the first N blocks of the batch (profiling captures)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick the tile schedule by timing (always on for octree_rk4)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="octree_rk4: keep the default 8^3 schedule")
     args = ap.parse_args()
     global MAX_BLOCKS
     MAX_BLOCKS = args.max_blocks
@@ -681,7 +684,7 @@ def main_octree(args, dgb, rank, world, local):
     prec = dgb.PREC_MIXED if args.precision == "mixed" else dgb.PREC_FP64
     op = mesh.operator()
     plan = dgb.Plan(mesh.blocks, dgb.default_params(sigma))
-    if args.autotune:
+    if not args.no_autotune:  # the octree's interiors (7, 13, 25, 49) favour 7^3 tiles
         tu = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(24)]
         tr = [torch.zeros_like(tu[0]) for _ in range(24)]
         plan.synth_fill_device([t.data_ptr() for t in tu], seed, 1e-6)
@@ -812,6 +815,12 @@ def main_drift(args, dgb):
     plan = dgb.Plan(mesh.blocks, dgb.default_params(0.4))
     uz = dgb.UnzipPlan(mesh.operator(), mesh.ndof)
     U = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(24)]
+    Rt = [torch.zeros_like(U[0]) for _ in range(24)]
+    plan.synth_fill_device([t.data_ptr() for t in U], seed, 1e-6)
+    for prec in (dgb.PREC_FP64, dgb.PREC_MIXED):  # tile schedule per precision
+        plan.autotune([t.data_ptr() for t in Rt], [t.data_ptr() for t in U], prec)
+    del Rt
+    torch.cuda.empty_cache()
     Cu = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(6)]
     Cz = [torch.zeros(mesh.ndof, dtype=torch.float64, device=dev) for _ in range(6)]
     host = [np.empty(mesh.ndof) for _ in range(24)]

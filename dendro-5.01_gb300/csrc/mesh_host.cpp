@@ -539,6 +539,36 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
             delete M;
             return DGB_ERR_INVALID;  // an independent node without an owning block
         }
+    // ---- renumber the independent nodes in the order their owners are laid
+    // out (block by block, x fastest): the zip then reads and writes runs of
+    // consecutive addresses, and the unzip copies of a block's own interior
+    // read them, instead of gathering across the whole zipped vector.  From
+    // here on dof_keys is in that order (the lookup above needs no more).
+    {
+        std::vector<uint32_t> owner_of(off, SENT);
+        for (uint64_t d = 0; d < ndof; d++) owner_of[M->zip_src[d]] = (uint32_t)d;
+        std::vector<uint32_t> newid(ndof);
+        std::vector<uint64_t> keys2(ndof), zip2(ndof);
+        uint32_t next = 0;
+        for (uint64_t p = 0; p < off; p++) {
+            const uint32_t d = owner_of[p];
+            if (d == SENT) continue;
+            newid[d] = next;
+            keys2[next] = M->dof_keys[d];
+            zip2[next] = p;
+            next++;
+        }
+        M->dof_keys.swap(keys2);
+        M->zip_src.swap(zip2);
+#pragma omp parallel for schedule(static)
+        for (long long p = 0; p < (long long)off; p++)
+            if (M->copy_src[p] != SENT) M->copy_src[p] = newid[M->copy_src[p]];
+#pragma omp parallel for schedule(static)
+        for (long long q = 0; q < (long long)M->src_refs.size(); q++) {
+            const uint64_t r = M->src_refs[q];
+            if (!(r & kInterp)) M->src_refs[q] = newid[r];
+        }
+    }
     *out = M;
     return DGB_OK;
 }

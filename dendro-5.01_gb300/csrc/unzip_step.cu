@@ -108,7 +108,15 @@ __global__ void __launch_bounds__(256) unzip_copy_kernel(const FieldPtrs f, cons
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += stride) {
         const uint32_t s = __ldg(src + p);
         if (s == kSentinel) continue;
-        for (int v = 0; v < f.nvars; v++) f.out[v][p] = __ldg(f.in[v] + s);
+        // all loads before the stores: 24 independent reads in flight per
+        // thread (out and in are not known not to alias)
+        double val[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++)
+            if (v < f.nvars) val[v] = __ldg(f.in[v] + s);
+#pragma unroll
+        for (int v = 0; v < NV; v++)
+            if (v < f.nvars) f.out[v][p] = val[v];
     }
 }
 
@@ -177,7 +185,13 @@ __global__ void __launch_bounds__(256) zip_kernel(const FieldPtrs f, const uint6
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t d = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; d < n; d += stride) {
         const uint64_t s = __ldg(src + d);
-        for (int v = 0; v < f.nvars; v++) f.out[v][d] = __ldg(f.in[v] + s);
+        double val[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++)
+            if (v < f.nvars) val[v] = __ldg(f.in[v] + s);
+#pragma unroll
+        for (int v = 0; v < NV; v++)
+            if (v < f.nvars) f.out[v][d] = val[v];
     }
 }
 
