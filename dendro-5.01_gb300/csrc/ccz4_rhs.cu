@@ -123,7 +123,9 @@ struct C4Geo {
     static constexpr int DXB = TX * (TY + 4) * (TZ + 4);  // d_x on the +-2 cross region
     static constexpr int DYB = TX * TY * (TZ + 4);
     static constexpr int PMAX = TX * TY * TZ;
-    static constexpr size_t bytes = (size_t)(2 * FBUF + DXB + DYB + 3 * PMAX) * 8;
+    // doubles: two staged fields, the d_x / d_y boxes, the shift at the tile
+    // points; then per direction the tile points ordered by the sign of the shift
+    static constexpr size_t bytes = (size_t)(2 * FBUF + DXB + DYB + 3 * PMAX) * 8 + 3 * PMAX * 2;
     // + hi/lo planes of the staged field and the s + e pair boxes (floats)
     static constexpr size_t bytes_mixed = bytes + (size_t)(2 * FBUF + 2 * DXB + 2 * DYB) * 4;
 };
@@ -172,7 +174,9 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
     double *dxb = fb1 + G::FBUF;
     double *dyb = dxb + G::DXB;
     double *bet = dyb + G::DYB;  // beta0..2 at the tile points
-    float *fhi = reinterpret_cast<float *>(bet + 3 * G::PMAX);  // MIXED only
+    // per direction d: tile points with beta_d > 0 first, then the others
+    uint16_t *advl = reinterpret_cast<uint16_t *>(bet + 3 * G::PMAX);
+    float *fhi = reinterpret_cast<float *>(advl + 3 * G::PMAX);  // MIXED only
     float *flo = fhi + G::FBUF;
     float *dxs = flo + G::FBUF;
     float *dxe = dxs + G::DXB;
@@ -193,14 +197,45 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
     const Ax4 ax[3] = {ax4(blk.h[0]), ax4(blk.h[1]), ax4(blk.h[2])};
     const int nn[3] = {nx, ny, nz};
 
+    // The upwind direction of every advective derivative is the sign of the
+    // shift at the point; with points ordered by that sign per direction, a
+    // warp evaluates one upwind form instead of both (the order of the points
+    // does not change any result: each writes its own slot).
+    __shared__ int s_cnt[6];
+    if (tid < 6) s_cnt[tid] = 0;
+    __syncthreads();
     for (int p = tid; p < P; p += kC4Threads) {
         const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
         const uint64_t gi = blk.offset + (uint64_t)(w.o[0] + ti + 3)
                           + (uint64_t)nx * ((uint64_t)(w.o[1] + tj + 3) + (uint64_t)ny * (w.o[2] + tk + 3));
-        bet[p] = __ldg(args.u[6] + gi);
-        bet[G::PMAX + p] = __ldg(args.u[7] + gi);
-        bet[2 * G::PMAX + p] = __ldg(args.u[8] + gi);
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const double b = __ldg(args.u[6 + d] + gi);
+            bet[d * G::PMAX + p] = b;
+            const int q = b > 0.0 ? atomicAdd(&s_cnt[2 * d], 1) : P - 1 - atomicAdd(&s_cnt[2 * d + 1], 1);
+            advl[d * G::PMAX + q] = (uint16_t)p;
+        }
     }
+    const int st3[3] = {1, sy, sz};
+    auto tile_pos = [&](int p, int d, int *ti_, int *tj_, int *tk_) {
+        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        *ti_ = ti; *tj_ = tj; *tk_ = tk;
+        return (d == 0 ? w.o[0] + ti : d == 1 ? w.o[1] + tj : w.o[2] + tk) + 3;
+    };
+
+    // FP64 upwind derivatives over the tile points ordered by the sign of the shift
+    auto adv64_sorted = [&](const double *F, double *Sa) {
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+            for (int q = tid; q < P; q += kC4Threads) {
+                const int p = advl[d * G::PMAX + q];
+                int ti, tj, tk;
+                const int pos = tile_pos(p, d, &ti, &tj, &tk);
+                const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                Sa[d * G::PMAX + p] = adv42_at(c, st3[d], pos, nn[d], lo[d], hi[d],
+                                               bet[d * G::PMAX + p], ax[d]);
+            }
+    };
 
     auto issue_load = [&](int v, double *dst) {
         const double *src = args.u[v] + rbase;
@@ -240,26 +275,36 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                 return r;
             };
             auto to64 = [](FP2 r, double scale) { return __dmul_rn(fp2_widen(r), scale); };
-            // one point: advective and (theta excluded) KO in FP32, scaled in FP64
+            // one point: KO (theta excluded) in FP32, scaled and summed in FP64
             auto adv_ko = [&](int p, int off, const int *pos) {
                 const int st[3] = {1, sy, sz};
+                if (v == kC4Theta) return;
                 double ko = 0.0;
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
-                    const bool up = bet[d * G::PMAX + p] > 0.0;
-                    FP2 a = up ? nadvp_c(fhi + off, st[d]) : nadvn_c(fhi + off, st[d]);
-                    a.e = __fadd_rn(a.e, up ? nadvp(flo + off, st[d]) : nadvn(flo + off, st[d]));
-                    Sa[d * G::PMAX + p] = to64(a, ax[d].c12);
-                    if (v != kC4Theta) {
-                        // the first / last interior point takes its neighbour's stencil
-                        const int sh = pos[d] == 3 ? st[d] : (pos[d] == nn[d] - 4 ? -st[d] : 0);
-                        FP2 k = nko_c(fhi + off + sh, st[d]);
-                        k.e = __fadd_rn(k.e, nko_32(flo + off + sh, st[d]));
-                        const double kd = to64(k, ax[d].pre);
-                        ko = d == 0 ? kd : __dadd_rn(ko, kd);
-                    }
+                    // the first / last interior point takes its neighbour's stencil
+                    const int sh = pos[d] == 3 ? st[d] : (pos[d] == nn[d] - 4 ? -st[d] : 0);
+                    FP2 k = nko_c(fhi + off + sh, st[d]);
+                    k.e = __fadd_rn(k.e, nko_32(flo + off + sh, st[d]));
+                    const double kd = to64(k, ax[d].pre);
+                    ko = d == 0 ? kd : __dadd_rn(ko, kd);
                 }
-                if (v != kC4Theta) Sko[p] = ko;
+                Sko[p] = ko;
+            };
+            // upwind derivatives over the tile points ordered by the sign of the shift
+            auto adv_sorted = [&]() {
+#pragma unroll
+                for (int d = 0; d < 3; d++)
+                    for (int q = tid; q < P; q += kC4Threads) {
+                        const int p = advl[d * G::PMAX + q];
+                        int ti, tj, tk;
+                        tile_pos(p, d, &ti, &tj, &tk);
+                        const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                        const bool up = bet[d * G::PMAX + p] > 0.0;
+                        FP2 a = up ? nadvp_c(fhi + off, st3[d]) : nadvn_c(fhi + off, st3[d]);
+                        a.e = __fadd_rn(a.e, up ? nadvp(flo + off, st3[d]) : nadvn(flo + off, st3[d]));
+                        Sa[d * G::PMAX + p] = to64(a, ax[d].c12);
+                    }
             };
             if (q2 < 0) {
                 for (int p = tid; p < P; p += kC4Threads) {
@@ -273,6 +318,7 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                     }
                     adv_ko(p, off, pos);
                 }
+                adv_sorted();
             } else {
                 double *S2 = S + (size_t)(DGB_CCZ4_D20 + 6 * q2) * G::PMAX;
                 const int by = ey + 4;
@@ -316,6 +362,7 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                     }
                     adv_ko(p, off, pos);
                 }
+                adv_sorted();
                 __syncthreads();
                 const double cxy = ax[0].c12 * ax[1].c12, cxz = ax[0].c12 * ax[2].c12,
                              cyz = ax[1].c12 * ax[2].c12;
@@ -340,8 +387,6 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
                     if (want_grad) Sg[d * G::PMAX + p] = d1_42_at(c, st[d], pos[d], nn[d], lo[d], hi[d], ax[d]);
-                    Sa[d * G::PMAX + p] = adv42_at(c, st[d], pos[d], nn[d], lo[d], hi[d],
-                                                   bet[d * G::PMAX + p], ax[d]);
                     if (v != kC4Theta) {
                         const double k = ko42c_at(c, st[d], pos[d], nn[d], lo[d], hi[d], ax[d]);
                         ko = d == 0 ? k : __dadd_rn(ko, k);
@@ -349,6 +394,7 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                 }
                 if (v != kC4Theta) Sko[p] = ko;
             }
+            adv64_sorted(F, Sa);
         } else {
             double *S2 = S + (size_t)(DGB_CCZ4_D20 + 6 * q2) * G::PMAX;
             // (1a) d_x on x in tile and (y in tile +- 2, z in tile) or (y in tile, z halo of 2)
@@ -387,13 +433,12 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                 double ko = 0.0;
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
-                    Sa[d * G::PMAX + p] = adv42_at(c, st[d], pos[d], nn[d], lo[d], hi[d],
-                                                   bet[d * G::PMAX + p], ax[d]);
                     const double k = ko42c_at(c, st[d], pos[d], nn[d], lo[d], hi[d], ax[d]);
                     ko = d == 0 ? k : __dadd_rn(ko, k);
                 }
                 Sko[p] = ko;
             }
+            adv64_sorted(F, Sa);
             __syncthreads();
             // (2) mixed from the boxes; d_x, d_y at the tile points
             for (int p = tid; p < P; p += kC4Threads) {

@@ -195,11 +195,12 @@ __device__ __forceinline__ double ko42c_at(const double *c, int s, int pos, int 
         t = __dadd_rn(t, dgb_mul_const<3>(c[-s]));
         return __ddiv_rn(__dsub_rn(t, c[0]), a.smr3);
     }
-    // first interior point: the stencil of pos 4, written from u7 down to u1
-    if (pos == 3) return __dmul_rn(a.pre, ko7(c + s, -s));
-    // last interior point: the stencil of pos n-5, written from u[n-2] down
-    if (pos == ie - 1) return __dmul_rn(a.pre, ko7(c - s, -s));
-    return __dmul_rn(a.pre, ko7(c, s));
+    // first interior point: the stencil of pos 4, written from u7 down to u1;
+    // last interior point: the stencil of pos n-5, written from u[n-2] down.
+    // Centre and step are selected, not branched on, so a warp that holds an
+    // end point of a line does not diverge.
+    const int sh = pos == 3 ? s : (pos == ie - 1 ? -s : 0);
+    return __dmul_rn(a.pre, ko7(c + sh, sh != 0 ? -s : s));
 }
 
 }  // namespace
