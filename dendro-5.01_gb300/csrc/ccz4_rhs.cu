@@ -22,9 +22,10 @@
 //
 // Mixed precision (MIXED = true, interior blocks): every stencil runs in
 // FP32 on the split doubles (fp32split.cuh), compensated on the hi part and
-// plain on the lo part, and is widened, added and scaled in FP64; the
-// algebra, the KO sum across directions, the boundary condition and all
-// field I/O stay FP64.  Domain-boundary blocks take the FP64 stencils.
+// plain on the lo part, is scaled by its float-pair scale and (KO) summed
+// across directions as float pairs, and reaches FP64 with one add; the
+// algebra, the boundary condition and all field I/O stay FP64.
+// Domain-boundary blocks take the FP64 stencils.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -274,22 +275,27 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                 r.e = __fadd_rn(r.e, n1_4(l, s));
                 return r;
             };
-            auto to64 = [](FP2 r, double scale) { return __dmul_rn(fp2_widen(r), scale); };
+            // scales as float pairs: scaling and the KO sum stay in FP32 pairs
+            const FC f12[3] = {split_const(ax[0].c12), split_const(ax[1].c12), split_const(ax[2].c12)};
+            const FC f12sq[3] = {split_const(ax[0].c12sq), split_const(ax[1].c12sq),
+                                 split_const(ax[2].c12sq)};
+            const FC fpre[3] = {split_const(ax[0].pre), split_const(ax[1].pre), split_const(ax[2].pre)};
+            auto to64 = [](FP2 r, FC f) { return fp2_widen(mulfc(r, f)); };
             // one point: KO (theta excluded) in FP32, scaled and summed in FP64
             auto adv_ko = [&](int p, int off, const int *pos) {
                 const int st[3] = {1, sy, sz};
                 if (v == kC4Theta) return;
-                double ko = 0.0;
+                FP2 ko{0.0f, 0.0f};
 #pragma unroll
                 for (int d = 0; d < 3; d++) {
                     // the first / last interior point takes its neighbour's stencil
                     const int sh = pos[d] == 3 ? st[d] : (pos[d] == nn[d] - 4 ? -st[d] : 0);
                     FP2 k = nko_c(fhi + off + sh, st[d]);
                     k.e = __fadd_rn(k.e, nko_32(flo + off + sh, st[d]));
-                    const double kd = to64(k, ax[d].pre);
-                    ko = d == 0 ? kd : __dadd_rn(ko, kd);
+                    const FP2 kd = mulfc(k, fpre[d]);
+                    ko = d == 0 ? kd : add2(ko, kd);
                 }
-                Sko[p] = ko;
+                Sko[p] = fp2_widen(ko);
             };
             // upwind derivatives over the tile points ordered by the sign of the shift
             auto adv_sorted = [&]() {
@@ -303,7 +309,7 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                         const bool up = bet[d * G::PMAX + p] > 0.0;
                         FP2 a = up ? nadvp_c(fhi + off, st3[d]) : nadvn_c(fhi + off, st3[d]);
                         a.e = __fadd_rn(a.e, up ? nadvp(flo + off, st3[d]) : nadvn(flo + off, st3[d]));
-                        Sa[d * G::PMAX + p] = to64(a, ax[d].c12);
+                        Sa[d * G::PMAX + p] = to64(a, f12[d]);
                     }
             };
             if (q2 < 0) {
@@ -312,9 +318,9 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                     const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                     if (want_grad) {
-                        Sg[p] = to64(N1(fhi + off, flo + off, 1), ax[0].c12);
-                        Sg[G::PMAX + p] = to64(N1(fhi + off, flo + off, sy), ax[1].c12);
-                        Sg[2 * G::PMAX + p] = to64(N1(fhi + off, flo + off, sz), ax[2].c12);
+                        Sg[p] = to64(N1(fhi + off, flo + off, 1), f12[0]);
+                        Sg[G::PMAX + p] = to64(N1(fhi + off, flo + off, sy), f12[1]);
+                        Sg[2 * G::PMAX + p] = to64(N1(fhi + off, flo + off, sz), f12[2]);
                     }
                     adv_ko(p, off, pos);
                 }
@@ -351,30 +357,30 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                     const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
                     const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                    Sg[2 * G::PMAX + p] = to64(N1(fhi + off, flo + off, sz), ax[2].c12);
+                    Sg[2 * G::PMAX + p] = to64(N1(fhi + off, flo + off, sz), f12[2]);
                     const int st[3] = {1, sy, sz};
                     const int slot[3] = {0, 3, 5};
 #pragma unroll
                     for (int d = 0; d < 3; d++) {
                         FP2 h = n2_4c(fhi + off, st[d]);
                         h.e = __fadd_rn(h.e, n2_4(flo + off, st[d]));
-                        S2[slot[d] * G::PMAX + p] = to64(h, ax[d].c12sq);
+                        S2[slot[d] * G::PMAX + p] = to64(h, f12sq[d]);
                     }
                     adv_ko(p, off, pos);
                 }
                 adv_sorted();
                 __syncthreads();
-                const double cxy = ax[0].c12 * ax[1].c12, cxz = ax[0].c12 * ax[2].c12,
-                             cyz = ax[1].c12 * ax[2].c12;
+                const FC fxy = split_const(ax[0].c12 * ax[1].c12), fxz = split_const(ax[0].c12 * ax[2].c12),
+                         fyz = split_const(ax[1].c12 * ax[2].c12);
                 for (int p = tid; p < P; p += kC4Threads) {
                     const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
                     const int bxi = ti + ex * ((tj + 2) + by * (tk + 2));
                     const int byi = ti + ex * (tj + ey * (tk + 2));
-                    Sg[p] = __dmul_rn(__dadd_rn(widen(dxs[bxi]), widen(dxe[bxi])), ax[0].c12);
-                    Sg[G::PMAX + p] = __dmul_rn(__dadd_rn(widen(dys[byi]), widen(dye[byi])), ax[1].c12);
-                    S2[1 * G::PMAX + p] = to64(N1(dxs + bxi, dxe + bxi, ex), cxy);
-                    S2[2 * G::PMAX + p] = to64(N1(dxs + bxi, dxe + bxi, ex * by), cxz);
-                    S2[4 * G::PMAX + p] = to64(N1(dys + byi, dye + byi, ex * ey), cyz);
+                    Sg[p] = to64(FP2{dxs[bxi], dxe[bxi]}, f12[0]);
+                    Sg[G::PMAX + p] = to64(FP2{dys[byi], dye[byi]}, f12[1]);
+                    S2[1 * G::PMAX + p] = to64(N1(dxs + bxi, dxe + bxi, ex), fxy);
+                    S2[2 * G::PMAX + p] = to64(N1(dxs + bxi, dxe + bxi, ex * by), fxz);
+                    S2[4 * G::PMAX + p] = to64(N1(dys + byi, dye + byi, ex * ey), fyz);
                 }
             }
         } else if (q2 < 0) {

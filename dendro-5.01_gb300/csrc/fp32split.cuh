@@ -121,5 +121,27 @@ __device__ __forceinline__ FP2 nko_c(const float *u, int s)
 }
 __device__ __forceinline__ double fp2_widen(FP2 h) { return __dadd_rn(widen(h.s), widen(h.e)); }
 
+// A double scale held as a float pair c = hi + lo (2^-48 relative), so that
+// the scaling of a stencil numerator stays on the FP32 pipes: TwoProduct for
+// s * hi, the small cross terms in FP32; the FP64 side is the one add of
+// fp2_widen.  Built once per tile.
+struct FC {
+    float hi, lo;
+};
+__device__ __forceinline__ FC split_const(double c)
+{
+    FC r;
+    r.hi = __double2float_rn(c);
+    r.lo = __double2float_rn(c - (double)r.hi);
+    return r;
+}
+__device__ __forceinline__ FP2 mulfc(FP2 x, FC c)
+{
+    FP2 r;
+    r.s = __fmul_rn(x.s, c.hi);
+    r.e = __fadd_rn(__fmaf_rn(x.s, c.hi, -r.s), __fadd_rn(__fmul_rn(x.s, c.lo), __fmul_rn(x.e, c.hi)));
+    return r;
+}
+
 }  // namespace
 }  // namespace dgb

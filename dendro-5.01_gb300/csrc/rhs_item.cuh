@@ -30,9 +30,9 @@
 // and evaluates every stencil in FP32 on symmetric differences
 // (u[+k] - u[-k], (u[k] - u0) + (u[-k] - u0)): compensated (TwoSum /
 // FMA TwoProduct) on the hi part, plain on the lo part.  Each stencil's
-// float pair is widened to FP64 by integer bit operations, added and scaled
-// in FP64; the sums across stencil terms (KO over directions, the algebra),
-// the RK update and all field I/O stay FP64.
+// float pair is scaled by its float-pair scale (and KO summed over the three
+// directions) in FP32 pairs and widened to FP64 by integer bit operations
+// with one FP64 add; the algebra, the RK update and all field I/O stay FP64.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -485,19 +485,22 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 h.e = __fadd_rn(h.e, nko_32(flo + off, s));
                 return h;
             };
-            // KO sum across the three directions in FP64
+            // scales as float pairs: the scaling and the KO sum across the three
+            // directions stay in FP32 pairs, one FP64 add per result
+            const FC f60[3] = {split_const(c60[0]), split_const(c60[1]), split_const(c60[2])};
+            const FC f180[3] = {split_const(c180[0]), split_const(c180[1]), split_const(c180[2])};
+            const FC fko[3] = {split_const(ko[0]), split_const(ko[1]), split_const(ko[2])};
             auto KO3 = [&](int off) {
-                return __dadd_rn(__dadd_rn(__dmul_rn(fp2_widen(NK(off, 1)), ko[0]),
-                                           __dmul_rn(fp2_widen(NK(off, sy)), ko[1])),
-                                 __dmul_rn(fp2_widen(NK(off, sz)), ko[2]));
+                return fp2_widen(add2(add2(mulfc(NK(off, 1), fko[0]), mulfc(NK(off, sy), fko[1])),
+                                      mulfc(NK(off, sz), fko[2])));
             };
             if (q2 < 0) {
                 for (int p = tid; p < P; p += kThreads) {
                     const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                    Sg[p] = __dmul_rn(fp2_widen(N1(off, 1)), c60[0]);
-                    Sg[G::PMAX + p] = __dmul_rn(fp2_widen(N1(off, sy)), c60[1]);
-                    Sg[2 * G::PMAX + p] = __dmul_rn(fp2_widen(N1(off, sz)), c60[2]);
+                    Sg[p] = fp2_widen(mulfc(N1(off, 1), f60[0]));
+                    Sg[G::PMAX + p] = fp2_widen(mulfc(N1(off, sy), f60[1]));
+                    Sg[2 * G::PMAX + p] = fp2_widen(mulfc(N1(off, sz), f60[2]));
                     Sko[p] = KO3(off);
                 }
             } else {
@@ -531,31 +534,32 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 for (int p = tid; p < P; p += kThreads) {
                     const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                    Sg[2 * G::PMAX + p] = __dmul_rn(fp2_widen(N1(off, sz)), c60[2]);
-                    S2[0 * G::PMAX + p] = __dmul_rn(fp2_widen(N2(off, 1)), c180[0]);
-                    S2[3 * G::PMAX + p] = __dmul_rn(fp2_widen(N2(off, sy)), c180[1]);
-                    S2[5 * G::PMAX + p] = __dmul_rn(fp2_widen(N2(off, sz)), c180[2]);
+                    Sg[2 * G::PMAX + p] = fp2_widen(mulfc(N1(off, sz), f60[2]));
+                    S2[0 * G::PMAX + p] = fp2_widen(mulfc(N2(off, 1), f180[0]));
+                    S2[3 * G::PMAX + p] = fp2_widen(mulfc(N2(off, sy), f180[1]));
+                    S2[5 * G::PMAX + p] = fp2_widen(mulfc(N2(off, sz), f180[2]));
                     Sko[p] = KO3(off);
                 }
                 __syncthreads();
                 // (2) mixed: the pair boxes differentiated again (compensated on s,
                 // plain on e), both scales applied in FP64
-                const double cxy = c60[0] * c60[1], cxz = c60[0] * c60[2], cyz = c60[1] * c60[2];
+                const FC fxy = split_const(c60[0] * c60[1]), fxz = split_const(c60[0] * c60[2]),
+                         fyz = split_const(c60[1] * c60[2]);
                 for (int p = tid; p < P; p += kThreads) {
                     const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
                     const int bxi = ti + ex * ((tj + 3) + bx_y * (tk + 3));
                     const int byi = ti + ex * (tj + ey * (tk + 3));
-                    Sg[p] = __dmul_rn(__dadd_rn(widen(dxs[bxi]), widen(dxe[bxi])), c60[0]);
-                    Sg[G::PMAX + p] = __dmul_rn(__dadd_rn(widen(dys[byi]), widen(dye[byi])), c60[1]);
+                    Sg[p] = fp2_widen(mulfc(FP2{dxs[bxi], dxe[bxi]}, f60[0]));
+                    Sg[G::PMAX + p] = fp2_widen(mulfc(FP2{dys[byi], dye[byi]}, f60[1]));
                     FP2 h = n1_c(dxs + bxi, ex);
                     h.e = __fadd_rn(h.e, n1_32(dxe + bxi, ex));
-                    S2[1 * G::PMAX + p] = __dmul_rn(fp2_widen(h), cxy);
+                    S2[1 * G::PMAX + p] = fp2_widen(mulfc(h, fxy));
                     h = n1_c(dxs + bxi, ex * bx_y);
                     h.e = __fadd_rn(h.e, n1_32(dxe + bxi, ex * bx_y));
-                    S2[2 * G::PMAX + p] = __dmul_rn(fp2_widen(h), cxz);
+                    S2[2 * G::PMAX + p] = fp2_widen(mulfc(h, fxz));
                     h = n1_c(dys + byi, ex * ey);
                     h.e = __fadd_rn(h.e, n1_32(dye + byi, ex * ey));
-                    S2[4 * G::PMAX + p] = __dmul_rn(fp2_widen(h), cyz);
+                    S2[4 * G::PMAX + p] = fp2_widen(mulfc(h, fyz));
                 }
             }
         }
