@@ -239,7 +239,7 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--workload", default="uneven20k",
                     choices=["uneven20k", "uniform512", "octree_rk4", "drift", "ccz4_uneven20k",
-                             "constraints_uneven20k"])
+                             "constraints_uneven20k", "wavelet_octree"])
     ap.add_argument("--fine-radius", type=float, default=1.0,
                     help="octree_rk4: radius of the finest level around each puncture")
     ap.add_argument("--drift-steps", type=int, default=100,
@@ -248,6 +248,10 @@ def main():
                     help="drift: finest octree level")
     ap.add_argument("--max-blocks", type=int, default=0,
                     help="use only the first N blocks of the batch (profiling captures)")
+    ap.add_argument("--octree-level", type=int, default=10,
+                    help="wavelet_octree: finest octree level (smaller cases for captures)")
+    ap.add_argument("--wavelet-vars", default="0",
+                    help="wavelet_octree: comma-separated refinement variable ids")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", action="store_true",
@@ -272,6 +276,8 @@ def main():
         return main_ccz4(args, dgb, rank, world, local)
     if args.workload == "constraints_uneven20k":
         return main_constraints(args, dgb, rank, world, local)
+    if args.workload == "wavelet_octree":
+        return main_wavelets(args, dgb, rank, world, local)
     blocks, seed, sigma = workload(dgb, args.workload)
     npts = interior_points(blocks)
     units = npts * 24
@@ -606,11 +612,11 @@ def main_constraints(args, dgb, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
-def octree_params(dgb, fine_radius):
+def octree_params(dgb, fine_radius, max_level=10):
     """2:1-balanced octree on [-32,32]^3: level 10 within fine_radius of each
     puncture, one level coarser per doubling of the distance, down to level 4;
     blocks of up to 8^3 leaves."""
-    return dgb.mesh_params(max_level=10, min_level=4, fine_radius=fine_radius)
+    return dgb.mesh_params(max_level=max_level, min_level=4, fine_radius=fine_radius)
 
 
 def cpu_rk4_baseline(dgb, seed, sigma, steps=1):
@@ -759,6 +765,216 @@ def main_octree(args, dgb, rank, world, local):
                           "impl": "ours"}))
     st.close()
     uz.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# Algorithmic FP64 operations of the wavelet indicator per leaf and variable:
+# interior leaf 196 + 112 + 64 seven-term interpolations (13 each) and 64
+# wavelets (difference, quotient, square, sum); boundary leaf 48 + 36 + 27
+# four-term interpolations (7 each) and 27 wavelets.
+FLOP_WAVELET_INTERIOR = 372 * 13 + 64 * 4
+FLOP_WAVELET_BOUNDARY = 111 * 7 + 27 * 4
+
+
+def cpu_wavelet_baseline(dgb, mesh, host_unzipped, var_ids, tables, tol, fac, target_s=12.0,
+                         steps=1):
+    """Oracle port of isReMeshUnzip (eight-child interpolation per element, as
+    the reference computes it) over a leaf sample, OpenMP over leaves."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    ora = oracle_py.Oracle()
+    cores = os.cpu_count() or 1
+    n = mesh.num_leaves
+    k = 64
+    while True:
+        idx = np.arange(0, n, k)
+        sub = {key: tables[key][idx] for key in ("patch_base", "block_side", "boundary")}
+        t0 = time.perf_counter()
+        ora.remesh_wavelets(host_unzipped, var_ids, sub["patch_base"], sub["block_side"],
+                            sub["boundary"], tol[idx], fac, cores)
+        dt = time.perf_counter() - t0
+        if dt > 0.25 * target_s or k == 1:
+            break
+        k = max(1, int(k / max(2.0, min(50.0, target_s / max(dt, 1e-3)))))
+    vals = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        ora.remesh_wavelets(host_unzipped, var_ids, sub["patch_base"], sub["block_side"],
+                            sub["boundary"], tol[idx], fac, cores)
+        vals.append(len(idx) / (time.perf_counter() - t0))
+    return {"value": float(np.median(vals)), "unit": "leaves/s", "cores": cores, "kind": "port",
+            "sample": f"every {k}-th leaf ({len(idx)} of {n}), refinement vars {var_ids}, "
+                      f"eight-child interpolation per element as WaveletEl computes it"}, vals
+
+
+def main_wavelets(args, dgb, rank, world, local):
+    """Mesh::isReMeshUnzip's wavelet indicator over every leaf of the level-10
+    octree (the octree_rk4 mesh) on its unzipped fields; units = leaves/s."""
+    seed = 20261203 + 5
+    var_ids = [int(v) for v in args.wavelet_vars.split(",")]
+    tol_min, fac = 1e-3, 1.0  # BSSN_WAVELET_TOL, BSSN_DENDRO_AMR_FAC of BSSN_GR/src/bssn.par.json
+    mesh = dgb.Mesh(octree_params(dgb, args.fine_radius, args.octree_level))
+    tables = mesh.leaf_patches()
+    tol = dgb.wavelet_tol_radial(tables["corner"], tol_min)
+    nl = mesh.num_leaves
+    nb = int(tables["boundary"].sum())
+    wl = {"workload": f"wavelet_octree: isReMeshUnzip indicator on the level-{args.octree_level} octree "
+                      f"({nl} leaves, {nb} on the domain boundary, {mesh.nblocks} blocks, "
+                      f"{mesh.nunzipped} unzipped points)",
+          "refine_vars": var_ids, "wavelet_tol": tol_min, "amr_coarse_fac": fac,
+          "step": "one wavelet indicator launch over all leaves (flags + per-leaf maximum)",
+          "units": "leaves per second",
+          "l2": "unzipped field (%.1f GB per variable) larger than L2" % (mesh.nunzipped * 8 / 1e9)}
+    metric = "isReMeshUnzip wavelet indicator leaves/s on 1 GB300 (FP64)"
+    xyz = mesh.dof_coords()
+    host = [np.empty(mesh.ndof) for _ in range(24)]
+    dgb.synth_fill_points(xyz, host, seed, 1e-6)
+    op = mesh.operator()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py
+        hu = [None] * 24
+        for v in var_ids:
+            hu[v] = oracle_py.unzip_apply(op, host[v], mesh.nunzipped)
+        hu = [a if a is not None else hu[var_ids[0]] for a in hu]
+        base, vals = cpu_wavelet_baseline(dgb, mesh, hu, var_ids, tables, tol, fac,
+                                          steps=args.steps + args.warmup)
+        v = float(np.median(vals[args.warmup:])) if len(vals) > args.warmup else base["value"]
+        print(json.dumps({"metric": metric, "value": v, "unit": "leaves/s", "n_gpus": 1,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": nl / v * 1e3,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64", "data": "synthetic", "config": wl, "impl": "reference",
+                          "cpu_baseline": dict(base, value=v),
+                          "e2e": {"value": v, "unit": "leaves/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    import torch
+    init_replicas(world, local)
+    dev = torch.device("cuda", local)
+    dgb.init(local)
+    uz = dgb.UnzipPlan(op, mesh.ndof)
+    ds = [torch.from_numpy(a).to(dev) for a in host]
+    du = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(24)]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    uz.unzip([t.data_ptr() for t in ds], [t.data_ptr() for t in du], sh)
+    d_base = torch.from_numpy(tables["patch_base"].astype(np.int64)).to(dev)
+    d_side = torch.from_numpy(tables["block_side"].astype(np.int32)).to(dev)
+    d_bdy = torch.from_numpy(tables["boundary"]).to(dev)
+    d_tol = torch.from_numpy(tol).to(dev)
+    wmax = torch.zeros(nl, dtype=torch.float64, device=dev)
+    flags = torch.zeros(nl, dtype=torch.uint8, device=dev)
+    changed = torch.zeros(1, dtype=torch.int64, device=dev)
+    uptr = [t.data_ptr() for t in du]
+
+    def launch(vids=var_ids, tol_t=d_tol):
+        dgb.remesh_wavelets(uptr, vids, mesh.nunzipped, nl, d_base.data_ptr(), d_side.data_ptr(),
+                            d_bdy.data_ptr(), tol_t.data_ptr(), fac, wmax.data_ptr(),
+                            flags.data_ptr(), changed.data_ptr(), sh)
+
+    # L2 flush: a 2 GB scratch buffer is written before every timed launch,
+    # outside its events, so each launch starts with the fields out of L2
+    scratch = torch.empty(2 << 27, dtype=torch.float64, device=dev)
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    time.sleep(0.3)
+    tot = 0.0
+    for _ in range(args.steps):
+        scratch.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        tot += e0.elapsed_time(e1)
+    clocks = clk.stop()
+    ms = replica_max_ms(tot / args.steps, world, dev)
+    value = replica_value(nl, world, ms)
+    f = flags.cpu().numpy()
+    wl["flags"] = {"split": int((f == 1).sum()), "coarse": int((f == 2).sum()),
+                   "no_change": int((f == 0).sum())}
+    # variables evaluated per leaf (the early exit) from single-variable launches
+    per = []
+    for v in var_ids:
+        launch([v])
+        per.append(wmax.cpu().numpy().copy())
+    launch()
+    torch.cuda.synchronize(dev)
+    per = np.maximum.accumulate(np.stack(per), axis=0)
+    passed = per > tol[None, :]
+    nev = np.where(passed.any(axis=0), passed.argmax(axis=0) + 1, len(var_ids))
+    bd = tables["boundary"].astype(bool)
+    flops = float(np.sum(nev[~bd]) * FLOP_WAVELET_INTERIOR + np.sum(nev[bd]) * FLOP_WAVELET_BOUNDARY)
+    fp64_gflops, _ = dgb.measure_fp64_peak()
+    achieved = flops / (ms * 1e-3) / 1e9
+    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
+            "frac": achieved / fp64_gflops, "traffic": None,
+            "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
+            "flop_per_leaf_var": {"interior": FLOP_WAVELET_INTERIOR,
+                                  "boundary": FLOP_WAVELET_BOUNDARY},
+            "vars_evaluated": int(nev.sum()),
+            "hbm_gbs_algorithmic": (int(nev.sum()) * 407 * 8 + nl * 9) / (ms * 1e-3) / 1e9}
+    # all 24 variables, no early exit reached at tol 1e30: the heaviest indicator
+    d_big = torch.full_like(d_tol, 1e30)
+    launch(list(range(24)), d_big)
+    scratch.fill_(1.0)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launch(list(range(24)), d_big)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms24 = e0.elapsed_time(e1)
+    wl["all_24_vars"] = {"ms": ms24, "leaves_per_s": nl / (ms24 * 1e-3),
+                         "gflops": (nl - nb) * 24 * FLOP_WAVELET_INTERIOR / (ms24 * 1e-3) / 1e9
+                         + nb * 24 * FLOP_WAVELET_BOUNDARY / (ms24 * 1e-3) / 1e9}
+    e2e = None
+    if not args.no_e2e:
+        # the reference's entry takes host unzipped vectors: pinned host fields,
+        # H2D of the refinement variables, the indicator, D2H of flags + maxima
+        hu = {v: du[v].cpu().pin_memory() for v in var_ids}
+        hflags = torch.empty(nl, dtype=torch.uint8).pin_memory()
+        hw = torch.empty(nl, dtype=torch.float64).pin_memory()
+        k = max(1, min(args.steps, 5))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(k):
+            for v in var_ids:
+                du[v].copy_(hu[v], non_blocking=True)
+            launch()
+            hflags.copy_(flags, non_blocking=True)
+            hw.copy_(wmax, non_blocking=True)
+            torch.cuda.synchronize(dev)
+        e2e_s = (time.perf_counter() - t0) / k
+        e2e = {"value": nl / e2e_s, "unit": "leaves/s",
+               "h2d_bytes_per_step": len(var_ids) * mesh.nunzipped * 8,
+               "d2h_bytes_per_step": nl * 9, "ms_per_step": e2e_s * 1e3,
+               "path": "unzipped refinement fields in pinned host arrays: H2D, "
+                       "dgb_remesh_wavelets, D2H of flags and maxima every step"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        hv = {v: du[v].cpu().numpy() for v in var_ids}
+        hu = [hv.get(v, hv[var_ids[0]]) for v in range(24)]
+        cpu, _ = cpu_wavelet_baseline(dgb, mesh, hu, var_ids, tables, tol, fac)
+    if rank == 0:
+        print(json.dumps({"metric": metric, "value": value, "unit": "leaves/s",
+                          "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic (seeded Brill-Lindquist + 1e-6 noise)",
+                          "config": wl, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                          "clocks": clocks, "gpu_launches": args.steps, "impl": "ours"}))
+    uz.close()
+    mesh.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 

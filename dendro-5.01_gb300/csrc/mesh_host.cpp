@@ -82,7 +82,8 @@ struct dgb_mesh {
     std::vector<dgb_block_desc> blocks;
     std::vector<int> block_lev;
     std::vector<uint32_t> block_anchor;  // 3 per block (lattice units)
-    std::vector<uint64_t> dof_keys;      // sorted positions of the independent nodes
+    std::vector<uint64_t> dof_keys;      // positions of the independent nodes: sorted while the
+                                         // operators are built, zip-owner order afterwards
     // unzip operator
     std::vector<uint32_t> copy_src;      // per padded point: dof, or 0xFFFFFFFF
     std::vector<uint64_t> interp_dst, interp_ref;
@@ -633,6 +634,57 @@ dgb_status dgb_mesh_unzip_operator(const dgb_mesh *M, uint32_t *copy_src, uint64
     if (src_refs) memcpy(src_refs, M->src_refs.data(), M->src_refs.size() * 8);
     if (level_ptr) memcpy(level_ptr, M->level_ptr.data(), M->level_ptr.size() * 8);
     if (zip_src) memcpy(zip_src, M->zip_src.data(), M->zip_src.size() * 8);
+    return DGB_OK;
+}
+
+dgb_status dgb_mesh_leaf_patches(const dgb_mesh *M, uint64_t *patch_base, uint32_t *block_side,
+                                 uint8_t *boundary, double *corner, double *hx)
+{
+    if (!M) return DGB_ERR_INVALID;
+    // a block of side P*m + 7 holds m^3 leaves of its level; leaf (x, y, z)
+    // of the block starts at padded index P*(x, y, z)
+    for (size_t b = 0; b < M->blocks.size(); b++) {
+        const dgb_block_desc &d = M->blocks[b];
+        const uint32_t side = d.sz[0], m = (side - 7) / P;
+        const int lev = M->block_lev[b];
+        const uint32_t s = M->S(lev);
+        const uint32_t *anc = &M->block_anchor[3 * b];
+        for (uint32_t z = 0; z < m; z++)
+            for (uint32_t y = 0; y < m; y++)
+                for (uint32_t x = 0; x < m; x++) {
+                    const uint32_t a[3] = {anc[0] + x * s, anc[1] + y * s, anc[2] + z * s};
+                    auto it = M->leaf_of.find(key(lev, a[0], a[1], a[2]));
+                    if (it == M->leaf_of.end()) return DGB_ERR_INVALID;
+                    const uint32_t e = it->second;
+                    if (patch_base)
+                        patch_base[e] = d.offset + (uint64_t)P * x +
+                                        (uint64_t)side * ((uint64_t)P * y + (uint64_t)side * P * z);
+                    if (block_side) block_side[e] = side;
+                    bool bdy = false;
+                    for (int q = 0; q < 3; q++) bdy = bdy || a[q] == 0 || a[q] + s == M->N;
+                    if (boundary) boundary[e] = bdy;
+                    if (corner)
+                        for (int q = 0; q < 3; q++)
+                            corner[3 * e + q] = M->prm.domain_min[q] + a[q] * M->unit;
+                    if (hx) hx[e] = M->sp(lev) * M->unit;
+                }
+    }
+    return DGB_OK;
+}
+
+dgb_status dgb_wavelet_tol_radial(const double *corner, uint64_t n, double tol_min, double tol_max,
+                                  double r0, double r1, int use_function, double *tol)
+{
+    if ((n && (!corner || !tol)) || (use_function && r1 == r0)) return DGB_ERR_INVALID;
+    for (uint64_t e = 0; e < n; e++) {
+        if (!use_function) {
+            tol[e] = tol_min;
+            continue;
+        }
+        const double *c = corner + 3 * e;
+        const double r = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        tol[e] = std::min(tol_max, std::max(tol_min, (tol_max - tol_min) / (r1 - r0) * (r - r0) + tol_min));
+    }
     return DGB_OK;
 }
 

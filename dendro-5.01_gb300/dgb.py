@@ -146,6 +146,13 @@ _SIGS = {
     "dgb_mesh_dof_coords": (C.c_int, [C.c_void_p, C.c_void_p]),
     "dgb_mesh_leaf_levels": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "dgb_mesh_unzip_operator": (C.c_int, [C.c_void_p] + [C.c_void_p] * 6),
+    "dgb_mesh_leaf_patches": (C.c_int, [C.c_void_p] + [C.c_void_p] * 5),
+    "dgb_wavelet_tol_radial": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double, C.c_double,
+                                         C.c_double, C.c_double, C.c_int, C.c_void_p]),
+    "dgb_remesh_wavelets": (C.c_int, [PtrArr, C.POINTER(C.c_uint32), C.c_int, C.c_uint64,
+                                      C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]),
     "dgb_unzip_plan_create": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint64,
                                         C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
                                         C.c_uint64, C.c_void_p, C.c_void_p,
@@ -411,6 +418,19 @@ class Mesh:
               "dgb_mesh_leaf_levels")
         return lev, anc
 
+    def leaf_patches(self):
+        """Per leaf: patch_base, block_side, boundary, corner (n x 3), hx."""
+        n = self.num_leaves
+        pb = np.zeros(n, dtype=np.uint64)
+        bs = np.zeros(n, dtype=np.uint32)
+        bd = np.zeros(n, dtype=np.uint8)
+        cr = np.zeros((n, 3))
+        hx = np.zeros(n)
+        check(lib().dgb_mesh_leaf_patches(self.h, pb.ctypes.data, bs.ctypes.data, bd.ctypes.data,
+                                          cr.ctypes.data, hx.ctypes.data),
+              "dgb_mesh_leaf_patches")
+        return {"patch_base": pb, "block_side": bs, "boundary": bd, "corner": cr, "hx": hx}
+
     def operator(self):
         cp = np.zeros(self.nunzipped, dtype=np.uint32)
         idst = np.zeros(self.ninterp, dtype=np.uint64)
@@ -437,6 +457,35 @@ class Mesh:
 
 
 SENTINEL = 0xFFFFFFFF
+
+# ----------------------------------------------------------------------------- remesh indicator
+OCT_NO_CHANGE, OCT_SPLIT, OCT_COARSE, OCT_INVALID = 0, 1, 2, 255
+WAVELET_MAX_VARS = 32
+
+
+def wavelet_tol_radial(corner, tol_min, tol_max=None, r0=0.0, r1=1.0, use_function=False):
+    """Per-leaf wavelet tolerance (bssn::computeWTol's radial ramp)."""
+    corner = np.ascontiguousarray(corner, dtype=np.float64).reshape(-1, 3)
+    tol = np.zeros(len(corner))
+    check(lib().dgb_wavelet_tol_radial(corner.ctypes.data, len(corner), tol_min,
+                                       tol_min if tol_max is None else tol_max, r0, r1,
+                                       1 if use_function else 0, tol.ctypes.data),
+          "dgb_wavelet_tol_radial")
+    return tol
+
+
+def remesh_wavelets(unzipped_ptrs, var_ids, unzip_len, nleaves, patch_base_ptr, block_side_ptr,
+                    boundary_ptr, tol_ptr, coarse_fac, wmax_ptr, flags_ptr, changed_ptr=None,
+                    stream=0):
+    """Mesh::isReMeshUnzip's indicator on device arrays (see dgb_remesh_wavelets)."""
+    u, keep = ptr_array(unzipped_ptrs)
+    vid = (C.c_uint32 * len(var_ids))(*var_ids)
+    check(lib().dgb_remesh_wavelets(u, vid, len(var_ids), unzip_len, nleaves,
+                                    C.c_void_p(patch_base_ptr), C.c_void_p(block_side_ptr),
+                                    C.c_void_p(boundary_ptr), C.c_void_p(tol_ptr), coarse_fac,
+                                    C.c_void_p(wmax_ptr), C.c_void_p(flags_ptr),
+                                    C.c_void_p(changed_ptr), C.c_void_p(stream)),
+          "dgb_remesh_wavelets")
 
 
 def synth_fill_points(xyz, fields, seed, noise=1e-6, nthreads=0):

@@ -247,6 +247,51 @@ dgb_status dgb_mesh_leaf_levels(const dgb_mesh *mesh, uint8_t *level, uint32_t *
 dgb_status dgb_mesh_unzip_operator(const dgb_mesh *mesh, uint32_t *copy_src, uint64_t *interp_dst,
                                    uint64_t *interp_ref, uint64_t *src_refs, uint64_t *level_ptr,
                                    uint64_t *zip_src);
+/* Per leaf of the mesh (dgb_mesh_sizes()[0] entries each; any pointer may be
+ * NULL): patch_base = first point of the leaf's 13^3 padded patch in the
+ * unzipped vector (its 7^3 nodes and 3 padding points per side,
+ * Mesh::getUnzipElementalNodalValues, include/mesh.tcc:9136-9176);
+ * block_side = side of its block's padded grid; boundary = 1 when the leaf
+ * touches the domain boundary (Mesh::isBoundaryOctant, include/mesh.h:1482-1486);
+ * corner = its minimum corner (3 per leaf) and hx = its node spacing, domain
+ * units: the arguments isReMeshUnzip passes its wavelet_tol callback
+ * (include/mesh.tcc:2090-2099). */
+dgb_status dgb_mesh_leaf_patches(const dgb_mesh *mesh, uint64_t *patch_base, uint32_t *block_side,
+                                 uint8_t *boundary, double *corner, double *hx);
+
+/* ---- wavelet refinement indicator (Mesh::isReMeshUnzip) ---------------- */
+/* Refinement flags (OCT_NO_CHANGE, OCT_SPLIT, OCT_COARSE, include/mesh.h:108-110) */
+#define DGB_OCT_NO_CHANGE 0u
+#define DGB_OCT_SPLIT 1u
+#define DGB_OCT_COARSE 2u
+#define DGB_OCT_INVALID 255u /* leaf patch outside the unzipped vector */
+#define DGB_WAVELET_MAX_VARS 32
+
+/* Wavelet tolerance per leaf from its corner (host arrays): the radial ramp
+ * of bssn::computeWTol (BSSN_GR/src/grUtils.cpp:1869-1891),
+ * min(tol_max, max(tol_min, (tol_max - tol_min) / (r1 - r0) * (r - r0) + tol_min))
+ * with r = |corner| in domain coordinates when use_function, else tol_min. */
+dgb_status dgb_wavelet_tol_radial(const double *corner, uint64_t nleaves, double tol_min,
+                                  double tol_max, double r0, double r1, int use_function,
+                                  double *tol);
+
+/* Replaces the indicator of Mesh::isReMeshUnzip (include/mesh.tcc:2035-2197;
+ * wavelets of WaveletEl::compute_wavelets_3D, src/waveletRefEl.cpp:92-271),
+ * element order 6.  unzipped: host array of device pointers (all fields of
+ * unzip_len points), var_ids: host array of nvars (1..DGB_WAVELET_MAX_VARS)
+ * refinement variables.  Per leaf (device arrays of nleaves, as
+ * dgb_mesh_leaf_patches gives them, tol from the wavelet_tol callback):
+ * wmax = the largest RMS wavelet over the variables, stopping at the first
+ * variable that passes tol (eleWMax); flags = DGB_OCT_SPLIT if wmax > tol,
+ * DGB_OCT_COARSE if wmax < coarse_fac * tol, else DGB_OCT_NO_CHANGE;
+ * DGB_OCT_INVALID (wmax NaN) for a leaf whose patch does not fit.  changed
+ * (device, may be NULL): number of leaves flagged split or coarse, the
+ * reference's isMeshLocalChanged.  Asynchronous on stream. */
+dgb_status dgb_remesh_wavelets(const double *const *unzipped, const uint32_t *var_ids, int nvars,
+                               uint64_t unzip_len, uint64_t nleaves, const uint64_t *patch_base,
+                               const uint32_t *block_side, const uint8_t *boundary,
+                               const double *tol, double coarse_fac, double *wmax, uint8_t *flags,
+                               unsigned long long *changed, void *stream);
 
 /* Device unzip / zip for any mesh, from its operator.  A node reference is
  * a 64-bit word: bit 63 clear = the zipped node in the low 32 bits; bit 63

@@ -76,6 +76,14 @@ class Oracle:
                                          C.c_int, C.c_int]
         L.orc_ccz4_adv42.restype = None
         L.orc_ccz4_adv42.argtypes = [C.c_int, _D, _D, C.c_double, C.POINTER(C.c_uint), _D, C.c_uint]
+        L.orc_wavelet_patch.restype = None
+        L.orc_wavelet_patch.argtypes = [_D, C.c_int, _D]
+        L.orc_wavelet_rms.restype = C.c_double
+        L.orc_wavelet_rms.argtypes = [_D]
+        L.orc_remesh_wavelets.restype = C.c_uint64
+        L.orc_remesh_wavelets.argtypes = [_PP, C.POINTER(C.c_uint32), C.c_int, C.c_uint64,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_double, C.c_void_p, C.c_void_p, C.c_int]
         for nm in ("orc_deriv64", "orc_deriv64_2", "orc_ko42", "orc_deriv42", "orc_deriv42_2",
                    "orc_ccz4_ko42"):
             f = getattr(L, nm)
@@ -156,6 +164,33 @@ class Oracle:
         uu, k2 = _ptrs(u)
         return self.L.orc_physcon_blocks(c, uu, n, off, sz, bf, pmin.ctypes.data_as(_D),
                                          pmax.ctypes.data_as(_D), nthreads)
+
+    def wavelet_patch(self, patch, boundary):
+        """compute_wavelets_3D on one 13^3 patch (x fastest): the 64 wavelet
+        slots and their RMS."""
+        p = np.ascontiguousarray(patch, dtype=np.float64).reshape(-1)
+        assert p.size == 13 ** 3
+        wc = np.zeros(64)
+        self.L.orc_wavelet_patch(p.ctypes.data_as(_D), 1 if boundary else 0, wc.ctypes.data_as(_D))
+        return wc, self.L.orc_wavelet_rms(wc.ctypes.data_as(_D))
+
+    def remesh_wavelets(self, unzipped, var_ids, patch_base, block_side, boundary, tol,
+                        coarse_fac, nthreads=0):
+        """isReMeshUnzip's indicator over a leaf list: (wmax, flags, changed)."""
+        n = len(patch_base)
+        pb = np.ascontiguousarray(patch_base, dtype=np.uint64)
+        bs = np.ascontiguousarray(block_side, dtype=np.uint32)
+        bd = np.ascontiguousarray(boundary, dtype=np.uint8)
+        tl = np.ascontiguousarray(tol, dtype=np.float64)
+        wmax = np.zeros(n)
+        flags = np.zeros(n, dtype=np.uint8)
+        uu, k1 = _ptrs(unzipped)
+        vid = (C.c_uint32 * len(var_ids))(*var_ids)
+        changed = self.L.orc_remesh_wavelets(uu, vid, len(var_ids), n, pb.ctypes.data,
+                                             bs.ctypes.data, bd.ctypes.data, tl.ctypes.data,
+                                             coarse_fac, wmax.ctypes.data, flags.ctypes.data,
+                                             nthreads or os.cpu_count())
+        return wmax, flags, int(changed)
 
     def bssnrhs_block(self, rhs, u, block, prm, apply_bcs=True):
         r, k1 = _ptrs(rhs)
