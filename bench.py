@@ -250,6 +250,8 @@ def main():
                     help="use only the first N blocks of the batch (profiling captures)")
     ap.add_argument("--octree-level", type=int, default=10,
                     help="wavelet_octree: finest octree level (smaller cases for captures)")
+    ap.add_argument("--fused", action="store_true",
+                    help="octree_rk4: the fused unzip -> RHS stepper (no unzipped field set)")
     ap.add_argument("--no-all-vars", action="store_true",
                     help="wavelet_octree: skip the 24-variable measurement (unzip only the "
                          "refinement variables)")
@@ -702,7 +704,10 @@ def main_octree(args, dgb, rank, world, local):
         del tu, tr
         torch.cuda.empty_cache()
     uz = dgb.UnzipPlan(op, mesh.ndof)
-    st = dgb.Stepper(plan, uz, prec)
+    st = dgb.Stepper(plan, uz, prec, fused=args.fused)
+    wl["stepper"] = ("fused unzip -> RHS (gather from the zipped state, no unzipped set)"
+                     if args.fused else "unzip -> RHS -> zip")
+    wl["stepper_device_gb"] = round(st.device_bytes / 1e9, 3)
     xyz = mesh.dof_coords()
     host = [np.empty(mesh.ndof) for _ in range(24)]
     dgb.synth_fill_points(xyz, host, seed, 1e-6)
@@ -755,7 +760,9 @@ def main_octree(args, dgb, rank, world, local):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu, _ = cpu_rk4_baseline(dgb, seed, sigma)
-    launches_per_step = 4 * (mesh.nlevels + 2 + 1 + 1 + 1)
+    # per stage: one source fill per level, interpolation, RHS, zip, update (+ the
+    # copy of the unzip when unfused)
+    launches_per_step = 4 * (mesh.nlevels + (3 if args.fused else 5))
     if rank == 0:
         print(json.dumps({"metric": METRIC, "value": value, "unit": "grid-pts*vars/s",
                           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

@@ -52,6 +52,7 @@ struct dgb_plan {
     double *d_scratch = nullptr;
     size_t scratch_doubles = 0;
     int occupancy[8][2] = {};  // resident CTAs per SM per (variant, precision)
+    int occupancy_g[8][2] = {};  // the same for the gather-mode kernels (0 = not yet known)
     int pc_occupancy = 0;      // constraint kernel, resident CTAs per SM (0 = not yet known)
     // CCZ4 kernel: its own workspace (241 slots per point), allocated at first use
     int c4_occupancy[2] = {0, 0};  // per precision
@@ -189,7 +190,7 @@ dgb_status run_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int 
     if (s != DGB_OK) return s;
     if (p->nitems[variant] == 0) return DGB_OK;
     DGB_CUDA(rhs_configure(variant, precision));
-    RhsArgs a;
+    RhsArgs a{};
     for (int v = 0; v < NV; v++) {
         a.u[v] = u[v];
         a.rhs[v] = rhs[v];
@@ -207,6 +208,49 @@ dgb_status run_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int 
 }
 
 }  // namespace
+
+dgb_status dgb::run_rhs_gather(dgb_plan *p, double *const *k, const double *const *z,
+                               const double *const *ib, const uint32_t *gmap, const uint32_t *zmap,
+                               uint32_t ndof, int precision, cudaStream_t st)
+{
+    if (precision != DGB_PREC_FP64 && precision != DGB_PREC_MIXED) {
+        set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
+        return DGB_ERR_INVALID;
+    }
+    const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
+    const int variant = p->variant[prec];
+    dgb_status s = build_items(p, variant);
+    if (s != DGB_OK) return s;
+    if (p->nitems[variant] == 0) return DGB_OK;
+    if (p->occupancy_g[variant][prec] == 0) {
+        // the workspace is sized for the plain kernels' residency: never exceed it
+        const int occ = rhs_max_ctas_per_sm_gather(variant, precision);
+        if (occ < 1) {
+            set_error("gather-mode RHS kernel cannot be resident");
+            return DGB_ERR_CUDA;
+        }
+        p->occupancy_g[variant][prec] = std::min(occ, p->occupancy[variant][prec]);
+    }
+    RhsArgs a{};
+    for (int v = 0; v < NV; v++) {
+        a.u[v] = z[v];
+        a.rhs[v] = k[v];
+        a.ib[v] = ib[v];
+    }
+    a.gmap = gmap;
+    a.zmap = zmap;
+    a.ndof = ndof;
+    a.blocks = p->d_blocks;
+    a.items = p->d_items[variant];
+    a.nitems = p->nitems[variant];
+    a.queue = p->d_queue;
+    a.scratch = p->d_scratch;
+    a.prm = rhs_params(p->prm);
+    const int grid = p->nsm * p->occupancy_g[variant][prec];
+    DGB_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned int), st));
+    DGB_CUDA(rhs_launch_gather(variant, precision, a, grid, st));
+    return DGB_OK;
+}
 
 extern "C" {
 

@@ -45,6 +45,14 @@ struct RhsArgs {
     unsigned int *queue;   // work-queue head, zeroed before each launch
     double *scratch;       // per-CTA derivative workspace
     RhsParams prm;
+    // gather mode (fused unzip) only: u = zipped fields, rhs = zipped outputs;
+    // padded point gi reads u[v][gmap[gi]] when gmap[gi] < ndof, else
+    // ib[v][gmap[gi] - ndof] (interpolated points); its RHS goes to
+    // rhs[v][zmap[gi]] unless zmap[gi] = 0xFFFFFFFF (not the node's owner)
+    const double *ib[NV];
+    const uint32_t *gmap;
+    const uint32_t *zmap;
+    uint32_t ndof;
 };
 
 // Tile schedule: one compiled kernel variant per max tile shape.
@@ -62,6 +70,14 @@ size_t rhs_scratch_per_cta(int variant);  // doubles
 cudaError_t rhs_launch(int variant, int precision, const RhsArgs &args, int grid,
                        cudaStream_t stream);
 cudaError_t rhs_configure(int variant, int precision);
+// the gather-mode (fused unzip) kernels, same variants
+cudaError_t rhs_launch_gather(int variant, int precision, const RhsArgs &args, int grid,
+                              cudaStream_t stream);
+int rhs_max_ctas_per_sm_gather(int variant, int precision);
+// the gather-mode RHS over a plan (dgb_api.cu)
+dgb_status run_rhs_gather(dgb_plan *p, double *const *k, const double *const *z,
+                          const double *const *ib, const uint32_t *gmap, const uint32_t *zmap,
+                          uint32_t ndof, int precision, cudaStream_t st);
 int rhs_max_ctas_per_sm(int variant, int precision);
 
 cudaError_t rk4_launch(int stage, double *const *dst, const double *const *prev,

@@ -247,6 +247,29 @@ struct AlgIOw {
     }
 };
 
+// Gather mode (fused unzip): the fields are the zipped state and the
+// interpolated-point buffer, read through the padded point's gather index;
+// the RHS at a padded point goes to its zipped node when the point owns it.
+__device__ __forceinline__ const double *gather_src(const RhsArgs &a, int v, uint32_t g)
+{
+    return g < a.ndof ? a.u[v] + g : a.ib[v] + (g - a.ndof);
+}
+
+struct AlgIOg {
+    const RhsArgs *a;
+    const double *S;
+    int pmax, p;
+    uint32_t g, o;  // gather index and owned zipped node (0xFFFFFFFF: none) of the point
+    double sigma;
+    __device__ __forceinline__ double u(int v) const { return __ldg(gather_src(*a, v, g)); }
+    __device__ __forceinline__ double d(int s) const { return S[(size_t)s * pmax + p]; }
+    __device__ __forceinline__ void out(int v, double x) const
+    {
+        const double r = __dadd_rn(x, __dmul_rn(sigma, S[(size_t)(DGB_NUM_DERIV + v) * pmax + p]));
+        if (o != 0xFFFFFFFFu) a->rhs[v][o] = r;
+    }
+};
+
 struct AlgPrm {
     double l1, l2, l3, l4, lf0, lf1;
 };
@@ -260,19 +283,21 @@ struct Geo {
     static constexpr int PMAX = TX * TY * TZ;
 };
 
-template <int TX, int TY, int TZ, bool MIXED>
+template <int TX, int TY, int TZ, bool MIXED, bool GATHER = false>
 struct Smem {
     using G = Geo<TX, TY, TZ>;
     // FP64: two field buffers + d_x box + d_y box (doubles)
     // MIXED: two field buffers (doubles) + hi/lo float planes + float-pair boxes
-    static constexpr size_t bytes = MIXED
+    // GATHER: + the staged region's gather indices (uint32)
+    static constexpr size_t base = MIXED
         ? (2 * G::FBUF * 8 + 2 * G::FBUF * 4 + 2 * (G::DXB + G::DYB) * 4)
         : (2 * G::FBUF * 8 + (G::DXB + G::DYB) * 8);
+    static constexpr size_t bytes = base + (GATHER ? G::FBUF * 4 : 0);
 };
 
 // One work item (a tile of one block): phase D then phase A.  S is this
 // CTA's slice of the derivative workspace.
-template <int TX, int TY, int TZ, bool MIXED>
+template <int TX, int TY, int TZ, bool MIXED, bool GATHER = false>
 __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                                          const DevBlock &blk, double *S, const AlgPrm &aprm)
 {
@@ -317,11 +342,25 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
         ax[2] = axis_scale(hz);
     }
 
-    auto issue_load = [&](int v, double *dst) {
-        const double *src = args.u[v] + rbase;
+    // gather mode: the staged region's gather indices, loaded once per item
+    uint32_t *gidx = reinterpret_cast<uint32_t *>(smem_raw + Smem<TX, TY, TZ, MIXED>::base);
+    if (GATHER) {
+        const uint32_t *gm = args.gmap + rbase;
         for (int q = tid; q < npad; q += kThreads) {
             const int i = q % px, r = q / px, j = r % py, k = r / py;
-            cp_async8(dst + q, src + i + (uint64_t)nx * (j + (uint64_t)ny * k));
+            gidx[q] = __ldg(gm + i + (uint64_t)nx * (j + (uint64_t)ny * k));
+        }
+        __syncthreads();
+    }
+    auto issue_load = [&](int v, double *dst) {
+        if (GATHER) {
+            for (int q = tid; q < npad; q += kThreads) cp_async8(dst + q, gather_src(args, v, gidx[q]));
+        } else {
+            const double *src = args.u[v] + rbase;
+            for (int q = tid; q < npad; q += kThreads) {
+                const int i = q % px, r = q / px, j = r % py, k = r / py;
+                cp_async8(dst + q, src + i + (uint64_t)nx * (j + (uint64_t)ny * k));
+            }
         }
         cp_async_commit();
     };
@@ -582,14 +621,20 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
             // rhs = -(1/r)(x f_x + y f_y + z f_z + falloff (f - asymptotic)),
             // replacing the algebra at this point, then + sigma * KO as elsewhere
             const double ninv_r = -__ddiv_rn(1.0, __dsqrt_rn(r2));
+            const uint32_t gg = GATHER ? __ldg(args.gmap + gi) : 0u;
+            const uint32_t go = GATHER ? __ldg(args.zmap + gi) : 0u;
             for (int v = 0; v < NV; v++) {
-                const double f = __ldg(args.u[v] + gi);
+                const double f = GATHER ? __ldg(gather_src(args, v, gg)) : __ldg(args.u[v] + gi);
                 const double *g = S + (size_t)(3 * v) * G::PMAX + p;
                 double t = __dadd_rn(__dmul_rn(x, g[0]), __dmul_rn(y, g[G::PMAX]));
                 t = __dadd_rn(t, __dmul_rn(z, g[2 * G::PMAX]));
                 t = __dadd_rn(t, __dmul_rn(c_bc_falloff[v], __dsub_rn(f, c_bc_asym[v])));
                 const double ko_sum = S[(size_t)(DGB_NUM_DERIV + v) * G::PMAX + p];
-                args.rhs[v][gi] = __dadd_rn(__dmul_rn(ninv_r, t), __dmul_rn(args.prm.sigma, ko_sum));
+                const double out = __dadd_rn(__dmul_rn(ninv_r, t), __dmul_rn(args.prm.sigma, ko_sum));
+                if (!GATHER)
+                    args.rhs[v][gi] = out;
+                else if (go != 0xFFFFFFFFu)
+                    args.rhs[v][go] = out;
             }
             continue;
         }
@@ -599,8 +644,14 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
             const double q = args.prm.eta_r0 / rr;
             eta *= (args.prm.eta_exp == 1.0) ? q : pow(q, args.prm.eta_exp);
         }
-        AlgIOw io{args.u, args.rhs, S, G::PMAX, p, gi, args.prm.sigma};
-        dgb_bssn_algebra(io, aprm, eta);
+        if (GATHER) {
+            AlgIOg io{&args, S, G::PMAX, p, __ldg(args.gmap + gi), __ldg(args.zmap + gi),
+                      args.prm.sigma};
+            dgb_bssn_algebra(io, aprm, eta);
+        } else {
+            AlgIOw io{args.u, args.rhs, S, G::PMAX, p, gi, args.prm.sigma};
+            dgb_bssn_algebra(io, aprm, eta);
+        }
     }
 }
 

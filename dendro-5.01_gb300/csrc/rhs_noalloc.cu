@@ -143,7 +143,7 @@ extern "C" dgb_status dgb_bssnrhs_block_noalloc(double *const *rhs, const double
     double *ws = nullptr;
     dgb_status s = workspace_on_current_device(&ws);
     if (s != DGB_OK) return s;
-    RhsArgs a;
+    RhsArgs a{};
     for (int v = 0; v < NV; v++) {
         a.u[v] = u[v];
         a.rhs[v] = rhs[v];

@@ -12,6 +12,14 @@
 // zip: one gather per independent node.  All HBM/L2-bound; the RK4 step
 // around them is  for s in 0..3: unzip(prev or im) -> bssnRHS -> zip ->
 // stage update  (BSSN_GR/src/rkBSSN.cpp:803-1012), captured once and replayed.
+//
+// Fused mode (DGB_STEP_FUSED_UNZIP): no unzipped field set.  Per stage only
+// the source elements (1) and the interpolated points (3, into a compact
+// buffer, one row per interpolated padded point) are materialised; the RHS
+// kernel stages its tiles from the zipped state and that buffer through a
+// per-padded-point gather index and writes each RHS value straight to the
+// zipped node its padded point owns (the zip), so steps 2 and the zip
+// disappear, and with them 2 x 24 x 8 bytes per padded point of device memory.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -133,6 +141,7 @@ struct GroupArgs {
     const uint16_t *gcode;  // cx + 13 * (cy + 13 * cz)
     uint64_t nsrc;
     LagTable T;
+    bool compact;           // write row r to out[v][r] (fused mode) instead of out[v][gdst[r]]
 };
 
 __device__ __forceinline__ double pass1(const double *in, int code, int stride, const LagTable &T)
@@ -174,7 +183,7 @@ __global__ void __launch_bounds__(256) unzip_group_kernel(const GroupArgs a)
             }
             __syncthreads();
             for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
-                a.f.out[v][a.gdst[r]] = Cc[a.gcode[r]];
+                a.f.out[v][a.compact ? r : a.gdst[r]] = Cc[a.gcode[r]];
         }
     }
 }
@@ -193,6 +202,35 @@ __global__ void __launch_bounds__(256) zip_kernel(const FieldPtrs f, const uint6
         for (int v = 0; v < NV; v++)
             if (v < f.nvars) f.out[v][d] = val[v];
     }
+}
+
+// Fused mode's maps.  gmap[p]: the zipped node a padded point copies, or
+// ndof + r for the r-th interpolated row (grouped order), or ndof + ninterp
+// (a zero row) for points beyond the domain faces; zmap[p]: the zipped node
+// whose value is read from padded point p by the zip, or kSentinel.
+__global__ void gmap_copy_kernel(uint32_t *gmap, const uint32_t *__restrict__ copy, uint64_t n,
+                                 uint32_t outside)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += stride) {
+        const uint32_t c = copy[p];
+        gmap[p] = c == kSentinel ? outside : c;
+    }
+}
+
+__global__ void gmap_interp_kernel(uint32_t *gmap, const uint64_t *__restrict__ gdst, uint64_t n,
+                                   uint32_t ndof)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += stride)
+        gmap[gdst[r]] = ndof + (uint32_t)r;
+}
+
+__global__ void zmap_kernel(uint32_t *zmap, const uint64_t *__restrict__ zip, uint64_t n)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t d = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; d < n; d += stride)
+        zmap[zip[d]] = (uint32_t)d;
 }
 
 unsigned grid_for(uint64_t n, int threads)
@@ -247,7 +285,11 @@ struct dgb_stepper {
     dgb_plan *plan = nullptr;
     dgb_unzip_plan *uz = nullptr;
     int precision = 0;
+    bool fused = false;
     double *d_U = nullptr, *d_R = nullptr, *d_k = nullptr, *d_im = nullptr;
+    uint32_t *d_gmap = nullptr, *d_zmap = nullptr;  // fused mode
+    double *d_ib = nullptr;                         // fused mode: NV x (ninterp + 1)
+    uint64_t device_bytes = 0;
     unsigned int *d_status = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -267,28 +309,61 @@ namespace {
         }                                                                                    \
     } while (0)
 
+// step 1: the source elements' nodal values, coarsest level first
+dgb_status fill_sources(dgb_unzip_plan *p, const double *const *zipped, int nvars, cudaStream_t st)
+{
+    if (!p->nsrc) return DGB_OK;
+    DgArgs a;
+    for (int v = 0; v < NV; v++) {
+        a.z[v] = v < nvars ? zipped[v] : nullptr;
+        a.dg[v] = p->d_dg + (size_t)v * p->nsrc * kNpe;
+    }
+    a.nvars = nvars;
+    a.refs = p->d_srefs;
+    a.T = p->T;
+    for (size_t l = 0; l + 1 < p->level_ptr.size(); l++) {
+        a.first = p->level_ptr[l];
+        a.count = p->level_ptr[l + 1] - p->level_ptr[l];
+        if (!a.count) continue;
+        dg_fill_kernel<<<grid_for(a.count * kNpe, 256), 256, 0, st>>>(a);
+        DGB_CUDA(cudaGetLastError());
+    }
+    return DGB_OK;
+}
+
+// step 3: the interpolated padded points, to their padded positions or (compact)
+// to rows 0..ninterp-1 of out in grouped order
+dgb_status interp_rows(dgb_unzip_plan *p, double *const *out, int nvars, bool compact,
+                       cudaStream_t st)
+{
+    if (!p->ninterp) return DGB_OK;
+    GroupArgs a;
+    a.f.nvars = nvars;
+    for (int v = 0; v < NV; v++) {
+        a.f.in[v] = nullptr;
+        a.f.out[v] = v < nvars ? out[v] : nullptr;
+        a.dg[v] = p->d_dg + (size_t)v * p->nsrc * kNpe;
+    }
+    a.gptr = p->d_gptr;
+    a.gdst = p->d_gdst;
+    a.gcode = p->d_gcode;
+    a.nsrc = p->nsrc;
+    a.T = p->T;
+    a.compact = compact;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t grid = p->nsrc < (uint64_t)nsm * 8 ? p->nsrc : (uint64_t)nsm * 8;
+    unzip_group_kernel<<<(unsigned)grid, 256, 0, st>>>(a);
+    DGB_CUDA(cudaGetLastError());
+    return DGB_OK;
+}
+
 dgb_status do_unzip(dgb_unzip_plan *p, const double *const *zipped, double *const *unzipped,
                     int nvars, cudaStream_t st)
 {
-    double *dg[NV];
-    for (int v = 0; v < NV; v++) dg[v] = p->d_dg + (size_t)v * p->nsrc * kNpe;
-    if (p->nsrc) {
-        DgArgs a;
-        for (int v = 0; v < NV; v++) {
-            a.z[v] = v < nvars ? zipped[v] : nullptr;
-            a.dg[v] = dg[v];
-        }
-        a.nvars = nvars;
-        a.refs = p->d_srefs;
-        a.T = p->T;
-        for (size_t l = 0; l + 1 < p->level_ptr.size(); l++) {
-            a.first = p->level_ptr[l];
-            a.count = p->level_ptr[l + 1] - p->level_ptr[l];
-            if (!a.count) continue;
-            dg_fill_kernel<<<grid_for(a.count * kNpe, 256), 256, 0, st>>>(a);
-            DGB_CUDA(cudaGetLastError());
-        }
-    }
+    dgb_status r = fill_sources(p, zipped, nvars, st);
+    if (r != DGB_OK) return r;
     FieldPtrs f;
     f.nvars = nvars;
     for (int v = 0; v < NV; v++) {
@@ -299,23 +374,7 @@ dgb_status do_unzip(dgb_unzip_plan *p, const double *const *zipped, double *cons
         unzip_copy_kernel<<<grid_for(p->nunz, 256), 256, 0, st>>>(f, p->d_copy, p->nunz);
         DGB_CUDA(cudaGetLastError());
     }
-    if (p->ninterp) {
-        GroupArgs a;
-        a.f = f;
-        for (int v = 0; v < NV; v++) a.dg[v] = dg[v];
-        a.gptr = p->d_gptr;
-        a.gdst = p->d_gdst;
-        a.gcode = p->d_gcode;
-        a.nsrc = p->nsrc;
-        a.T = p->T;
-        int dev = 0, nsm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        const uint64_t grid = p->nsrc < (uint64_t)nsm * 8 ? p->nsrc : (uint64_t)nsm * 8;
-        unzip_group_kernel<<<(unsigned)grid, 256, 0, st>>>(a);
-        DGB_CUDA(cudaGetLastError());
-    }
-    return DGB_OK;
+    return interp_rows(p, unzipped, nvars, false, st);
 }
 
 dgb_status do_zip(dgb_unzip_plan *p, const double *const *unzipped, double *const *zipped,
@@ -342,21 +401,33 @@ dgb_status enqueue_step(dgb_stepper *s, double *const *state, double dt, double 
     double *U[NV], *R[NV], *IM[NV];
     const double *K[4 * NV];
     for (int v = 0; v < NV; v++) {
-        U[v] = s->d_U + (size_t)v * nu;
-        R[v] = s->d_R + (size_t)v * nu;
+        U[v] = s->d_U ? s->d_U + (size_t)v * nu : nullptr;
+        R[v] = s->d_R ? s->d_R + (size_t)v * nu : nullptr;
         IM[v] = s->d_im + (size_t)v * nd;
         for (int q = 0; q < 4; q++) K[q * NV + v] = s->d_k + ((size_t)q * NV + v) * nd;
     }
+    double *IB[NV];
+    const uint64_t nib = s->uz->ninterp + 1;
+    for (int v = 0; v < NV; v++) IB[v] = s->d_ib ? s->d_ib + (size_t)v * nib : nullptr;
     for (int stage = 0; stage < 4; stage++) {
         const double *const *src = stage == 0 ? (const double *const *)state : (const double *const *)IM;
-        dgb_status r = do_unzip(s->uz, src, U, NV, st);
-        if (r != DGB_OK) return r;
-        r = dgb_bssn_rhs(s->plan, R, U, s->precision, st);
-        if (r != DGB_OK) return r;
         double *KS[NV];
         for (int v = 0; v < NV; v++) KS[v] = (double *)K[stage * NV + v];
-        r = do_zip(s->uz, R, KS, NV, st);
-        if (r != DGB_OK) return r;
+        if (s->fused) {
+            dgb_status r = fill_sources(s->uz, src, NV, st);
+            if (r == DGB_OK) r = interp_rows(s->uz, IB, NV, true, st);
+            if (r == DGB_OK)
+                r = run_rhs_gather(s->plan, KS, src, (const double *const *)IB, s->d_gmap,
+                                   s->d_zmap, (uint32_t)nd, s->precision, st);
+            if (r != DGB_OK) return r;
+        } else {
+            dgb_status r = do_unzip(s->uz, src, U, NV, st);
+            if (r != DGB_OK) return r;
+            r = dgb_bssn_rhs(s->plan, R, U, s->precision, st);
+            if (r != DGB_OK) return r;
+            r = do_zip(s->uz, R, KS, NV, st);
+            if (r != DGB_OK) return r;
+        }
         DGB_CUDA(rk4_launch(stage, stage < 3 ? IM : state, (const double *const *)state, K, nd, dt,
                             chi_floor, s->d_status, st));
     }
@@ -511,39 +582,84 @@ dgb_status dgb_stepper_destroy(dgb_stepper *s)
     cudaFree(s->d_R);
     cudaFree(s->d_k);
     cudaFree(s->d_im);
+    cudaFree(s->d_gmap);
+    cudaFree(s->d_zmap);
+    cudaFree(s->d_ib);
     cudaFree(s->d_status);
     delete s;
     return DGB_OK;
 }
 
-dgb_status dgb_stepper_create(dgb_plan *rhs_plan, dgb_unzip_plan *uz, int precision,
-                              dgb_stepper **out)
+dgb_status dgb_stepper_create_ex(dgb_plan *rhs_plan, dgb_unzip_plan *uz, int precision,
+                                 unsigned flags, dgb_stepper **out)
 {
     if (!rhs_plan || !uz || !out) {
         set_error("dgb_stepper_create: null argument");
+        return DGB_ERR_INVALID;
+    }
+    if (flags & ~(unsigned)DGB_STEP_FUSED_UNZIP) {
+        set_error("dgb_stepper_create: unknown flags");
         return DGB_ERR_INVALID;
     }
     if (dgb_plan_unzipped_size(rhs_plan) != uz->nunz) {
         set_error("dgb_stepper_create: the RHS plan and the unzip plan disagree on the unzipped size");
         return DGB_ERR_INVALID;
     }
+    const bool fused = (flags & DGB_STEP_FUSED_UNZIP) != 0;
+    const size_t nu = uz->nunz, nd = uz->ndof, nib = uz->ninterp + 1;
+    if (fused && nd + nib >= kSentinel) {
+        set_error("dgb_stepper_create: too many nodes for 32-bit gather indices");
+        return DGB_ERR_INVALID;
+    }
     dgb_stepper *s = new dgb_stepper();
     s->plan = rhs_plan;
     s->uz = uz;
     s->precision = precision;
-    const size_t nu = uz->nunz, nd = uz->ndof;
-    cudaError_t e = cudaMalloc(&s->d_U, (size_t)NV * nu * 8);
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_R, (size_t)NV * nu * 8);
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_k, (size_t)4 * NV * nd * 8);
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_im, (size_t)NV * nd * 8);
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_status, sizeof(unsigned int));
-    // padding beyond domain faces is never written by unzip: keep it finite
-    if (e == cudaSuccess) e = cudaMemset(s->d_U, 0, (size_t)NV * nu * 8);
-    if (e == cudaSuccess) e = cudaMemset(s->d_R, 0, (size_t)NV * nu * 8);
-    if (e == cudaSuccess) e = cudaMemset(s->d_status, 0, sizeof(unsigned int));
+    s->fused = fused;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](void **p, size_t bytes) {
+        if (e != cudaSuccess) return;
+        e = cudaMalloc(p, bytes);
+        if (e == cudaSuccess) s->device_bytes += bytes;
+    };
+    if (!fused) {
+        alloc((void **)&s->d_U, (size_t)NV * nu * 8);
+        alloc((void **)&s->d_R, (size_t)NV * nu * 8);
+    } else {
+        alloc((void **)&s->d_gmap, nu * 4);
+        alloc((void **)&s->d_zmap, nu * 4);
+        alloc((void **)&s->d_ib, (size_t)NV * nib * 8);
+    }
+    alloc((void **)&s->d_k, (size_t)4 * NV * nd * 8);
+    alloc((void **)&s->d_im, (size_t)NV * nd * 8);
+    alloc((void **)&s->d_status, sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_out, cudaEventDisableTiming);
+    // padding beyond domain faces is never written by unzip: keep it finite
+    // (fused mode: the zero row the gather index of such points names)
+    if (e == cudaSuccess && !fused) e = cudaMemsetAsync(s->d_U, 0, (size_t)NV * nu * 8, s->st);
+    if (e == cudaSuccess && !fused) e = cudaMemsetAsync(s->d_R, 0, (size_t)NV * nu * 8, s->st);
+    if (e == cudaSuccess && fused) e = cudaMemsetAsync(s->d_ib, 0, (size_t)NV * nib * 8, s->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_im, 0, (size_t)NV * nd * 8, s->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_status, 0, sizeof(unsigned int), s->st);
+    if (e == cudaSuccess && fused) {
+        if (nu) {
+            gmap_copy_kernel<<<grid_for(nu, 256), 256, 0, s->st>>>(s->d_gmap, uz->d_copy, nu,
+                                                                  (uint32_t)(nd + uz->ninterp));
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess && uz->ninterp) {
+            gmap_interp_kernel<<<grid_for(uz->ninterp, 256), 256, 0, s->st>>>(
+                s->d_gmap, uz->d_gdst, uz->ninterp, (uint32_t)nd);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess && nu) e = cudaMemsetAsync(s->d_zmap, 0xFF, nu * 4, s->st);
+        if (e == cudaSuccess && nd) {
+            zmap_kernel<<<grid_for(nd, 256), 256, 0, s->st>>>(s->d_zmap, uz->d_zip, nd);
+            e = cudaGetLastError();
+        }
+    }
     if (e != cudaSuccess) {
         set_error(std::string("dgb_stepper_create: ") + cudaGetErrorString(e));
         dgb_stepper_destroy(s);
@@ -551,17 +667,41 @@ dgb_status dgb_stepper_create(dgb_plan *rhs_plan, dgb_unzip_plan *uz, int precis
     }
     // one RHS outside any capture: builds the plan's work items and kernel attributes
     double *U[NV], *R[NV];
-    for (int v = 0; v < NV; v++) {
-        U[v] = s->d_U + (size_t)v * nu;
-        R[v] = s->d_R + (size_t)v * nu;
+    dgb_status r;
+    if (!fused) {
+        for (int v = 0; v < NV; v++) {
+            U[v] = s->d_U + (size_t)v * nu;
+            R[v] = s->d_R + (size_t)v * nu;
+        }
+        r = dgb_bssn_rhs(rhs_plan, R, U, precision, s->st);
+    } else {
+        const double *Z[NV], *IB[NV];
+        for (int v = 0; v < NV; v++) {
+            Z[v] = s->d_im + (size_t)v * nd;
+            R[v] = s->d_k + (size_t)v * nd;
+            IB[v] = s->d_ib + (size_t)v * nib;
+        }
+        r = run_rhs_gather(rhs_plan, R, Z, IB, s->d_gmap, s->d_zmap, (uint32_t)nd, precision, s->st);
     }
-    dgb_status r = dgb_bssn_rhs(rhs_plan, R, U, precision, s->st);
     if (r == DGB_OK && cudaStreamSynchronize(s->st) != cudaSuccess) r = DGB_ERR_CUDA;
     if (r != DGB_OK) {
         dgb_stepper_destroy(s);
         return r;
     }
     *out = s;
+    return DGB_OK;
+}
+
+dgb_status dgb_stepper_create(dgb_plan *rhs_plan, dgb_unzip_plan *uz, int precision,
+                              dgb_stepper **out)
+{
+    return dgb_stepper_create_ex(rhs_plan, uz, precision, 0u, out);
+}
+
+dgb_status dgb_stepper_device_bytes(const dgb_stepper *s, uint64_t *bytes)
+{
+    if (!s || !bytes) return DGB_ERR_INVALID;
+    *bytes = s->device_bytes;
     return DGB_OK;
 }
 

@@ -161,6 +161,9 @@ _SIGS = {
     "dgb_unzip": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
     "dgb_zip": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
     "dgb_stepper_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "dgb_stepper_create_ex": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint,
+                                        C.POINTER(C.c_void_p)]),
+    "dgb_stepper_device_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "dgb_stepper_destroy": (C.c_int, [C.c_void_p]),
     "dgb_rk4_step": (C.c_int, [C.c_void_p, PtrArr, C.c_double, C.c_double, C.c_int,
                                C.c_void_p]),
@@ -526,13 +529,23 @@ class UnzipPlan:
             self.h = None
 
 
+STEP_FUSED_UNZIP = 1
+
+
 class Stepper:
-    def __init__(self, plan, uz, precision=PREC_FP64):
+    def __init__(self, plan, uz, precision=PREC_FP64, fused=False):
         h = C.c_void_p()
-        check(lib().dgb_stepper_create(plan.h, uz.h, precision, C.byref(h)),
-              "dgb_stepper_create")
+        check(lib().dgb_stepper_create_ex(plan.h, uz.h, precision,
+                                          STEP_FUSED_UNZIP if fused else 0, C.byref(h)),
+              "dgb_stepper_create_ex")
         self.h = h
         self._keep = (plan, uz)
+
+    @property
+    def device_bytes(self):
+        b = C.c_uint64()
+        check(lib().dgb_stepper_device_bytes(self.h, C.byref(b)), "dgb_stepper_device_bytes")
+        return b.value
 
     def step(self, state_ptrs, dt, nsteps=1, chi_floor=1e-4, stream=0):
         s, k = ptr_array(state_ptrs)

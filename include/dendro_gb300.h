@@ -333,6 +333,17 @@ dgb_status dgb_zip(dgb_unzip_plan *plan, const double *const *unzipped, double *
 typedef struct dgb_stepper dgb_stepper;
 dgb_status dgb_stepper_create(dgb_plan *rhs_plan, dgb_unzip_plan *uz, int precision,
                               dgb_stepper **stepper);
+/* flags: DGB_STEP_FUSED_UNZIP = the fused unzip -> RHS step: no unzipped
+ * field set is held; the RHS kernel stages its tiles from the zipped state
+ * (and a compact buffer of the interpolated padded points) through a gather
+ * index per padded point and writes each value to the zipped node its
+ * padded point owns.  Same results as the unfused stepper, bit for bit; 8
+ * bytes per padded point of maps instead of 2 x 24 x 8 bytes of fields. */
+#define DGB_STEP_FUSED_UNZIP 1u
+dgb_status dgb_stepper_create_ex(dgb_plan *rhs_plan, dgb_unzip_plan *uz, int precision,
+                                 unsigned flags, dgb_stepper **stepper);
+/* Device memory the stepper itself holds (bytes). */
+dgb_status dgb_stepper_device_bytes(const dgb_stepper *stepper, uint64_t *bytes);
 dgb_status dgb_stepper_destroy(dgb_stepper *stepper);
 dgb_status dgb_rk4_step(dgb_stepper *stepper, double *const *state, double dt, double chi_floor,
                         int nsteps, void *stream);

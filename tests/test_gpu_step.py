@@ -97,3 +97,32 @@ def test_rk4_step_graph_replay_is_deterministic(dgb, gpu, small_mesh):
         assert torch.equal(a[v], b[v])
     st.close()
     uz.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_unzip_step_matches_unfused(dgb, gpu, small_mesh, precision):
+    """The fused unzip -> RHS stepper (no unzipped field set) gives the
+    unfused stepper's state bit for bit, with less device memory."""
+    torch = gpu
+    m = small_mesh
+    prec = dgb.PREC_MIXED if precision == "mixed" else dgb.PREC_FP64
+    plan = dgb.Plan(m.blocks, dgb.default_params(0.4))
+    uz = dgb.UnzipPlan(m.operator(), m.ndof)
+    plain = dgb.Stepper(plan, uz, prec)
+    fused = dgb.Stepper(plan, uz, prec, fused=True)
+    z0 = mesh_state(dgb, m)
+    dt = 0.25 * 64.0 / (2 ** 6 * 6)
+    a = [torch.from_numpy(x.copy()).cuda() for x in z0]
+    b = [torch.from_numpy(x.copy()).cuda() for x in z0]
+    plain.step([t.data_ptr() for t in a], dt, nsteps=2)
+    fused.step([t.data_ptr() for t in b], dt, nsteps=2)
+    torch.cuda.synchronize()
+    for v in range(24):
+        assert torch.equal(a[v], b[v]), dgb.VAR_NAMES[v]
+    assert fused.device_bytes < plain.device_bytes
+    unzipped_bytes = 2 * 24 * 8 * m.nunzipped
+    assert plain.device_bytes - fused.device_bytes >= unzipped_bytes - 8 * m.nunzipped \
+        - 24 * 8 * (m.ninterp + 1)
+    plain.close()
+    fused.close()
+    uz.close()
