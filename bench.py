@@ -250,8 +250,9 @@ def main():
                     help="use only the first N blocks of the batch (profiling captures)")
     ap.add_argument("--octree-level", type=int, default=10,
                     help="wavelet_octree: finest octree level (smaller cases for captures)")
-    ap.add_argument("--fused", action="store_true",
-                    help="octree_rk4: the fused unzip -> RHS stepper (no unzipped field set)")
+    ap.add_argument("--stepper", default="fused", choices=["fused", "unfused"],
+                    help="octree_rk4: fused unzip -> RHS (no unzipped field set, default) or "
+                         "unzip -> RHS -> zip")
     ap.add_argument("--no-all-vars", action="store_true",
                     help="wavelet_octree: skip the 24-variable measurement (unzip only the "
                          "refinement variables)")
@@ -666,7 +667,7 @@ def main_octree(args, dgb, rank, world, local):
                       f"{mesh.num_leaves} leaves, {mesh.nblocks} blocks, "
                       f"{mesh.ndof} independent nodes",
           "step": "one RK4 step = 4 x (unzip -> bssnRHS+KO+BCs -> zip -> stage update), "
-                  "one CUDA graph",
+                  "one CUDA graph (fused stepper: the RHS gathers the unzip and writes the zip)",
           "units": "independent nodes x 24 vars per RK4 step", "ko_sigma": sigma,
           "dt": dt, "cfl": 0.25, "padded_points": mesh.nunzipped, "interior_points": n_int,
           "mesh_build_s": round(t_mesh, 2), "precision": args.precision,
@@ -704,9 +705,9 @@ def main_octree(args, dgb, rank, world, local):
         del tu, tr
         torch.cuda.empty_cache()
     uz = dgb.UnzipPlan(op, mesh.ndof)
-    st = dgb.Stepper(plan, uz, prec, fused=args.fused)
+    st = dgb.Stepper(plan, uz, prec, fused=args.stepper == "fused")
     wl["stepper"] = ("fused unzip -> RHS (gather from the zipped state, no unzipped set)"
-                     if args.fused else "unzip -> RHS -> zip")
+                     if args.stepper == "fused" else "unzip -> RHS -> zip")
     wl["stepper_device_gb"] = round(st.device_bytes / 1e9, 3)
     xyz = mesh.dof_coords()
     host = [np.empty(mesh.ndof) for _ in range(24)]
@@ -762,7 +763,7 @@ def main_octree(args, dgb, rank, world, local):
         cpu, _ = cpu_rk4_baseline(dgb, seed, sigma)
     # per stage: one source fill per level, interpolation, RHS, zip, update (+ the
     # copy of the unzip when unfused)
-    launches_per_step = 4 * (mesh.nlevels + (3 if args.fused else 5))
+    launches_per_step = 4 * (mesh.nlevels + (3 if args.stepper == "fused" else 5))
     if rank == 0:
         print(json.dumps({"metric": METRIC, "value": value, "unit": "grid-pts*vars/s",
                           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
