@@ -8,8 +8,8 @@
 // round-to-nearest-even product (the rounding the reference's stencils use):
 // for x = m * 2^(e-1075) with a 53-bit significand m, c*m is an exact integer
 // below 2^63; it is shifted back to 53 bits with round-half-even on the
-// dropped bits.  Zero, subnormal, infinite/NaN inputs and results that could
-// leave the normal range take the hardware multiply.
+// dropped bits.  Zero keeps its bits; subnormal, infinite/NaN inputs and
+// results that could leave the normal range take the hardware multiply.
 #pragma once
 #include <stdint.h>
 #include <string.h>
@@ -51,17 +51,29 @@ DGB_XM_HD int dgb_clz64(uint64_t v)
 #endif
 }
 
-// 2 * x: exact, an exponent increment for normal x.
+// The hardware multiply for the rare inputs (subnormal, huge, non-finite),
+// out of line on the device: inlined behind the exponent test, the compiler
+// may turn the branch into a select and issue the DMUL on every call, which
+// occupies the FP64 pipe (predicated off or not) and defeats the purpose.
+#if defined(__CUDA_ARCH__)
+template <uint32_t C>
+__device__ __noinline__ double dgb_mul_hw(double x)
+{
+    return __dmul_rn((double)C, x);
+}
+#define DGB_XM_SLOW(C, x) dgb_mul_hw<C>(x)
+#else
+#define DGB_XM_SLOW(C, x) ((double)(C) * (x))
+#endif
+
+// 2 * x: exact, an exponent increment for normal x; +-0 stays +-0.
 DGB_XM_HD double dgb_mul2(double x)
 {
     const uint64_t b = dgb_dbits(x);
     const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
     if (e == 0u || e >= 0x7FEu) {
-#if defined(__CUDA_ARCH__)
-        return __dmul_rn(2.0, x);
-#else
-        return 2.0 * x;
-#endif
+        if ((b << 1) == 0ull) return x;
+        return DGB_XM_SLOW(2u, x);
     }
     return dgb_bitsd(b + (1ull << 52));
 }
@@ -74,11 +86,8 @@ DGB_XM_HD double dgb_mul_const(double x)
     const uint64_t b = dgb_dbits(x);
     const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
     if (e == 0u || e >= 0x7FFu - 10u) {
-#if defined(__CUDA_ARCH__)
-        return __dmul_rn((double)C, x);
-#else
-        return (double)C * x;
-#endif
+        if ((b << 1) == 0ull) return x;  // C * (+-0) = +-0
+        return DGB_XM_SLOW(C, x);
     }
     const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
     const uint64_t p = m * (uint64_t)C;           // exact, < 2^63

@@ -74,6 +74,14 @@ namespace {
 
 DGB_HD double selftest_input(uint64_t seed, uint64_t i)
 {
+    // the edge cases first: +-0, subnormals, the normal range's ends, +-inf, NaN
+    const uint64_t special[12] = {0x0000000000000000ull, 0x8000000000000000ull,
+                                  0x0000000000000001ull, 0x800FFFFFFFFFFFFFull,
+                                  0x0010000000000000ull, 0x7FEFFFFFFFFFFFFFull,
+                                  0x7FF0000000000000ull, 0xFFF0000000000000ull,
+                                  0x7FF8000000000000ull, 0x3FF0000000000000ull,
+                                  0xBFF0000000000001ull, 0x7F50000000000000ull};
+    if (i < 12) return dgb_bitsd(special[i]);
     uint64_t b = dgb_mix64(seed ^ dgb_mix64(i));
     const uint64_t r = dgb_mix64(b);
     switch (i & 3u) {
@@ -101,9 +109,11 @@ DGB_HD uint64_t selftest_one(double x)
 
 DGB_HD uint64_t selftest_all(double x)
 {
-    uint64_t bad = selftest_one<6>(x) + selftest_one<9>(x) + selftest_one<15>(x)
-                 + selftest_one<20>(x) + selftest_one<27>(x) + selftest_one<45>(x)
-                 + selftest_one<270>(x) + selftest_one<490>(x);
+    uint64_t bad = selftest_one<3>(x) + selftest_one<5>(x) + selftest_one<6>(x)
+                 + selftest_one<9>(x) + selftest_one<10>(x) + selftest_one<12>(x)
+                 + selftest_one<15>(x) + selftest_one<18>(x) + selftest_one<19>(x)
+                 + selftest_one<20>(x) + selftest_one<27>(x) + selftest_one<30>(x)
+                 + selftest_one<45>(x) + selftest_one<270>(x) + selftest_one<490>(x);
 #if defined(__CUDA_ARCH__)
     const double two = __dmul_rn(2.0, x);
 #else
