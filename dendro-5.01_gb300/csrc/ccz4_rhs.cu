@@ -164,7 +164,13 @@ struct C4IO {
     }
 };
 
-template <int TX, int TY, int TZ, bool MIXED>
+// Phase D of a work item: stage each field, write its derivatives and KO sum
+// to the workspace.  BDY: the block touches a domain face.  Interior blocks
+// are compiled with the closure tests constant-false, so the one-sided
+// stencils (and the KO closures' divisions) are neither branched to nor
+// evaluated and selected away, and the upwind forms are split by the sorted
+// point lists.
+template <int TX, int TY, int TZ, bool MIXED, bool BDY>
 __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, const DevBlock &blk,
                                         double *S)
 {
@@ -192,7 +198,7 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
     const int sy = px, sz = px * py;
     const uint64_t rbase = blk.offset + (uint64_t)w.o[0]
                          + (uint64_t)nx * ((uint64_t)w.o[1] + (uint64_t)ny * w.o[2]);
-    const uint32_t bflag = blk.bflag;
+    const uint32_t bflag = BDY ? blk.bflag : 0u;
     const bool lo[3] = {(bflag & 1u) != 0, (bflag & 4u) != 0, (bflag & 16u) != 0};
     const bool hi[3] = {(bflag & 2u) != 0, (bflag & 8u) != 0, (bflag & 32u) != 0};
     const Ax4 ax[3] = {ax4(blk.h[0]), ax4(blk.h[1]), ax4(blk.h[2])};
@@ -224,18 +230,39 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
         return (d == 0 ? w.o[0] + ti : d == 1 ? w.o[1] + tj : w.o[2] + tk) + 3;
     };
 
-    // FP64 upwind derivatives over the tile points ordered by the sign of the shift
+    // FP64 upwind derivatives over the tile points ordered by the sign of the
+    // shift; interior blocks: the first s_cnt[2d] points take the forward
+    // form, the rest the backward one, each in a loop of its own
     auto adv64_sorted = [&](const double *F, double *Sa) {
 #pragma unroll
-        for (int d = 0; d < 3; d++)
-            for (int q = tid; q < P; q += kC4Threads) {
-                const int p = advl[d * G::PMAX + q];
-                int ti, tj, tk;
-                const int pos = tile_pos(p, d, &ti, &tj, &tk);
-                const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                Sa[d * G::PMAX + p] = adv42_at(c, st3[d], pos, nn[d], lo[d], hi[d],
-                                               bet[d * G::PMAX + p], ax[d]);
+        for (int d = 0; d < 3; d++) {
+            if (BDY) {
+                for (int q = tid; q < P; q += kC4Threads) {
+                    const int p = advl[d * G::PMAX + q];
+                    int ti, tj, tk;
+                    const int pos = tile_pos(p, d, &ti, &tj, &tk);
+                    const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                    Sa[d * G::PMAX + p] = adv42_at(c, st3[d], pos, nn[d], lo[d], hi[d],
+                                                   bet[d * G::PMAX + p], ax[d]);
+                }
+            } else {
+                const int npos = s_cnt[2 * d];
+                for (int q = tid; q < npos; q += kC4Threads) {
+                    const int p = advl[d * G::PMAX + q];
+                    int ti, tj, tk;
+                    tile_pos(p, d, &ti, &tj, &tk);
+                    const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                    Sa[d * G::PMAX + p] = adv42_pos(c, st3[d], ax[d].c12);
+                }
+                for (int q = npos + tid; q < P; q += kC4Threads) {
+                    const int p = advl[d * G::PMAX + q];
+                    int ti, tj, tk;
+                    tile_pos(p, d, &ti, &tj, &tk);
+                    const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                    Sa[d * G::PMAX + p] = adv42_neg(c, st3[d], ax[d].c12);
+                }
             }
+        }
     };
 
     auto issue_load = [&](int v, double *dst) {
@@ -297,20 +324,31 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                 }
                 Sko[p] = fp2_widen(ko);
             };
-            // upwind derivatives over the tile points ordered by the sign of the shift
+            // upwind derivatives over the tile points ordered by the sign of the
+            // shift: forward form on the first s_cnt[2d], backward on the rest
             auto adv_sorted = [&]() {
 #pragma unroll
-                for (int d = 0; d < 3; d++)
-                    for (int q = tid; q < P; q += kC4Threads) {
+                for (int d = 0; d < 3; d++) {
+                    const int npos = s_cnt[2 * d];
+                    for (int q = tid; q < npos; q += kC4Threads) {
                         const int p = advl[d * G::PMAX + q];
                         int ti, tj, tk;
                         tile_pos(p, d, &ti, &tj, &tk);
                         const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
-                        const bool up = bet[d * G::PMAX + p] > 0.0;
-                        FP2 a = up ? nadvp_c(fhi + off, st3[d]) : nadvn_c(fhi + off, st3[d]);
-                        a.e = __fadd_rn(a.e, up ? nadvp(flo + off, st3[d]) : nadvn(flo + off, st3[d]));
+                        FP2 a = nadvp_c(fhi + off, st3[d]);
+                        a.e = __fadd_rn(a.e, nadvp(flo + off, st3[d]));
                         Sa[d * G::PMAX + p] = to64(a, f12[d]);
                     }
+                    for (int q = npos + tid; q < P; q += kC4Threads) {
+                        const int p = advl[d * G::PMAX + q];
+                        int ti, tj, tk;
+                        tile_pos(p, d, &ti, &tj, &tk);
+                        const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
+                        FP2 a = nadvn_c(fhi + off, st3[d]);
+                        a.e = __fadd_rn(a.e, nadvn(flo + off, st3[d]));
+                        Sa[d * G::PMAX + p] = to64(a, f12[d]);
+                    }
+                }
             };
             if (q2 < 0) {
                 for (int p = tid; p < P; p += kC4Threads) {
@@ -461,7 +499,22 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
         }
         __syncthreads();  // F and the boxes are reused
     }
+}
 
+// Phase A of a work item (one thread per tile point), shared by interior and
+// boundary blocks: the algebra, the boundary condition on flagged faces, KO.
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ void c4_points(const C4Args &args, const WorkItem &w, const DevBlock &blk,
+                                          const double *S)
+{
+    using G = C4Geo<TX, TY, TZ>;
+    const int tid = threadIdx.x;
+    const int nx = blk.sz[0], ny = blk.sz[1], nz = blk.sz[2];
+    const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
+    const int P = ex * ey * ez;
+    const uint32_t bflag = blk.bflag;
+    const bool lo[3] = {(bflag & 1u) != 0, (bflag & 4u) != 0, (bflag & 16u) != 0};
+    const bool hi[3] = {(bflag & 2u) != 0, (bflag & 8u) != 0, (bflag & 32u) != 0};
     const C4AlgPrm aprm{args.prm.l1, args.prm.l2, args.prm.l3, args.prm.l4, args.prm.lf0,
                         args.prm.lf1, args.prm.k1, args.prm.k2, args.prm.p};
     for (int p = tid; p < P; p += kC4Threads) {
@@ -502,7 +555,11 @@ __global__ void __launch_bounds__(kC4Threads, kC4MinBlocks) c4_kernel(const C4Ar
         if (it >= (int)args.nitems) break;
         const WorkItem w = args.items[it];
         const DevBlock blk = args.blocks[w.blk];
-        c4_item<TX, TY, TZ, MIXED>(args, w, blk, S);
+        if (blk.bflag == 0)
+            c4_item<TX, TY, TZ, MIXED, false>(args, w, blk, S);
+        else
+            c4_item<TX, TY, TZ, MIXED, true>(args, w, blk, S);
+        c4_points<TX, TY, TZ>(args, w, blk, S);
     }
 }
 

@@ -321,7 +321,10 @@ struct PcGeo {
     static constexpr size_t bytes = (size_t)(2 * FBUF + DXB + DYB) * 8;
 };
 
-template <int TX, int TY, int TZ>
+// Phase D of a work item.  BDY: the block touches a domain face.  Interior
+// blocks are compiled with the closure tests constant-false, so the
+// one-sided stencils are neither branched to nor evaluated and selected away.
+template <int TX, int TY, int TZ, bool BDY>
 __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem &w, const DevBlock &blk,
                                              double *S)
 {
@@ -341,7 +344,7 @@ __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem 
     // staged region starts 2 points before the tile's first interior point
     const uint64_t rbase = blk.offset + (uint64_t)(w.o[0] + 1)
                          + (uint64_t)nx * ((uint64_t)(w.o[1] + 1) + (uint64_t)ny * (w.o[2] + 1));
-    const uint32_t bflag = blk.bflag;
+    const uint32_t bflag = BDY ? blk.bflag : 0u;
     const bool lo[3] = {(bflag & 1u) != 0, (bflag & 4u) != 0, (bflag & 16u) != 0};
     const bool hi[3] = {(bflag & 2u) != 0, (bflag & 8u) != 0, (bflag & 32u) != 0};
     const Ax4 ax[3] = {ax4(blk.h[0]), ax4(blk.h[1]), ax4(blk.h[2])};
@@ -424,7 +427,19 @@ __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem 
         }
         __syncthreads();  // F and the boxes are reused
     }
+}
 
+// Phase A of a work item (one thread per tile point), shared by interior and
+// boundary blocks.
+template <int TX, int TY, int TZ>
+__device__ __forceinline__ void physcon_points(const PcArgs &args, const WorkItem &w,
+                                               const DevBlock &blk, const double *S)
+{
+    using G = PcGeo<TX, TY, TZ>;
+    const int tid = threadIdx.x;
+    const int nx = blk.sz[0], ny = blk.sz[1];
+    const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
+    const int P = ex * ey * ez;
     for (int p = tid; p < P; p += kPcThreads) {
         const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
         const int i = w.o[0] + ti + 3, j = w.o[1] + tj + 3, k = w.o[2] + tk + 3;
@@ -455,7 +470,11 @@ __global__ void __launch_bounds__(kPcThreads, kPcMinBlocks) physcon_kernel(const
         if (it >= (int)args.nitems) break;
         const WorkItem w = args.items[it];
         const DevBlock blk = args.blocks[w.blk];
-        physcon_item<TX, TY, TZ>(args, w, blk, S);
+        if (blk.bflag == 0)
+            physcon_item<TX, TY, TZ, false>(args, w, blk, S);
+        else
+            physcon_item<TX, TY, TZ, true>(args, w, blk, S);
+        physcon_points<TX, TY, TZ>(args, w, blk, S);
     }
 }
 
