@@ -472,25 +472,23 @@ def main_ccz4(args, dgb, rank, world, local):
             "hbm_gbs_algorithmic": 25 * 8 * (n + npts) / (ms * 1e-3) / 1e9}
     e2e = None
     if not args.no_e2e:
-        hu = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(25)]
-        hr = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(25)]
-        for v in range(25):
-            hu[v].copy_(du[v])
+        del du, dr
+        torch.cuda.empty_cache()
+        hu = [np.empty(n) for _ in range(25)]
+        dgb.synth_fill_host(blocks, hu, seed, 1e-6)
+        hr = [np.zeros(n) for _ in range(25)]
+        plan.ccz4_rhs_host(prm, hr, hu, prec)  # warm-up: allocates the plan's staging
         k = max(1, min(args.steps, 3))
-        torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         for _ in range(k):
-            for v in range(25):
-                du[v].copy_(hu[v], non_blocking=True)
-            plan.ccz4_rhs(prm, rp, up, prec, sh)
-            for v in range(25):
-                hr[v].copy_(dr[v], non_blocking=True)
-            torch.cuda.synchronize(dev)
+            plan.ccz4_rhs_host(prm, hr, hu, prec)
         e2e_s = (time.perf_counter() - t0) / k
         e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
                "h2d_bytes_per_step": 25 * n * 8, "d2h_bytes_per_step": 25 * n * 8,
                "ms_per_step": e2e_s * 1e3,
-               "path": "pinned host arrays: H2D of the fields, dgb_ccz4_rhs, D2H of the rhs"}
+               "path": "dgb_ccz4_rhs_host (host arrays): chunked pipeline, host threads into "
+                       "pinned staging, uploads and downloads overlapping the kernel, interior "
+                       "points written back"}
         del hu, hr
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -82,11 +82,12 @@ void host_scatter_interior(double *const *rhs, const double *src, size_t slot_pt
 // Only interior points are written back, so the caller's rhs padding is
 // untouched without uploading rhs.
 struct HostPipe {
+    // slots hold up to NV4 (CCZ4) fields; BSSN uses the first NV
     size_t slot_pts = 0;
     std::vector<uint64_t> start, span;
     std::vector<std::vector<uint32_t>> members;
     std::vector<dgb_plan *> sub;
-    double *d_slots = nullptr;          // 3 u slots, then 3 rhs slots, NV * slot_pts each
+    double *d_slots = nullptr;          // 3 u slots, then 3 rhs slots, NV4 * slot_pts each
     double *h_in[2] = {nullptr, nullptr}, *h_out[2] = {nullptr, nullptr};  // pinned
     cudaStream_t s_h2d = nullptr, s_comp = nullptr, s_d2h = nullptr;
     std::vector<cudaEvent_t> ev_h2d, ev_comp, ev_d2h;
@@ -376,8 +377,10 @@ dgb_status dgb_plan_destroy(dgb_plan *p)
     cudaFree(p->d_first);
     for (auto d : p->d_items) cudaFree(d);
     cudaFree(p->d_queue);
-    if (!p->borrowed_scratch) cudaFree(p->d_scratch);
-    cudaFree(p->d_scratch4);
+    if (!p->borrowed_scratch) {
+        cudaFree(p->d_scratch);
+        cudaFree(p->d_scratch4);
+    }
     destroy_pipe(p->pipe);
     delete p;
     return DGB_OK;
@@ -450,6 +453,40 @@ dgb_status dgb_physical_constraints(dgb_plan *p, double *const *cons, const doub
     return DGB_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The CCZ4 kernel's residency and workspace, at first use per precision.
+dgb_status c4_workspace(dgb_plan *p, int precision)
+{
+    const int pq = precision == DGB_PREC_MIXED ? 1 : 0;
+    if (p->c4_occupancy[pq] != 0) return DGB_OK;
+    const int occ = c4_max_ctas_per_sm(precision);
+    if (occ < 1) {
+        set_error("dgb_ccz4_rhs: kernel cannot be resident");
+        return DGB_ERR_CUDA;
+    }
+    const size_t need = c4_scratch_per_cta() * (size_t)occ * (size_t)p->nsm;
+    if (need > p->scratch4_doubles) {
+        if (p->borrowed_scratch) {
+            set_error("dgb_ccz4_rhs: a chunk plan's borrowed workspace is too small");
+            return DGB_ERR_INVALID;
+        }
+        cudaFree(p->d_scratch4);
+        p->d_scratch4 = nullptr;
+        p->scratch4_doubles = 0;
+        DGB_CUDA(cudaMalloc(&p->d_scratch4, need * sizeof(double)));
+        p->scratch4_doubles = need;
+    }
+    p->c4_occupancy[pq] = occ;
+    return DGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 dgb_status dgb_ccz4_rhs(dgb_plan *p, const dgb_ccz4_params *prm, double *const *rhs,
                         const double *const *u, int precision, void *stream)
 {
@@ -470,22 +507,8 @@ dgb_status dgb_ccz4_rhs(dgb_plan *p, const dgb_ccz4_params *prm, double *const *
     dgb_status s = build_items(p, 0);  // the 8x8x8 schedule
     if (s != DGB_OK) return s;
     if (p->nitems[0] == 0) return DGB_OK;
-    if (p->c4_occupancy[pq] == 0) {
-        const int occ = c4_max_ctas_per_sm(precision);
-        if (occ < 1) {
-            set_error("dgb_ccz4_rhs: kernel cannot be resident");
-            return DGB_ERR_CUDA;
-        }
-        const size_t need = c4_scratch_per_cta() * (size_t)occ * (size_t)p->nsm;
-        if (need > p->scratch4_doubles) {
-            cudaFree(p->d_scratch4);
-            p->d_scratch4 = nullptr;
-            p->scratch4_doubles = 0;
-            DGB_CUDA(cudaMalloc(&p->d_scratch4, need * sizeof(double)));
-            p->scratch4_doubles = need;
-        }
-        p->c4_occupancy[pq] = occ;
-    }
+    s = c4_workspace(p, precision);
+    if (s != DGB_OK) return s;
     DGB_CUDA(c4_configure(precision));
     C4Args a;
     for (int v = 0; v < NV4; v++) {
@@ -593,6 +616,8 @@ dgb_status dgb_plan_autotune(dgb_plan *p, double *const *rhs, const double *cons
     return DGB_OK;
 }
 
+}  // extern "C"
+
 namespace {
 
 // Padded points per chunk: ~1.2 GB of fields each way per chunk, small next to
@@ -651,7 +676,7 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
         sp->borrowed_scratch = true;
         for (int q = 0; q < 2; q++) sp->variant[q] = p->variant[q];
     }
-    const size_t slot = (size_t)NV * h->slot_pts;
+    const size_t slot = (size_t)NV4 * h->slot_pts;
     DGB_CUDA(cudaMalloc(&h->d_slots, 6 * slot * sizeof(double)));
     for (int q = 0; q < 2; q++) {
         DGB_CUDA(cudaMallocHost(&h->h_in[q], slot * sizeof(double)));
@@ -672,33 +697,36 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
     return DGB_OK;
 }
 
-dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int precision)
+// The pipeline over the chunks for nv fields; compute(sub-plan, rhs, u, stream)
+// runs the kernel of one chunk.
+template <class Compute>
+dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int nv,
+                    Compute compute)
 {
     HostPipe *h = p->pipe;
     const long nch = (long)h->members.size();
-    const size_t slot = (size_t)NV * h->slot_pts;
-    const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
+    const size_t slot = (size_t)NV4 * h->slot_pts;
     auto ptrs = [&](int kind, long c, double **out) {  // kind 0: u slot, 1: rhs slot
         double *base = h->d_slots + (size_t)(3 * kind + (int)(c % 3)) * slot;
-        for (int v = 0; v < NV; v++) out[v] = base + (size_t)v * h->slot_pts;
+        for (int v = 0; v < nv; v++) out[v] = base + (size_t)v * h->slot_pts;
     };
     for (long step = 0; step < nch + 3; step++) {
         const long c = step - 1, d = step - 2, a = step, e = step - 3;
         if (c >= 0 && c < nch) {  // compute chunk c once its upload is done
             DGB_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_h2d[c], 0));
             if (c >= 3) DGB_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_d2h[c - 3], 0));
-            double *du[NV], *dr[NV];
+            double *du[NV4], *dr[NV4];
             ptrs(0, c, du);
             ptrs(1, c, dr);
-            dgb_status s = run_rhs(h->sub[c], dr, du, precision, p->variant[prec], h->s_comp);
+            dgb_status s = compute(h->sub[c], dr, (const double *const *)du, h->s_comp);
             if (s != DGB_OK) return s;
             DGB_CUDA(cudaEventRecord(h->ev_comp[c], h->s_comp));
         }
         if (d >= 0 && d < nch) {  // download chunk d once computed
             DGB_CUDA(cudaStreamWaitEvent(h->s_d2h, h->ev_comp[d], 0));
-            double *dr[NV];
+            double *dr[NV4];
             ptrs(1, d, dr);
-            for (int v = 0; v < NV; v++)
+            for (int v = 0; v < nv; v++)
                 DGB_CUDA(cudaMemcpyAsync(h->h_out[d % 2] + (size_t)v * h->slot_pts, dr[v],
                                          h->span[d] * sizeof(double), cudaMemcpyDeviceToHost,
                                          h->s_d2h));
@@ -706,11 +734,11 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
         }
         if (a < nch) {  // gather and upload chunk a
             if (a >= 2) DGB_CUDA(cudaEventSynchronize(h->ev_h2d[a - 2]));
-            host_gather(h->h_in[a % 2], h->slot_pts, u, NV, h->start[a], h->span[a]);
+            host_gather(h->h_in[a % 2], h->slot_pts, u, nv, h->start[a], h->span[a]);
             if (a >= 3) DGB_CUDA(cudaStreamWaitEvent(h->s_h2d, h->ev_comp[a - 3], 0));
-            double *du[NV];
+            double *du[NV4];
             ptrs(0, a, du);
-            for (int v = 0; v < NV; v++)
+            for (int v = 0; v < nv; v++)
                 DGB_CUDA(cudaMemcpyAsync(du[v], h->h_in[a % 2] + (size_t)v * h->slot_pts,
                                          h->span[a] * sizeof(double), cudaMemcpyHostToDevice,
                                          h->s_h2d));
@@ -718,14 +746,50 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
         }
         if (e >= 0 && e < nch) {  // scatter chunk e's interior points back
             DGB_CUDA(cudaEventSynchronize(h->ev_d2h[e]));
-            host_scatter_interior(rhs, h->h_out[e % 2], h->slot_pts, NV, p->blocks.data(),
+            host_scatter_interior(rhs, h->h_out[e % 2], h->slot_pts, nv, p->blocks.data(),
                                   h->members[e].data(), h->members[e].size(), h->start[e]);
         }
     }
     return DGB_OK;
 }
 
+// The plan's pipeline, built at first use; the sub-plans take the parent's
+// schedule choice.
+dgb_status ensure_pipe(dgb_plan *p)
+{
+    if (!p->pipe) {
+        HostPipe *h = new HostPipe();
+        dgb_status s = build_pipe_into(p, h);
+        if (s != DGB_OK) {
+            destroy_pipe(h);
+            return s;
+        }
+        p->pipe = h;
+    }
+    for (dgb_plan *sp : p->pipe->sub)
+        for (int q = 0; q < 2; q++) sp->variant[q] = p->variant[q];
+    return DGB_OK;
+}
+
+// whatever happened, nothing may still be copying into the staging buffers
+dgb_status finish_pipe(dgb_plan *p, dgb_status s, const char *what)
+{
+    HostPipe *h = p->pipe;
+    cudaError_t e1 = cudaStreamSynchronize(h->s_h2d);
+    cudaError_t e2 = cudaStreamSynchronize(h->s_comp);
+    cudaError_t e3 = cudaStreamSynchronize(h->s_d2h);
+    if (s != DGB_OK) return s;
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+        set_error(std::string(what) + ": " +
+                  cudaGetErrorString(e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3));
+        return DGB_ERR_CUDA;
+    }
+    return DGB_OK;
+}
+
 }  // namespace
+
+extern "C" {
 
 dgb_status dgb_bssn_rhs_host(dgb_plan *p, double *const *rhs, const double *const *u, int precision)
 {
@@ -743,30 +807,48 @@ dgb_status dgb_bssn_rhs_host(dgb_plan *p, double *const *rhs, const double *cons
         return DGB_ERR_INVALID;
     }
     if (p->blocks.empty()) return DGB_OK;
-    if (!p->pipe) {
-        HostPipe *h = new HostPipe();
-        dgb_status s = build_pipe_into(p, h);
-        if (s != DGB_OK) {
-            destroy_pipe(h);
-            return s;
-        }
-        p->pipe = h;
-    }
-    HostPipe *h = p->pipe;
-    for (size_t c = 0; c < h->sub.size(); c++)  // the parent's schedule choice
-        for (int q = 0; q < 2; q++) h->sub[c]->variant[q] = p->variant[q];
-    dgb_status s = run_pipe(p, rhs, u, precision);
-    // whatever happened, nothing may still be copying into the staging buffers
-    cudaError_t e1 = cudaStreamSynchronize(h->s_h2d);
-    cudaError_t e2 = cudaStreamSynchronize(h->s_comp);
-    cudaError_t e3 = cudaStreamSynchronize(h->s_d2h);
+    dgb_status s = ensure_pipe(p);
     if (s != DGB_OK) return s;
-    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
-        set_error(std::string("dgb_bssn_rhs_host: ") +
-                  cudaGetErrorString(e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3));
-        return DGB_ERR_CUDA;
+    const int variant = p->variant[precision == DGB_PREC_MIXED ? 1 : 0];
+    s = run_pipe(p, rhs, u, NV,
+                 [&](dgb_plan *sp, double *const *dr, const double *const *du, cudaStream_t st) {
+                     return run_rhs(sp, dr, du, precision, variant, st);
+                 });
+    return finish_pipe(p, s, "dgb_bssn_rhs_host");
+}
+
+dgb_status dgb_ccz4_rhs_host(dgb_plan *p, const dgb_ccz4_params *prm, double *const *rhs,
+                             const double *const *u, int precision)
+{
+    if (!p || !prm || !rhs || !u) {
+        set_error("dgb_ccz4_rhs_host: null argument");
+        return DGB_ERR_INVALID;
     }
-    return DGB_OK;
+    for (int v = 0; v < NV4; v++)
+        if (!rhs[v] || !u[v]) {
+            set_error("dgb_ccz4_rhs_host: null field pointer");
+            return DGB_ERR_INVALID;
+        }
+    if (precision != DGB_PREC_FP64 && precision != DGB_PREC_MIXED) {
+        set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
+        return DGB_ERR_INVALID;
+    }
+    if (p->blocks.empty()) return DGB_OK;
+    // the chunks run one after another on the parent's CCZ4 workspace
+    dgb_status s = c4_workspace(p, precision);
+    if (s == DGB_OK) s = ensure_pipe(p);
+    if (s != DGB_OK) return s;
+    const int pq = precision == DGB_PREC_MIXED ? 1 : 0;
+    for (dgb_plan *sp : p->pipe->sub) {
+        sp->d_scratch4 = p->d_scratch4;
+        sp->scratch4_doubles = p->scratch4_doubles;
+        sp->c4_occupancy[pq] = p->c4_occupancy[pq];
+    }
+    s = run_pipe(p, rhs, u, NV4,
+                 [&](dgb_plan *sp, double *const *dr, const double *const *du, cudaStream_t st) {
+                     return dgb_ccz4_rhs(sp, prm, dr, du, precision, st);
+                 });
+    return finish_pipe(p, s, "dgb_ccz4_rhs_host");
 }
 
 dgb_status dgb_bssnrhs_block_host(double *const *rhs, const double *const *u, uint64_t offset,

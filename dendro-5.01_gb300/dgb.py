@@ -120,6 +120,7 @@ _SIGS = {
                                             C.c_uint32, C.POINTER(BssnParams), C.c_void_p]),
     "dgb_plan_autotune": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
     "dgb_ccz4_rhs": (C.c_int, [C.c_void_p, C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
+    "dgb_ccz4_rhs_host": (C.c_int, [C.c_void_p, C.c_void_p, PtrArr, PtrArr, C.c_int]),
     "dgb_physical_constraints": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_void_p]),
     "dgb_constraint_l2": (C.c_int, [PtrArr, C.c_int, C.c_void_p, C.c_double, C.c_uint64,
                                     C.POINTER(C.c_double), C.c_void_p]),
@@ -291,6 +292,13 @@ class Plan:
         u, k2 = ptr_array(u_ptrs)
         check(lib().dgb_ccz4_rhs(self.h, C.byref(params), r, u, precision, C.c_void_p(stream)),
               "dgb_ccz4_rhs")
+
+    def ccz4_rhs_host(self, params, rhs_arrays, u_arrays, precision=PREC_FP64):
+        """CCZ4 right-hand side on 25 host (numpy) arrays each way."""
+        r, k1 = host_ptrs(rhs_arrays)
+        u, k2 = host_ptrs(u_arrays)
+        check(lib().dgb_ccz4_rhs_host(self.h, C.byref(params), r, u, precision),
+              "dgb_ccz4_rhs_host")
 
     def physical_constraints(self, cons_ptrs, u_ptrs, stream=0):
         """ham, mom0-2, psi4_real, psi4_img at every block interior point."""

@@ -166,6 +166,12 @@ typedef struct {
  * `stream`; calls on one plan must be ordered on one stream. */
 dgb_status dgb_ccz4_rhs(dgb_plan *plan, const dgb_ccz4_params *prm, double *const *rhs,
                         const double *const *u, int precision, void *stream);
+/* Same call with HOST arrays (the reference's calling convention, 25 fields
+ * each way): the chunked pipeline of dgb_bssn_rhs_host (host gather, upload,
+ * kernel, download and scatter of the interior points overlapped);
+ * synchronous; the padding of rhs is left untouched. */
+dgb_status dgb_ccz4_rhs_host(dgb_plan *plan, const dgb_ccz4_params *prm, double *const *rhs,
+                             const double *const *u, int precision);
 
 /* Constraint diagnostics over every block of a plan, device pointers:
  * replaces the per-block loop over physical_constraints (BSSN_GR/src/physcon.cpp:12-96,

@@ -172,3 +172,34 @@ def test_ccz4_mixed_precision(dgb, gpu, oracle, which):
         fmask = interior_mask(flagged, n)
         err = normwise(got, want, fmask)
         assert np.all(err <= FP64_TOL), dict(zip(dgb.CCZ4_VAR_NAMES, err))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ccz4_host_pipeline_many_chunks(dgb, gpu, precision, monkeypatch):
+    """dgb_ccz4_rhs_host over many chunks, block list not in offset order and
+    boundary blocks included: the device entry's bits, padding untouched."""
+    torch = gpu
+    monkeypatch.setenv("DGB_HOST_CHUNK_PTS", "30000")
+    prec = dgb.PREC_MIXED if precision == "mixed" else dgb.PREC_FP64
+    allb = dgb.synth_blocks(2, SEED2)
+    blocks = repack(dgb, allb, sample_uneven(allb, (6, 3, 2, 0)))
+    rows = [(b.offset, tuple(b.sz), b.bflag, tuple(b.ptmin), tuple(b.ptmax)) for b in blocks]
+    rows = [(o, sz, (63 if i % 3 == 0 else 0), pmin, pmax)
+            for i, (o, sz, _, pmin, pmax) in enumerate(rows)]
+    blocks = dgb.blocks_array(rows)
+    shuffled = dgb.blocks_array(rows[::-1])
+    u = ccz4_fields(dgb, blocks, SEED2)
+    prm = dgb.default_ccz4_params()
+    plan = dgb.Plan(shuffled, dgb.default_params(0.1))
+    du = [torch.from_numpy(a).cuda() for a in u]
+    n = len(u[0])
+    dr = [torch.full((n,), 7.0, dtype=torch.float64, device="cuda") for _ in range(25)]
+    plan.ccz4_rhs(prm, [t.data_ptr() for t in dr], [t.data_ptr() for t in du], prec)
+    torch.cuda.synchronize()
+    dev = [t.cpu().numpy() for t in dr]
+    for rep in range(2):  # the second call reuses the pipeline
+        host = [np.full(n, 7.0) for _ in range(25)]
+        plan.ccz4_rhs_host(prm, host, u, prec)
+        for v in range(25):
+            assert np.array_equal(dev[v], host[v]), (rep, dgb.CCZ4_VAR_NAMES[v])
+    plan.close()
