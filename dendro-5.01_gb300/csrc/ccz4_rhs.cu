@@ -167,8 +167,8 @@ struct C4IO {
 // Phase D of a work item: stage each field, write its derivatives and KO sum
 // to the workspace.  BDY: the block touches a domain face.  Interior blocks
 // are compiled with the closure tests constant-false, so the one-sided
-// stencils (and the KO closures' divisions) are neither branched to nor
-// evaluated and selected away, and the upwind forms are split by the sorted
+// stencils (and the KO closures' divisions) are not issued under a false
+// predicate on every point, and the upwind forms are split by the sorted
 // point lists.
 template <int TX, int TY, int TZ, bool MIXED, bool BDY>
 __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, const DevBlock &blk,

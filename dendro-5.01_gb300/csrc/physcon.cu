@@ -323,7 +323,7 @@ struct PcGeo {
 
 // Phase D of a work item.  BDY: the block touches a domain face.  Interior
 // blocks are compiled with the closure tests constant-false, so the
-// one-sided stencils are neither branched to nor evaluated and selected away.
+// one-sided stencils are not issued under a false predicate on every point.
 template <int TX, int TY, int TZ, bool BDY>
 __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem &w, const DevBlock &blk,
                                              double *S)
