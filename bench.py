@@ -17,6 +17,11 @@ Arms:
                           bssnrhs with OpenMP over blocks, as
                           BSSN_GR/src/rhsTestBed.cpp runs it), each step a
                           bounded, stratified sample of the same workload.
+Other workloads (--workload): uniform512 (512 x 13^3 blocks), octree_rk4
+(the full RK4 step on a level-10 octree, one CUDA graph; --stepper
+fused|unfused), ccz4_uneven20k, constraints_uneven20k, drift (mixed vs FP64
+over 100 steps), wavelet_octree (the isReMeshUnzip indicator); each with its own
+reference arm on the host cores.
 Multi-GPU (torchrun): replicas — every rank runs the whole batch on its own
 GPU with no collective on the data path; max time over ranks.
 """

@@ -334,8 +334,8 @@ dgb_status dgb_zip(dgb_unzip_plan *plan, const double *const *unzipped, double *
  * zip -> stage update with the constraint closure; the four stages of one
  * step are one CUDA graph, captured on the first call and replayed.
  * Replaces RK_BSSN::performSingleIteration's RK4 branch
- * (BSSN_GR/src/rkBSSN.cpp:603-1012).  The stepper owns the unzipped and
- * stage buffers. */
+ * (BSSN_GR/src/rkBSSN.cpp:603-1012).  The stepper owns its stage buffers and,
+ * unless fused (DGB_STEP_FUSED_UNZIP below), the unzipped field set. */
 typedef struct dgb_stepper dgb_stepper;
 dgb_status dgb_stepper_create(dgb_plan *rhs_plan, dgb_unzip_plan *uz, int precision,
                               dgb_stepper **stepper);
