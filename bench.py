@@ -20,8 +20,9 @@ Arms:
 Other workloads (--workload): uniform512 (512 x 13^3 blocks), octree_rk4
 (the full RK4 step on a level-10 octree, one CUDA graph; --stepper
 fused|unfused), ccz4_uneven20k, constraints_uneven20k, drift (mixed vs FP64
-over 100 steps), wavelet_octree (the isReMeshUnzip indicator); each with its own
-reference arm on the host cores.
+over 100 steps), wavelet_octree (the isReMeshUnzip indicator); each but drift
+(which compares the two precisions with each other) has its own reference arm on
+the host cores.
 Multi-GPU (torchrun): replicas — every rank runs the whole batch on its own
 GPU with no collective on the data path; max time over ranks.
 """
