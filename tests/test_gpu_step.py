@@ -52,7 +52,7 @@ def test_unzip_zip_match_host_operator(dgb, gpu, small_mesh):
     uz.close()
 
 
-@pytest.mark.parametrize("nsteps", [1, 2])
+@pytest.mark.parametrize("nsteps", [1, 2, 10])
 def test_rk4_step_matches_oracle(dgb, gpu, oracle, small_mesh, nsteps):
     torch = gpu
     m = small_mesh
