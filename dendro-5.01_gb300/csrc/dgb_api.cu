@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "dgb_internal.h"
+#include "host_rows.h"
 #include "synth.cuh"
 
 namespace dgb {
@@ -68,15 +69,15 @@ void destroy_pipe(struct HostPipe *h);
 namespace dgb {
 void host_gather(double *dst, size_t slot_pts, const double *const *u, int nv, uint64_t start,
                  uint64_t span);
-void host_scatter_interior(double *const *rhs, const double *src, size_t slot_pts, int nv,
-                           const dgb_block_desc *blocks, const uint32_t *members, size_t nmem,
-                           uint64_t start);
+void host_scatter_rows(double *const *rhs, const double *src, size_t islot, int nv,
+                       const IRow *rows, size_t nrows, uint64_t start);
 }  // namespace dgb
 
 // The host-array entry point as a pipeline over chunks of blocks (contiguous
 // in the caller's unzipped arrays): host threads copy chunk a's fields into
 // pinned staging while the GPU uploads chunk a-1... in order per chunk
-//   gather (host) -> H2D -> RHS -> D2H -> scatter of interior points (host)
+//   gather (host) -> H2D -> RHS -> pack the interior rows (device) -> D2H
+//   -> scatter of the interior rows (host)
 // with three device slots, two pinned staging buffers each way and separate
 // upload / compute / download streams, so transfers overlap the kernel.
 // Only interior points are written back, so the caller's rhs padding is
@@ -88,6 +89,15 @@ struct HostPipe {
     std::vector<std::vector<uint32_t>> members;
     std::vector<dgb_plan *> sub;
     double *d_slots = nullptr;          // 3 u slots, then 3 rhs slots, NV4 * slot_pts each
+    // the right-hand side's interior points of a chunk, packed row by row on the
+    // device before the download: only interior values cross the link and
+    // land in host memory
+    std::vector<IRow> rows;             // all chunks, in chunk order
+    std::vector<size_t> row_ptr;        // chunk c: rows[row_ptr[c] .. row_ptr[c+1])
+    std::vector<uint64_t> ispan;        // packed interior points per chunk
+    size_t islot = 0;
+    IRow *d_rows = nullptr;
+    double *d_packed = nullptr;         // 3 packed slots, NV4 * islot each
     double *h_in[2] = {nullptr, nullptr}, *h_out[2] = {nullptr, nullptr};  // pinned
     cudaStream_t s_h2d = nullptr, s_comp = nullptr, s_d2h = nullptr;
     std::vector<cudaEvent_t> ev_h2d, ev_comp, ev_d2h;
@@ -98,6 +108,8 @@ void destroy_pipe(HostPipe *h)
     if (!h) return;
     for (dgb_plan *sp : h->sub) dgb_plan_destroy(sp);
     cudaFree(h->d_slots);
+    cudaFree(h->d_rows);
+    cudaFree(h->d_packed);
     for (int q = 0; q < 2; q++) {
         cudaFreeHost(h->h_in[q]);
         cudaFreeHost(h->h_out[q]);
@@ -620,6 +632,35 @@ dgb_status dgb_plan_autotune(dgb_plan *p, double *const *rhs, const double *cons
 
 namespace {
 
+// Packs the interior rows of a chunk's right-hand side (nv fields, field v at
+// slot + v * slot_pts) into packed (field v at packed + v * islot): one warp
+// per (row, field).
+__global__ void __launch_bounds__(256) pack_rows_kernel(const double *__restrict__ slot,
+                                                        size_t slot_pts, double *__restrict__ packed,
+                                                        size_t islot, const IRow *__restrict__ rows,
+                                                        uint64_t nrows, int nv)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; w < nrows * nv;
+         w += nw) {
+        const IRow r = rows[w % nrows];
+        const uint64_t v = w / nrows;
+        const double *src = slot + v * slot_pts + r.src;
+        double *dst = packed + v * islot + r.dst;
+        for (uint32_t i = lane; i < r.len; i += 32) dst[i] = __ldg(src + i);
+    }
+}
+
+cudaError_t pack_rows_launch(const double *slot, size_t slot_pts, double *packed, size_t islot,
+                             const IRow *rows, uint64_t nrows, int nv, cudaStream_t st)
+{
+    const uint64_t warps = nrows * (uint64_t)nv;
+    const unsigned grid = (unsigned)std::min<uint64_t>((warps + 7) / 8, (uint64_t)g_nsm * 16);
+    pack_rows_kernel<<<grid, 256, 0, st>>>(slot, slot_pts, packed, islot, rows, nrows, nv);
+    return cudaGetLastError();
+}
+
 // Padded points per chunk: ~1.2 GB of fields each way per chunk, small next to
 // the 20k-block batch (~40 chunks) and large next to any block.
 constexpr uint64_t kChunkPts = 6u << 20;
@@ -676,11 +717,36 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
         sp->borrowed_scratch = true;
         for (int q = 0; q < 2; q++) sp->variant[q] = p->variant[q];
     }
+    // interior rows of each chunk, blocks in chunk order
+    h->row_ptr.assign(1, 0);
+    for (size_t c = 0; c < h->members.size(); c++) {
+        uint32_t packed = 0;
+        for (uint32_t b : h->members[c]) {
+            const dgb_block_desc &d = p->blocks[b];
+            const uint64_t base = d.offset - h->start[c];
+            const uint32_t nx = d.sz[0], ny = d.sz[1], nz = d.sz[2];
+            for (uint32_t k = 3; k + 3 < nz; k++)
+                for (uint32_t j = 3; j + 3 < ny; j++) {
+                    h->rows.push_back(IRow{(uint32_t)(base + 3 + (uint64_t)nx * (j + (uint64_t)ny * k)),
+                                           packed, nx - 6});
+                    packed += nx - 6;
+                }
+        }
+        h->ispan.push_back(packed);
+        h->islot = std::max<size_t>(h->islot, packed);
+        h->row_ptr.push_back(h->rows.size());
+    }
     const size_t slot = (size_t)NV4 * h->slot_pts;
+    const size_t pslot = (size_t)NV4 * h->islot;
     DGB_CUDA(cudaMalloc(&h->d_slots, 6 * slot * sizeof(double)));
+    DGB_CUDA(cudaMalloc(&h->d_packed, 3 * std::max<size_t>(pslot, 1) * sizeof(double)));
+    DGB_CUDA(cudaMalloc(&h->d_rows, std::max<size_t>(h->rows.size(), 1) * sizeof(IRow)));
+    if (!h->rows.empty())
+        DGB_CUDA(cudaMemcpy(h->d_rows, h->rows.data(), h->rows.size() * sizeof(IRow),
+                            cudaMemcpyHostToDevice));
     for (int q = 0; q < 2; q++) {
         DGB_CUDA(cudaMallocHost(&h->h_in[q], slot * sizeof(double)));
-        DGB_CUDA(cudaMallocHost(&h->h_out[q], slot * sizeof(double)));
+        DGB_CUDA(cudaMallocHost(&h->h_out[q], std::max<size_t>(pslot, 1) * sizeof(double)));
     }
     DGB_CUDA(cudaStreamCreateWithFlags(&h->s_h2d, cudaStreamNonBlocking));
     DGB_CUDA(cudaStreamCreateWithFlags(&h->s_comp, cudaStreamNonBlocking));
@@ -706,6 +772,7 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
     HostPipe *h = p->pipe;
     const long nch = (long)h->members.size();
     const size_t slot = (size_t)NV4 * h->slot_pts;
+    const size_t pslot = (size_t)NV4 * h->islot;
     auto ptrs = [&](int kind, long c, double **out) {  // kind 0: u slot, 1: rhs slot
         double *base = h->d_slots + (size_t)(3 * kind + (int)(c % 3)) * slot;
         for (int v = 0; v < nv; v++) out[v] = base + (size_t)v * h->slot_pts;
@@ -720,16 +787,20 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
             ptrs(1, c, dr);
             dgb_status s = compute(h->sub[c], dr, (const double *const *)du, h->s_comp);
             if (s != DGB_OK) return s;
+            const size_t nr = h->row_ptr[c + 1] - h->row_ptr[c];
+            if (nr) {
+                DGB_CUDA(pack_rows_launch(dr[0], h->slot_pts, h->d_packed + (size_t)(c % 3) * pslot,
+                                          h->islot, h->d_rows + h->row_ptr[c], nr, nv, h->s_comp));
+            }
             DGB_CUDA(cudaEventRecord(h->ev_comp[c], h->s_comp));
         }
-        if (d >= 0 && d < nch) {  // download chunk d once computed
+        if (d >= 0 && d < nch) {  // download chunk d's packed interior once computed
             DGB_CUDA(cudaStreamWaitEvent(h->s_d2h, h->ev_comp[d], 0));
-            double *dr[NV4];
-            ptrs(1, d, dr);
-            for (int v = 0; v < nv; v++)
-                DGB_CUDA(cudaMemcpyAsync(h->h_out[d % 2] + (size_t)v * h->slot_pts, dr[v],
-                                         h->span[d] * sizeof(double), cudaMemcpyDeviceToHost,
-                                         h->s_d2h));
+            const double *pk = h->d_packed + (size_t)(d % 3) * pslot;
+            for (int v = 0; v < nv && h->ispan[d]; v++)
+                DGB_CUDA(cudaMemcpyAsync(h->h_out[d % 2] + (size_t)v * h->islot,
+                                         pk + (size_t)v * h->islot, h->ispan[d] * sizeof(double),
+                                         cudaMemcpyDeviceToHost, h->s_d2h));
             DGB_CUDA(cudaEventRecord(h->ev_d2h[d], h->s_d2h));
         }
         if (a < nch) {  // gather and upload chunk a
@@ -744,10 +815,10 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
                                          h->s_h2d));
             DGB_CUDA(cudaEventRecord(h->ev_h2d[a], h->s_h2d));
         }
-        if (e >= 0 && e < nch) {  // scatter chunk e's interior points back
+        if (e >= 0 && e < nch) {  // scatter chunk e's interior rows back
             DGB_CUDA(cudaEventSynchronize(h->ev_d2h[e]));
-            host_scatter_interior(rhs, h->h_out[e % 2], h->slot_pts, nv, p->blocks.data(),
-                                  h->members[e].data(), h->members[e].size(), h->start[e]);
+            host_scatter_rows(rhs, h->h_out[e % 2], h->islot, nv, h->rows.data() + h->row_ptr[e],
+                              h->row_ptr[e + 1] - h->row_ptr[e], h->start[e]);
         }
     }
     return DGB_OK;
