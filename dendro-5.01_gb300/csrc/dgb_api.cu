@@ -767,15 +767,17 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
 // runs the kernel of one chunk.
 template <class Compute>
 dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int nv,
-                    Compute compute)
+                    Compute compute, int nv_out = -1)
 {
+    // nv fields in; nv_out (default nv) fields out
+    if (nv_out < 0) nv_out = nv;
     HostPipe *h = p->pipe;
     const long nch = (long)h->members.size();
     const size_t slot = (size_t)NV4 * h->slot_pts;
     const size_t pslot = (size_t)NV4 * h->islot;
     auto ptrs = [&](int kind, long c, double **out) {  // kind 0: u slot, 1: rhs slot
         double *base = h->d_slots + (size_t)(3 * kind + (int)(c % 3)) * slot;
-        for (int v = 0; v < nv; v++) out[v] = base + (size_t)v * h->slot_pts;
+        for (int v = 0; v < NV4; v++) out[v] = base + (size_t)v * h->slot_pts;
     };
     for (long step = 0; step < nch + 3; step++) {
         const long c = step - 1, d = step - 2, a = step, e = step - 3;
@@ -790,14 +792,15 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
             const size_t nr = h->row_ptr[c + 1] - h->row_ptr[c];
             if (nr) {
                 DGB_CUDA(pack_rows_launch(dr[0], h->slot_pts, h->d_packed + (size_t)(c % 3) * pslot,
-                                          h->islot, h->d_rows + h->row_ptr[c], nr, nv, h->s_comp));
+                                          h->islot, h->d_rows + h->row_ptr[c], nr, nv_out,
+                                          h->s_comp));
             }
             DGB_CUDA(cudaEventRecord(h->ev_comp[c], h->s_comp));
         }
         if (d >= 0 && d < nch) {  // download chunk d's packed interior once computed
             DGB_CUDA(cudaStreamWaitEvent(h->s_d2h, h->ev_comp[d], 0));
             const double *pk = h->d_packed + (size_t)(d % 3) * pslot;
-            for (int v = 0; v < nv && h->ispan[d]; v++)
+            for (int v = 0; v < nv_out && h->ispan[d]; v++)
                 DGB_CUDA(cudaMemcpyAsync(h->h_out[d % 2] + (size_t)v * h->islot,
                                          pk + (size_t)v * h->islot, h->ispan[d] * sizeof(double),
                                          cudaMemcpyDeviceToHost, h->s_d2h));
@@ -817,8 +820,9 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
         }
         if (e >= 0 && e < nch) {  // scatter chunk e's interior rows back
             DGB_CUDA(cudaEventSynchronize(h->ev_d2h[e]));
-            host_scatter_rows(rhs, h->h_out[e % 2], h->islot, nv, h->rows.data() + h->row_ptr[e],
-                              h->row_ptr[e + 1] - h->row_ptr[e], h->start[e]);
+            host_scatter_rows(rhs, h->h_out[e % 2], h->islot, nv_out,
+                              h->rows.data() + h->row_ptr[e], h->row_ptr[e + 1] - h->row_ptr[e],
+                              h->start[e]);
         }
     }
     return DGB_OK;
@@ -920,6 +924,34 @@ dgb_status dgb_ccz4_rhs_host(dgb_plan *p, const dgb_ccz4_params *prm, double *co
                      return dgb_ccz4_rhs(sp, prm, dr, du, precision, st);
                  });
     return finish_pipe(p, s, "dgb_ccz4_rhs_host");
+}
+
+dgb_status dgb_physical_constraints_host(dgb_plan *p, double *const *cons, const double *const *u)
+{
+    if (!p || !cons || !u) {
+        set_error("dgb_physical_constraints_host: null argument");
+        return DGB_ERR_INVALID;
+    }
+    for (int v = 0; v < NV; v++)
+        if (!u[v]) {
+            set_error("dgb_physical_constraints_host: null field pointer");
+            return DGB_ERR_INVALID;
+        }
+    for (int c = 0; c < DGB_NUM_CONSTRAINTS; c++)
+        if (!cons[c]) {
+            set_error("dgb_physical_constraints_host: null output pointer");
+            return DGB_ERR_INVALID;
+        }
+    if (p->blocks.empty()) return DGB_OK;
+    dgb_status s = ensure_pipe(p);
+    if (s != DGB_OK) return s;
+    s = run_pipe(
+        p, cons, u, NV,
+        [&](dgb_plan *sp, double *const *dr, const double *const *du, cudaStream_t st) {
+            return dgb_physical_constraints(sp, dr, du, st);
+        },
+        DGB_NUM_CONSTRAINTS);
+    return finish_pipe(p, s, "dgb_physical_constraints_host");
 }
 
 dgb_status dgb_bssnrhs_block_host(double *const *rhs, const double *const *u, uint64_t offset,

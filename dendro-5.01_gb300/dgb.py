@@ -122,6 +122,7 @@ _SIGS = {
     "dgb_ccz4_rhs": (C.c_int, [C.c_void_p, C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
     "dgb_ccz4_rhs_host": (C.c_int, [C.c_void_p, C.c_void_p, PtrArr, PtrArr, C.c_int]),
     "dgb_physical_constraints": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_void_p]),
+    "dgb_physical_constraints_host": (C.c_int, [C.c_void_p, PtrArr, PtrArr]),
     "dgb_constraint_l2": (C.c_int, [PtrArr, C.c_int, C.c_void_p, C.c_double, C.c_uint64,
                                     C.POINTER(C.c_double), C.c_void_p]),
     "dgb_plan_tile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint32)]),
@@ -299,6 +300,13 @@ class Plan:
         u, k2 = host_ptrs(u_arrays)
         check(lib().dgb_ccz4_rhs_host(self.h, C.byref(params), r, u, precision),
               "dgb_ccz4_rhs_host")
+
+    def physical_constraints_host(self, cons_arrays, u_arrays):
+        """The constraint diagnostics on host (numpy) arrays: 6 out, 24 in."""
+        c, k1 = host_ptrs(cons_arrays)
+        u, k2 = host_ptrs(u_arrays)
+        check(lib().dgb_physical_constraints_host(self.h, c, u),
+              "dgb_physical_constraints_host")
 
     def physical_constraints(self, cons_ptrs, u_ptrs, stream=0):
         """ham, mom0-2, psi4_real, psi4_img at every block interior point."""

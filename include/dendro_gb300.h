@@ -183,6 +183,11 @@ dgb_status dgb_ccz4_rhs_host(dgb_plan *plan, const dgb_ccz4_params *prm, double 
  * dgb_bssn_rhs, so calls on one plan must be ordered on one stream. */
 dgb_status dgb_physical_constraints(dgb_plan *plan, double *const *cons, const double *const *u,
                                     void *stream);
+/* Same call with HOST arrays (24 fields in, 6 out), through the chunked
+ * pipeline of the host-array RHS entries; synchronous; only interior points
+ * of the outputs are written. */
+dgb_status dgb_physical_constraints_host(dgb_plan *plan, double *const *cons,
+                                         const double *const *u);
 /* Masked RMS of nvars (<= DGB_NUM_CONSTRAINTS) zipped device vectors of
  * ndof values: sqrt(sum c^2 / count) over the nodes whose mask value is not
  * below threshold (mask may be NULL: every node counts).  Replaces

@@ -158,3 +158,26 @@ def test_constraint_pipeline_on_mesh(dgb, gpu, oracle):
     uz.close()
     plan.close()
     m.close()
+
+
+def test_constraints_host_pipeline_many_chunks(dgb, gpu, monkeypatch):
+    """dgb_physical_constraints_host over many chunks (24 fields in, 6 out),
+    block list not in offset order, boundary blocks included: the device
+    entry's bits, padding of the outputs untouched."""
+    torch = gpu
+    monkeypatch.setenv("DGB_HOST_CHUNK_PTS", "30000")
+    allb = dgb.synth_blocks(2, SEED2)
+    blocks = repack(dgb, allb, sample_uneven(allb, (6, 3, 2, 0)))
+    rows = [(b.offset, tuple(b.sz), (63 if i % 3 == 0 else 0), tuple(b.ptmin), tuple(b.ptmax))
+            for i, b in enumerate(blocks)]
+    blocks = dgb.blocks_array(rows)
+    u = host_fields(dgb, blocks, SEED2)
+    plan = dgb.Plan(dgb.blocks_array(rows[::-1]), dgb.default_params(0.1))
+    dev = gpu_constraints(dgb, torch, plan, u)
+    n = len(u[0])
+    for rep in range(2):  # the second call reuses the pipeline
+        host = [np.full(n, 7.0) for _ in range(6)]
+        plan.physical_constraints_host(host, u)
+        for c in range(6):
+            assert np.array_equal(dev[c], host[c]), (rep, dgb.CONSTRAINT_NAMES[c])
+    plan.close()
