@@ -337,7 +337,10 @@ def main():
     up = [t.data_ptr() for t in du]
     rp = [t.data_ptr() for t in dr]
     if args.autotune:
+        t0 = time.perf_counter()
         plan.autotune(rp, up, prec, sh)
+        wl["autotune_s"] = round(time.perf_counter() - t0, 1)
+        wl["class_tiles"] = [[list(sz), face, list(cap)] for sz, face, cap in plan.class_tiles(prec)]
     for _ in range(args.warmup):
         plan.rhs_device(rp, up, prec, sh)
     torch.cuda.synchronize(dev)
@@ -606,6 +609,26 @@ def main_constraints(args, dgb, rank, world, local):
             "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
             "flop_per_point": FLOP_PER_POINT_PHYSCON,
             "hbm_gbs_algorithmic": (17 * n + 6 * npts) * 8 / (ms * 1e-3) / 1e9}
+    e2e = None
+    if not args.no_e2e:
+        del du, dc
+        torch.cuda.empty_cache()
+        hu = [np.empty(n) for _ in range(24)]
+        dgb.synth_fill_host(blocks, hu, seed, 1e-6)
+        hc = [np.zeros(n) for _ in range(6)]
+        plan.physical_constraints_host(hc, hu)  # warm-up: builds the plan's pipeline
+        k = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(k):
+            plan.physical_constraints_host(hc, hu)
+        e2e_s = (time.perf_counter() - t0) / k
+        e2e = {"value": npts / e2e_s, "unit": "grid-pts/s",
+               "h2d_bytes_per_step": 24 * n * 8, "d2h_bytes_per_step": 6 * npts * 8,
+               "ms_per_step": e2e_s * 1e3,
+               "path": "dgb_physical_constraints_host (host arrays): chunked pipeline, host "
+                       "threads into pinned staging, uploads, interior rows packed on the "
+                       "device and downloaded, written back by host threads"}
+        del hu, hc
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu, _ = cpu_constraints_baseline(dgb, blocks, seed)
@@ -615,7 +638,7 @@ def main_constraints(args, dgb, rank, world, local):
                           "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                           "vs_baseline": None, "dtype": "f64",
                           "data": "synthetic (seeded Brill-Lindquist + 1e-6 noise)",
-                          "config": wl, "roofline": roof, "cpu_baseline": cpu, "e2e": None,
+                          "config": wl, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                           "clocks": clocks, "gpu_launches": args.steps, "impl": "ours"}))
     plan.close()
     if world > 1:
@@ -700,12 +723,15 @@ def main_octree(args, dgb, rank, world, local):
     prec = dgb.PREC_MIXED if args.precision == "mixed" else dgb.PREC_FP64
     op = mesh.operator()
     plan = dgb.Plan(mesh.blocks, dgb.default_params(sigma))
-    if not args.no_autotune:  # the octree's interiors (7, 13, 25, 49) favour 7^3 tiles
+    if not args.no_autotune:  # tile caps per block-size class (interiors 7, 13, 25, 49)
         tu = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(24)]
         tr = [torch.zeros_like(tu[0]) for _ in range(24)]
         plan.synth_fill_device([t.data_ptr() for t in tu], seed, 1e-6)
+        t0 = time.perf_counter()
         plan.autotune([t.data_ptr() for t in tr], [t.data_ptr() for t in tu], prec)
+        wl["autotune_s"] = round(time.perf_counter() - t0, 1)
         wl["tile"] = plan.tile(prec)
+        wl["class_tiles"] = [[list(sz), face, list(cap)] for sz, face, cap in plan.class_tiles(prec)]
         del tu, tr
         torch.cuda.empty_cache()
     uz = dgb.UnzipPlan(op, mesh.ndof)

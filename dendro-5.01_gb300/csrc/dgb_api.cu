@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -49,6 +50,17 @@ struct dgb_plan {
     std::vector<WorkItem *> d_items;
     std::vector<uint32_t> nitems;
     int variant[2] = {0, 0};  // chosen tile variant per precision
+    // per precision: tile caps per block-size class picked by the autotuner
+    // (class key: sizes and whether the block touches a domain face); blocks of
+    // classes without an entry take the variant's full tile
+    std::map<uint64_t, TileShape> caps[2];
+    uint64_t caps_gen[2] = {0, 0};
+    struct ItemCache {
+        int variant = -1;
+        uint64_t gen = ~0ull;
+        WorkItem *d = nullptr;
+        uint32_t n = 0;
+    } rhs_items[2];  // the BSSN RHS's work items per precision
     unsigned int *d_queue = nullptr;
     double *d_scratch = nullptr;
     size_t scratch_doubles = 0;
@@ -141,14 +153,23 @@ void split_extent(int m, int t, std::vector<std::pair<int, int>> &out)
     }
 }
 
-dgb_status build_items(dgb_plan *p, int variant)
+uint64_t class_key(const dgb_block_desc &d)
 {
-    if (p->d_items[variant]) return DGB_OK;
-    const TileShape t = kTileShapes[variant];
-    std::vector<WorkItem> items;
+    return ((uint64_t)d.sz[0] << 42) | ((uint64_t)d.sz[1] << 22) | ((uint64_t)d.sz[2] << 2) |
+           (d.bflag != 0 ? 1u : 0u);
+}
+
+// Work items of the blocks `sel` accepts, each block cut with its tile cap
+// (cap(b) <= the variant's tile), largest tiles first.
+template <class Sel, class Cap>
+dgb_status make_items(const dgb_plan *p, Sel sel, Cap cap, std::vector<WorkItem> &items)
+{
+    items.clear();
     std::vector<std::pair<int, int>> sx, sy, sz;
     for (size_t b = 0; b < p->blocks.size(); b++) {
         const dgb_block_desc &d = p->blocks[b];
+        if (!sel(d)) continue;
+        const TileShape t = cap(d);
         split_extent((int)d.sz[0] - 6, t.tx, sx);
         split_extent((int)d.sz[1] - 6, t.ty, sy);
         split_extent((int)d.sz[2] - 6, t.tz, sz);
@@ -172,13 +193,73 @@ dgb_status build_items(dgb_plan *p, int variant)
     std::stable_sort(items.begin(), items.end(), [](const WorkItem &a, const WorkItem &b) {
         return a.e[0] * a.e[1] * a.e[2] > b.e[0] * b.e[1] * b.e[2];
     });
+    return DGB_OK;
+}
+
+dgb_status upload_items(const std::vector<WorkItem> &items, WorkItem **d)
+{
+    *d = nullptr;
+    if (items.empty()) return DGB_OK;
+    DGB_CUDA(cudaMalloc(d, items.size() * sizeof(WorkItem)));
+    DGB_CUDA(cudaMemcpy(*d, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+    return DGB_OK;
+}
+
+// The variant's full-tile schedule (also the CCZ4 and constraint kernels').
+dgb_status build_items(dgb_plan *p, int variant)
+{
+    if (p->d_items[variant]) return DGB_OK;
+    const TileShape t = kTileShapes[variant];
+    std::vector<WorkItem> items;
+    dgb_status s = make_items(p, [](const dgb_block_desc &) { return true; },
+                              [&](const dgb_block_desc &) { return t; }, items);
+    if (s != DGB_OK) return s;
     WorkItem *d = nullptr;
-    if (!items.empty()) {
-        DGB_CUDA(cudaMalloc(&d, items.size() * sizeof(WorkItem)));
-        DGB_CUDA(cudaMemcpy(d, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
-    }
+    s = upload_items(items, &d);
+    if (s != DGB_OK) return s;
     p->d_items[variant] = d;
     p->nitems[variant] = (uint32_t)items.size();
+    return DGB_OK;
+}
+
+TileShape clip(TileShape a, TileShape m)
+{
+    return TileShape{std::min(a.tx, m.tx), std::min(a.ty, m.ty), std::min(a.tz, m.tz)};
+}
+
+// The BSSN RHS's schedule for a precision: the variant's tile, capped per
+// block-size class where the autotuner chose a cap.
+dgb_status rhs_items(dgb_plan *p, int variant, int prec, const WorkItem **d, uint32_t *n)
+{
+    dgb_plan::ItemCache &c = p->rhs_items[prec];
+    if (p->caps[prec].empty()) {
+        dgb_status s = build_items(p, variant);
+        *d = p->d_items[variant];
+        *n = p->nitems[variant];
+        return s;
+    }
+    if (c.variant != variant || c.gen != p->caps_gen[prec]) {
+        const TileShape m = kTileShapes[variant];
+        std::vector<WorkItem> items;
+        dgb_status s = make_items(
+            p, [](const dgb_block_desc &) { return true; },
+            [&](const dgb_block_desc &b) {
+                auto it = p->caps[prec].find(class_key(b));
+                return it == p->caps[prec].end() ? m : clip(it->second, m);
+            },
+            items);
+        if (s != DGB_OK) return s;
+        cudaFree(c.d);
+        c.d = nullptr;
+        c.n = 0;
+        s = upload_items(items, &c.d);
+        if (s != DGB_OK) return s;
+        c.n = (uint32_t)items.size();
+        c.variant = variant;
+        c.gen = p->caps_gen[prec];
+    }
+    *d = c.d;
+    *n = c.n;
     return DGB_OK;
 }
 
@@ -192,6 +273,9 @@ RhsParams rhs_params(const dgb_bssn_params &q)
     return r;
 }
 
+dgb_status run_rhs_on(dgb_plan *p, double *const *rhs, const double *const *u, int precision,
+                      int variant, const WorkItem *items, uint32_t nitems, cudaStream_t st);
+
 dgb_status run_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int precision,
                    int variant, cudaStream_t st)
 {
@@ -199,9 +283,18 @@ dgb_status run_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int 
         set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
         return DGB_ERR_INVALID;
     }
-    dgb_status s = build_items(p, variant);
+    const WorkItem *items = nullptr;
+    uint32_t nitems = 0;
+    dgb_status s = rhs_items(p, variant, precision == DGB_PREC_MIXED ? 1 : 0, &items, &nitems);
     if (s != DGB_OK) return s;
-    if (p->nitems[variant] == 0) return DGB_OK;
+    return run_rhs_on(p, rhs, u, precision, variant, items, nitems, st);
+}
+
+// The RHS kernel of `variant` over an explicit work-item list.
+dgb_status run_rhs_on(dgb_plan *p, double *const *rhs, const double *const *u, int precision,
+                      int variant, const WorkItem *items, uint32_t nitems, cudaStream_t st)
+{
+    if (nitems == 0) return DGB_OK;
     DGB_CUDA(rhs_configure(variant, precision));
     RhsArgs a{};
     for (int v = 0; v < NV; v++) {
@@ -209,8 +302,8 @@ dgb_status run_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int 
         a.rhs[v] = rhs[v];
     }
     a.blocks = p->d_blocks;
-    a.items = p->d_items[variant];
-    a.nitems = p->nitems[variant];
+    a.items = items;
+    a.nitems = nitems;
     a.queue = p->d_queue;
     a.scratch = p->d_scratch;
     a.prm = rhs_params(p->prm);
@@ -232,9 +325,11 @@ dgb_status dgb::run_rhs_gather(dgb_plan *p, double *const *k, const double *cons
     }
     const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
     const int variant = p->variant[prec];
-    dgb_status s = build_items(p, variant);
+    const WorkItem *items = nullptr;
+    uint32_t nitems = 0;
+    dgb_status s = rhs_items(p, variant, prec, &items, &nitems);
     if (s != DGB_OK) return s;
-    if (p->nitems[variant] == 0) return DGB_OK;
+    if (nitems == 0) return DGB_OK;
     if (p->occupancy_g[variant][prec] == 0) {
         // the workspace is sized for the plain kernels' residency: never exceed it
         const int occ = rhs_max_ctas_per_sm_gather(variant, precision);
@@ -254,8 +349,8 @@ dgb_status dgb::run_rhs_gather(dgb_plan *p, double *const *k, const double *cons
     a.zmap = zmap;
     a.ndof = ndof;
     a.blocks = p->d_blocks;
-    a.items = p->d_items[variant];
-    a.nitems = p->nitems[variant];
+    a.items = items;
+    a.nitems = nitems;
     a.queue = p->d_queue;
     a.scratch = p->d_scratch;
     a.prm = rhs_params(p->prm);
@@ -388,6 +483,7 @@ dgb_status dgb_plan_destroy(dgb_plan *p)
     cudaFree(p->d_blocks);
     cudaFree(p->d_first);
     for (auto d : p->d_items) cudaFree(d);
+    for (int q = 0; q < 2; q++) cudaFree(p->rhs_items[q].d);
     cudaFree(p->d_queue);
     if (!p->borrowed_scratch) {
         cudaFree(p->d_scratch);
@@ -417,7 +513,10 @@ dgb_status dgb_plan_set_tile_variant(dgb_plan *p, int precision, int variant)
         set_error("dgb_plan_set_tile_variant: bad plan or variant");
         return DGB_ERR_INVALID;
     }
-    p->variant[precision == DGB_PREC_MIXED ? 1 : 0] = variant;
+    const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
+    p->variant[prec] = variant;
+    p->caps[prec].clear();  // the variant's full tile for every block
+    p->caps_gen[prec]++;
     return DGB_OK;
 }
 
@@ -600,31 +699,112 @@ dgb_status dgb_plan_autotune(dgb_plan *p, double *const *rhs, const double *cons
                              int precision, void *stream)
 {
     if (!p || !rhs || !u) return DGB_ERR_INVALID;
+    if (precision != DGB_PREC_FP64 && precision != DGB_PREC_MIXED) {
+        set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
+        return DGB_ERR_INVALID;
+    }
     cudaStream_t st = (cudaStream_t)stream;
     const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
+    // block-size classes
+    std::map<uint64_t, size_t> classes;
+    for (const dgb_block_desc &d : p->blocks) classes[class_key(d)]++;
     cudaEvent_t e0, e1;
     DGB_CUDA(cudaEventCreate(&e0));
     DGB_CUDA(cudaEventCreate(&e1));
-    float best = 1e30f;
-    int bestv = p->variant[prec];
-    for (int v = 0; v < kNumTileShapes; v++) {
-        dgb_status s = run_rhs(p, rhs, u, precision, v, st);  // warm-up
-        if (s != DGB_OK) return s;
+    dgb_status s = DGB_OK;
+    std::vector<WorkItem> items;
+    WorkItem *d = nullptr;
+    // one class on one variant with one cap: time of a launch over that class
+    auto time_class = [&](int v, uint64_t key, TileShape cap, float *ms) -> dgb_status {
+        dgb_status r = make_items(
+            p, [&](const dgb_block_desc &b) { return class_key(b) == key; },
+            [&](const dgb_block_desc &) { return cap; }, items);
+        if (r != DGB_OK) return r;
+        cudaFree(d);
+        d = nullptr;
+        r = upload_items(items, &d);
+        if (r != DGB_OK) return r;
+        const uint32_t n = (uint32_t)items.size();
+        r = run_rhs_on(p, rhs, u, precision, v, d, n, st);  // warm-up
+        if (r != DGB_OK) return r;
         DGB_CUDA(cudaEventRecord(e0, st));
-        s = run_rhs(p, rhs, u, precision, v, st);
-        if (s != DGB_OK) return s;
+        r = run_rhs_on(p, rhs, u, precision, v, d, n, st);
+        if (r != DGB_OK) return r;
         DGB_CUDA(cudaEventRecord(e1, st));
         DGB_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        DGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best) {
-            best = ms;
-            bestv = v;
+        DGB_CUDA(cudaEventElapsedTime(ms, e0, e1));
+        return DGB_OK;
+    };
+    float best_total = 1e30f;
+    int best_v = p->variant[prec];
+    std::map<uint64_t, TileShape> best_caps;
+    for (int v = 0; v < kNumTileShapes && s == DGB_OK; v++) {
+        const TileShape m = kTileShapes[v];
+        // candidate caps: every compiled tile shape clipped to this variant's tile
+        std::vector<TileShape> cands;
+        for (int q = 0; q < kNumTileShapes; q++) {
+            const TileShape c = clip(kTileShapes[q], m);
+            bool dup = false;
+            for (const TileShape &x : cands) dup = dup || (x.tx == c.tx && x.ty == c.ty && x.tz == c.tz);
+            if (!dup) cands.push_back(c);
+        }
+        float total = 0.f;
+        std::map<uint64_t, TileShape> caps;
+        for (const auto &kv : classes) {
+            float best = 1e30f;
+            TileShape bc = m;
+            for (const TileShape &c : cands) {
+                float ms = 0.f;
+                s = time_class(v, kv.first, c, &ms);
+                if (s == DGB_ERR_INVALID) {  // a cap too thin for a boundary block: skip it
+                    s = DGB_OK;
+                    continue;
+                }
+                if (s != DGB_OK) break;
+                if (ms < best) {
+                    best = ms;
+                    bc = c;
+                }
+            }
+            if (s != DGB_OK) break;
+            total += best;
+            caps[kv.first] = bc;
+        }
+        if (s == DGB_OK && total < best_total) {
+            best_total = total;
+            best_v = v;
+            best_caps = caps;
         }
     }
+    cudaFree(d);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    p->variant[prec] = bestv;
+    if (s != DGB_OK) return s;
+    p->variant[prec] = best_v;
+    p->caps[prec] = best_caps;
+    p->caps_gen[prec]++;
+    return DGB_OK;
+}
+
+dgb_status dgb_plan_class_tiles(const dgb_plan *p, int precision, uint32_t *rows, size_t cap,
+                                size_t *count)
+{
+    if (!p || !count) return DGB_ERR_INVALID;
+    const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
+    *count = p->caps[prec].size();
+    if (!rows) return DGB_OK;
+    size_t i = 0;
+    for (const auto &kv : p->caps[prec]) {
+        if (i >= cap) break;
+        uint32_t *r = rows + 7 * i++;
+        r[0] = (uint32_t)(kv.first >> 42);
+        r[1] = (uint32_t)((kv.first >> 22) & 0xFFFFF);
+        r[2] = (uint32_t)((kv.first >> 2) & 0xFFFFF);
+        r[3] = (uint32_t)(kv.first & 1u);
+        r[4] = kv.second.tx;
+        r[5] = kv.second.ty;
+        r[6] = kv.second.tz;
+    }
     return DGB_OK;
 }
 
@@ -841,8 +1021,22 @@ dgb_status ensure_pipe(dgb_plan *p)
         }
         p->pipe = h;
     }
+    auto same = [](const std::map<uint64_t, TileShape> &a, const std::map<uint64_t, TileShape> &b) {
+        if (a.size() != b.size()) return false;
+        for (auto i = a.begin(), j = b.begin(); i != a.end(); ++i, ++j)
+            if (i->first != j->first || i->second.tx != j->second.tx ||
+                i->second.ty != j->second.ty || i->second.tz != j->second.tz)
+                return false;
+        return true;
+    };
     for (dgb_plan *sp : p->pipe->sub)
-        for (int q = 0; q < 2; q++) sp->variant[q] = p->variant[q];
+        for (int q = 0; q < 2; q++) {
+            sp->variant[q] = p->variant[q];
+            if (!same(sp->caps[q], p->caps[q])) {
+                sp->caps[q] = p->caps[q];
+                sp->caps_gen[q]++;
+            }
+        }
     return DGB_OK;
 }
 

@@ -126,6 +126,8 @@ _SIGS = {
     "dgb_constraint_l2": (C.c_int, [PtrArr, C.c_int, C.c_void_p, C.c_double, C.c_uint64,
                                     C.POINTER(C.c_double), C.c_void_p]),
     "dgb_plan_tile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint32)]),
+    "dgb_plan_class_tiles": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t,
+                                       C.POINTER(C.c_size_t)]),
     "dgb_num_tile_variants": (C.c_int, []),
     "dgb_plan_set_tile_variant": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "dgb_rk4_stage": (C.c_int, [C.c_int, PtrArr, PtrArr, PtrArr, C.c_uint64, C.c_double,
@@ -325,6 +327,17 @@ class Plan:
         t = (C.c_uint32 * 3)()
         check(lib().dgb_plan_tile(self.h, precision, t), "dgb_plan_tile")
         return tuple(t)
+
+    def class_tiles(self, precision=PREC_FP64):
+        """The autotuner's per-class caps: list of ((sx, sy, sz), face, (cx, cy, cz))."""
+        n = C.c_size_t(0)
+        check(lib().dgb_plan_class_tiles(self.h, precision, None, 0, C.byref(n)),
+              "dgb_plan_class_tiles")
+        rows = (C.c_uint32 * (7 * max(1, n.value)))()
+        check(lib().dgb_plan_class_tiles(self.h, precision, rows, n.value, C.byref(n)),
+              "dgb_plan_class_tiles")
+        return [((rows[7 * i], rows[7 * i + 1], rows[7 * i + 2]), rows[7 * i + 3],
+                 (rows[7 * i + 4], rows[7 * i + 5], rows[7 * i + 6])) for i in range(n.value)]
 
     def set_tile_variant(self, variant, precision=PREC_FP64):
         check(lib().dgb_plan_set_tile_variant(self.h, precision, variant),

@@ -128,14 +128,24 @@ dgb_status dgb_bssnrhs_block_noalloc(double *const *rhs, const double *const *u,
                                      const uint32_t *sz, uint32_t bflag,
                                      const dgb_bssn_params *prm, void *stream);
 
-/* Autotuner: times the candidate tile schedules for each block-size class of
- * the plan on device buffers and keeps the fastest.  Optional. */
+/* Autotuner: for every compiled kernel variant (maximum tile) and every
+ * block-size class of the plan (sizes, and whether the block touches a domain
+ * face), times each candidate tile cap on the caller's device buffers; keeps
+ * the variant whose per-class best caps give the shortest total, and those
+ * caps.  Optional; the chosen schedule is used by every BSSN RHS entry of the
+ * plan until the next autotune or dgb_plan_set_tile_variant. */
 dgb_status dgb_plan_autotune(dgb_plan *plan, double *const *rhs, const double *const *u,
                              int precision, void *stream);
+/* The per-class tile caps the autotuner chose: count classes; when rows is not
+ * NULL, up to cap rows of 7 values (sx, sy, sz, touches-a-face, cap_x, cap_y,
+ * cap_z). */
+dgb_status dgb_plan_class_tiles(const dgb_plan *plan, int precision, uint32_t *rows, size_t cap,
+                                size_t *count);
 /* Current maximum tile extents (out: tx,ty,tz) of the schedule chosen for
  * `precision`; every block is cut into the fewest tiles within them. */
 dgb_status dgb_plan_tile(const dgb_plan *plan, int precision, uint32_t *tile3);
-/* Compiled tile schedules: count, and explicit choice (bypasses autotune). */
+/* Compiled tile schedules: count, and explicit choice (bypasses autotune and
+ * clears its per-class caps). */
 int dgb_num_tile_variants(void);
 dgb_status dgb_plan_set_tile_variant(dgb_plan *plan, int precision, int variant);
 

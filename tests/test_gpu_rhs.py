@@ -74,6 +74,17 @@ def test_rhs_all_tile_variants_agree(dgb, gpu, oracle):
     plan.autotune([t.data_ptr() for t in dr], [t.data_ptr() for t in du], 0)
     got = run_device(dgb, torch, plan, u)
     assert np.all(normwise(got, want, mask) <= FP64_TOL)
+    # one tile cap per block-size class, within the chosen variant's tile
+    ct = plan.class_tiles(0)
+    assert len(ct) == len({tuple(b.sz) + (b.bflag != 0,) for b in blocks})
+    tmax = plan.tile(0)
+    for sz, face, cap in ct:
+        assert all(1 <= c <= m for c, m in zip(cap, tmax)), (sz, cap, tmax)
+    # the host pipeline's chunk plans take the tuned schedule: same bits
+    host = [np.zeros(len(u[0])) for _ in range(24)]
+    plan.rhs_host(host, u)
+    for v in range(24):
+        assert np.array_equal(host[v][mask], got[v][mask])
 
 
 def test_rhs_host_entry_matches_device(dgb, gpu):
