@@ -49,7 +49,10 @@ __global__ void __launch_bounds__(256) rk4_kernel(const Rk4Args a)
         double det = g00 * (g11 * g22 - g12 * g12) - g01 * g01 * g22 + 2.0 * g01 * g02 * g12
                    - g02 * g02 * g11;
         if (!(det > 0.0)) atomicOr(a.status, 1u);
-        const double sc = 1.0 / pow(det, 1.0 / 3.0);
+        // det^(-1/3): the reference's 1 / pow(det, 1/3) as one reciprocal cube
+        // root (within an ulp of it; the pow costs several times the rest of the node)
+        const double sc = det < 0.0 ? __longlong_as_double(0x7ff8000000000000ll)  // as pow's NaN
+                                    : rcbrt(det);
         g00 *= sc; g01 *= sc; g02 *= sc; g11 *= sc; g12 *= sc; g22 *= sc;
         det = g00 * (g11 * g22 - g12 * g12) - g01 * g01 * g22 + 2.0 * g01 * g02 * g12
             - g02 * g02 * g11;
