@@ -1092,7 +1092,7 @@ def main_drift(args, dgb):
     every = max(1, args.drift_steps // 10)
     runs, finals = {}, {}
     for name, prec in (("fp64", dgb.PREC_FP64), ("mixed", dgb.PREC_MIXED)):
-        st = dgb.Stepper(plan, uz, prec)
+        st = dgb.Stepper(plan, uz, prec, fused=True)
         ds = [torch.from_numpy(a).to(dev) for a in host]
         ptrs = [t.data_ptr() for t in ds]
         hist = [[0] + constraint_norms(dgb, plan, uz, ptrs, U, Cu, Cz, mesh.ndof, sh)]
