@@ -110,8 +110,8 @@ __device__ __forceinline__ double rel_wavelet_sq(double diff, double u, unsigned
 
 // Squared wavelets of one leaf's patch (u at its first point) into row[0..63]
 // (interior) or row[0..26] (boundary), slot order of compute_wavelets_3D.
-__device__ __forceinline__ void leaf_wavelets(const WvArgs &a, WvSmem &s, const double *u,
-                                              uint64_t n, bool bdy, double *row, int lane)
+__device__ __forceinline__ void leaf_wavelets(WvSmem &s, const double *u, uint64_t n, bool bdy,
+                                              double *row, int lane)
 {
     if (!bdy) {
         double odd[2];
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kWvWarps * 32, 4) wavelet_kernel(const WvArgs 
                 const uint64_t bb = __shfl_sync(0xffffffffu, base, b);
                 const uint64_t nb = __shfl_sync(0xffffffffu, n, b);
                 const bool db = __shfl_sync(0xffffffffu, (int)bdy, b) != 0;
-                leaf_wavelets(a, s, a.u[v] + bb, nb, db, s.sq[b], lane);
+                leaf_wavelets(s, a.u[v] + bb, nb, db, s.sq[b], lane);
             }
             if ((active >> lane) & 1u) {
                 const double *row = s.sq[lane];
