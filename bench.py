@@ -223,6 +223,19 @@ def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="b
         if dt > 0.25 * target_s or frac >= 1.0:
             break
         frac = min(1.0, frac * max(2.0, min(50.0, target_s / max(dt, 1e-3))))
+    # the same port on one core, over a sixteenth of the sample (first: the
+    # OpenMP thread count it sets is set back by the all-core runs below)
+    idx1 = cpu_sample(sub, 1.0 / 16)
+    sub1 = repack(dgb, sub, idx1)
+    u1 = [np.zeros(dgb.unzipped_size(sub1)) for _ in range(nv)]
+    dgb.synth_fill_host(sub1, u1, seed, 1e-6)
+    r1 = [np.zeros_like(u1[0]) for _ in range(nv)]
+    one_core = dict(bssn=lambda: ora.bssnrhs_blocks(r1, u1, sub1, prm, 1),
+                    ccz4=lambda: ora.ccz4rhs_blocks(r1, u1, sub1, prm, True, 1))[system]
+    t0 = time.perf_counter()
+    assert one_core() == 0
+    v1 = interior_points(sub1) * nv / (time.perf_counter() - t0)
+    del u1, r1
     pts = interior_points(sub)
     vals = []
     for _ in range(steps):
@@ -230,10 +243,11 @@ def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="b
         assert call(r, u, sub) == 0
         vals.append(pts * nv / (time.perf_counter() - t0))
     return {"value": float(np.median(vals)), "unit": "grid-pts*vars/s", "cores": cores,
-            "kind": "port",
+            "kind": "port", "value_1core": v1,
             "sample": f"{len(sub)} of {len(blocks)} blocks (stratified by size, "
                       f"{pts} interior points), FP64, OpenMP over blocks, "
-                      f"{'ccz4rhs' if system == 'ccz4' else 'bssnrhs'}"}, vals
+                      f"{'ccz4rhs' if system == 'ccz4' else 'bssnrhs'}; value_1core: "
+                      f"{len(sub1)} of those blocks on one thread"}, vals
 
 
 def main():
