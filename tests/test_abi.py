@@ -105,3 +105,36 @@ def test_generated_ccz4_algebra_up_to_date():
     out = subprocess.run([sys.executable, gen], capture_output=True, text=True, check=True).stdout
     cur = open(os.path.join(ROOT, "dendro-5.01_gb300", "csrc", "ccz4_algebra.cuh")).read()
     assert out == cur, "csrc/ccz4_algebra.cuh is stale: rerun codegen/gen_ccz4_algebra.py"
+
+
+def test_argument_checks_without_device(dgb):
+    """Entry points reject bad arguments with DGB_ERR_INVALID before touching
+    the device (no GPU needed)."""
+    import ctypes as C
+    L = dgb.lib()
+    INVALID = 1
+    # wavelet indicator: variable count, missing leaf tables, null fields
+    u, keep = dgb.ptr_array([0])
+    assert L.dgb_remesh_wavelets(u, (C.c_uint32 * 1)(0), 0, 0, 0, None, None, None, None, 0.1,
+                                 None, None, None, None) == INVALID
+    assert L.dgb_remesh_wavelets(u, (C.c_uint32 * 33)(*range(33)), 33, 0, 0, None, None, None,
+                                 None, 0.1, None, None, None, None) == INVALID
+    assert L.dgb_remesh_wavelets(u, (C.c_uint32 * 1)(0), 1, 100, 5, None, None, None, None, 0.1,
+                                 None, None, None, None) == INVALID
+    z = C.c_uint64(0)
+    assert L.dgb_remesh_wavelets(u, (C.c_uint32 * 1)(0), 1, 100, 1, C.byref(z), C.byref(z),
+                                 C.byref(z), C.byref(z), 0.1, C.byref(z), C.byref(z), None,
+                                 None) == INVALID  # field pointer 0
+    # tolerance ramp: r1 == r0 is undefined
+    corner = np.zeros((2, 3))
+    tol = np.zeros(2)
+    assert L.dgb_wavelet_tol_radial(corner.ctypes.data, 2, 1e-4, 1e-3, 1.0, 1.0, 1,
+                                    tol.ctypes.data) == INVALID
+    # null handles and arrays
+    assert L.dgb_mesh_leaf_patches(None, None, None, None, None, None) == INVALID
+    assert L.dgb_stepper_create_ex(None, None, 0, 0, C.byref(C.c_void_p())) == INVALID
+    assert L.dgb_stepper_device_bytes(None, C.byref(z)) == INVALID
+    assert L.dgb_plan_class_tiles(None, 0, None, 0, C.byref(C.c_size_t())) == INVALID
+    assert L.dgb_bssn_rhs_host(None, None, None, 0) == INVALID
+    assert L.dgb_ccz4_rhs_host(None, None, None, None, 0) == INVALID
+    assert L.dgb_physical_constraints_host(None, None, None) == INVALID
