@@ -10,6 +10,8 @@
 // below 2^63; it is shifted back to 53 bits with round-half-even on the
 // dropped bits.  Zero keeps its bits; subnormal, infinite/NaN inputs and
 // results that could leave the normal range take the hardware multiply.
+// Products by powers of two (2^K, the 4th-order stencils' 4, 8, 16 and the
+// algebra's 0.5, 2, 0.25) are an exponent shift (dgb_mul_pow2).
 #pragma once
 #include <stdint.h>
 #include <string.h>
@@ -65,6 +67,43 @@ __device__ __noinline__ double dgb_mul_hw(double x)
 #else
 #define DGB_XM_SLOW(C, x) ((double)(C) * (x))
 #endif
+
+// 2^K as a double, exact for |K| < 31
+template <int K>
+struct dgb_pow2 {
+    static constexpr double value = K >= 0 ? (double)(1u << (K >= 0 ? K : 0))
+                                           : 1.0 / (double)(1u << (K < 0 ? -K : 0));
+};
+
+#if defined(__CUDA_ARCH__)
+template <int K>
+__device__ __noinline__ double dgb_mul_hw_pow2(double x)
+{
+    return __dmul_rn(dgb_pow2<K>::value, x);
+}
+#define DGB_XM_SLOW_POW2(K, x) dgb_mul_hw_pow2<K>(x)
+#else
+#define DGB_XM_SLOW_POW2(K, x) (dgb_pow2<K>::value * (x))
+#endif
+
+// RN(2^K * x) for a compile-time K, 1 <= |K| <= 8: exact, an exponent shift
+// for normal x whose product stays normal; +-0 keeps its bits; subnormal,
+// infinite/NaN inputs and products that would leave the normal range take
+// the hardware multiply.
+template <int K>
+DGB_XM_HD double dgb_mul_pow2(double x)
+{
+    static_assert(K != 0 && K >= -8 && K <= 8, "small powers of two only");
+    const uint64_t b = dgb_dbits(x);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    const bool fast = K > 0 ? (e != 0u && e < 0x7FFu - (uint32_t)(K > 0 ? K : 0))
+                            : (e > (uint32_t)(K < 0 ? -K : 0) && e != 0x7FFu);
+    if (!fast) {
+        if ((b << 1) == 0ull) return x;  // 2^K * (+-0) = +-0
+        return DGB_XM_SLOW_POW2(K, x);
+    }
+    return dgb_bitsd(b + ((uint64_t)(int64_t)K << 52));
+}
 
 // 2 * x: exact, an exponent increment for normal x; +-0 stays +-0.
 DGB_XM_HD double dgb_mul2(double x)

@@ -75,13 +75,15 @@ namespace {
 DGB_HD double selftest_input(uint64_t seed, uint64_t i)
 {
     // the edge cases first: +-0, subnormals, the normal range's ends, +-inf, NaN
-    const uint64_t special[12] = {0x0000000000000000ull, 0x8000000000000000ull,
+    const uint64_t special[16] = {0x0000000000000000ull, 0x8000000000000000ull,
                                   0x0000000000000001ull, 0x800FFFFFFFFFFFFFull,
                                   0x0010000000000000ull, 0x7FEFFFFFFFFFFFFFull,
                                   0x7FF0000000000000ull, 0xFFF0000000000000ull,
                                   0x7FF8000000000000ull, 0x3FF0000000000000ull,
-                                  0xBFF0000000000001ull, 0x7F50000000000000ull};
-    if (i < 12) return dgb_bitsd(special[i]);
+                                  0xBFF0000000000001ull, 0x7F50000000000000ull,
+                                  0x0020000000000000ull, 0x803FFFFFFFFFFFFFull,
+                                  0x7FDFFFFFFFFFFFFFull, 0xFF7FFFFFFFFFFFFFull};
+    if (i < 16) return dgb_bitsd(special[i]);
     uint64_t b = dgb_mix64(seed ^ dgb_mix64(i));
     const uint64_t r = dgb_mix64(b);
     switch (i & 3u) {
@@ -107,6 +109,21 @@ DGB_HD uint64_t selftest_one(double x)
     return (ba != bc && !(nan_a && nan_c)) ? 1u : 0u;
 }
 
+template <int K>
+DGB_HD uint64_t selftest_pow2(double x)
+{
+#if defined(__CUDA_ARCH__)
+    const double a = __dmul_rn(dgb_pow2<K>::value, x);
+#else
+    const double a = dgb_pow2<K>::value * x;
+#endif
+    const double c = dgb_mul_pow2<K>(x);
+    const uint64_t ba = dgb_dbits(a), bc = dgb_dbits(c);
+    const bool nan_a = (ba & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+    const bool nan_c = (bc & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+    return (ba != bc && !(nan_a && nan_c)) ? 1u : 0u;
+}
+
 DGB_HD uint64_t selftest_all(double x)
 {
     uint64_t bad = selftest_one<3>(x) + selftest_one<5>(x) + selftest_one<6>(x)
@@ -121,6 +138,8 @@ DGB_HD uint64_t selftest_all(double x)
 #endif
     const double t2 = dgb_mul2(x);
     if (dgb_dbits(two) != dgb_dbits(t2) && two == two) bad++;
+    bad += selftest_pow2<-2>(x) + selftest_pow2<-1>(x) + selftest_pow2<1>(x)
+         + selftest_pow2<2>(x) + selftest_pow2<3>(x) + selftest_pow2<4>(x);
     return bad;
 }
 

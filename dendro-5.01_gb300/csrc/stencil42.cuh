@@ -1,7 +1,7 @@
 // 4th-order finite-difference stencils on staged (shared-memory) lines, in
 // the reference's rounding order: one rounding per operation, left to
-// right, products by 2, 4, 8, 16 exact and the other integer tap products
-// formed exactly on the integer pipes (exact_mul.cuh).  `c` points at the
+// right, products by 2, 4, 8, 16 (exponent shifts) and the other integer tap
+// products formed exactly on the integer pipes (exact_mul.cuh).  `c` points at the
 // value of the current point, `s` is the stride along the axis, `pos` the
 // point's index along an axis of n points (interior [3, n-3)), lo / hi the
 // block's domain-boundary flags on that axis.
@@ -44,16 +44,16 @@ __device__ __forceinline__ Ax4 ax4(double h)
 
 __device__ __forceinline__ double d1_42(const double *u, int s, double c12)
 {
-    double t = __dsub_rn(u[-2 * s], 8.0 * u[-s]);
-    t = __dadd_rn(t, 8.0 * u[s]);
+    double t = __dsub_rn(u[-2 * s], dgb_mul_pow2<3>(u[-s]));
+    t = __dadd_rn(t, dgb_mul_pow2<3>(u[s]));
     t = __dsub_rn(t, u[2 * s]);
     return __dmul_rn(t, c12);
 }
 __device__ __forceinline__ double d2_42(const double *u, int s, double c12sq)
 {
-    double t = __dadd_rn(-u[-2 * s], 16.0 * u[-s]);
+    double t = __dadd_rn(-u[-2 * s], dgb_mul_pow2<4>(u[-s]));
     t = __dsub_rn(t, dgb_mul_const<30>(u[0]));
-    t = __dadd_rn(t, 16.0 * u[s]);
+    t = __dadd_rn(t, dgb_mul_pow2<4>(u[s]));
     t = __dsub_rn(t, u[2 * s]);
     return __dmul_rn(t, c12sq);
 }
@@ -61,13 +61,13 @@ __device__ __forceinline__ double d2_42(const double *u, int s, double c12sq)
 // (-3 u0 + 4 u1 - u2) * (0.5/h): the one-sided first derivative, forward
 __device__ __forceinline__ double fwd3(const double *c, int s, double half)
 {
-    const double t = __dadd_rn(-dgb_mul_const<3>(c[0]), 4.0 * c[s]);
+    const double t = __dadd_rn(-dgb_mul_const<3>(c[0]), dgb_mul_pow2<2>(c[s]));
     return __dmul_rn(__dsub_rn(t, c[2 * s]), half);
 }
 // (u_-2 - 4 u_-1 + 3 u0) * (0.5/h): backward
 __device__ __forceinline__ double bwd3(const double *c, int s, double half)
 {
-    const double t = __dsub_rn(c[-2 * s], 4.0 * c[-s]);
+    const double t = __dsub_rn(c[-2 * s], dgb_mul_pow2<2>(c[-s]));
     return __dmul_rn(__dadd_rn(t, dgb_mul_const<3>(c[0])), half);
 }
 // (-u_-1 + u1) * (0.5/h)
@@ -89,18 +89,18 @@ __device__ __forceinline__ double d2_42_at(const double *c, int s, int pos, int 
                                            const Ax4 &a)
 {
     if (lo && pos == 3) {
-        double t = __dsub_rn(2.0 * c[0], dgb_mul_const<5>(c[s]));
-        t = __dadd_rn(t, 4.0 * c[2 * s]);
+        double t = __dsub_rn(dgb_mul2(c[0]), dgb_mul_const<5>(c[s]));
+        t = __dadd_rn(t, dgb_mul_pow2<2>(c[2 * s]));
         return __dmul_rn(__dsub_rn(t, c[3 * s]), a.sq);
     }
     if ((lo && pos == 4) || (hi && pos == n - 5)) {
-        const double t = __dsub_rn(c[-s], 2.0 * c[0]);
+        const double t = __dsub_rn(c[-s], dgb_mul2(c[0]));
         return __dmul_rn(__dadd_rn(t, c[s]), a.sq);
     }
     if (hi && pos == n - 4) {
-        double t = __dadd_rn(-c[-3 * s], 4.0 * c[-2 * s]);
+        double t = __dadd_rn(-c[-3 * s], dgb_mul_pow2<2>(c[-2 * s]));
         t = __dsub_rn(t, dgb_mul_const<5>(c[-s]));
-        return __dmul_rn(__dadd_rn(t, 2.0 * c[0]), a.sq);
+        return __dmul_rn(__dadd_rn(t, dgb_mul2(c[0])), a.sq);
     }
     return d2_42(c, s, a.c12sq);
 }
