@@ -10,8 +10,8 @@
 // below 2^63; it is shifted back to 53 bits with round-half-even on the
 // dropped bits.  Zero keeps its bits; subnormal, infinite/NaN inputs and
 // results that could leave the normal range take the hardware multiply.
-// Products by powers of two (2^K, the 4th-order stencils' 4, 8, 16 and the
-// algebra's 0.5, 2, 0.25) are an exponent shift (dgb_mul_pow2).
+// Products by powers of two (2^K: the 4th-order stencils' 4, 8, 16) are an
+// exponent shift (dgb_mul_pow2).
 #pragma once
 #include <stdint.h>
 #include <string.h>
