@@ -188,6 +188,33 @@ def cpu_sample(blocks, fraction):
     return sorted(idx)
 
 
+def time_host_entry(call, steps):
+    """Seconds per call of a synchronous host-array entry: two warm-up calls
+    (the first builds the plan's pipeline and staging), then the median of
+    min(max(steps, 3), 5) timed calls."""
+    call()
+    call()
+    ts = []
+    for _ in range(min(max(steps, 3), 5)):
+        t0 = time.perf_counter()
+        call()
+        ts.append(time.perf_counter() - t0)
+    return float(np.median(ts))
+
+
+def e2e_host_arrays(dgb, count, n, pageable):
+    """The host arrays of an e2e run: page-locked memory from dgb_host_alloc
+    (the host-array entries upload fields there without their staging copy),
+    or pageable numpy arrays; page-locked falls back to pageable if the host
+    cannot lock that much memory.  Returns (arrays, kind)."""
+    if not pageable:
+        try:
+            return [dgb.host_array(n) for _ in range(count)], "page-locked (dgb_host_alloc)"
+        except RuntimeError:
+            pass
+    return [np.zeros(n) for _ in range(count)], "pageable"
+
+
 def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="bssn"):
     """Times the oracle port of the reference CPU path on all host cores
     (system "bssn": bssnrhs; "ccz4": ccz4rhs with its 25 variables)."""
@@ -279,6 +306,9 @@ def main():
     ap.add_argument("--wavelet-vars", default="0",
                     help="wavelet_octree: comma-separated refinement variable ids")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-pageable", action="store_true",
+                    help="e2e of the host-array entries with pageable numpy arrays (through "
+                         "the library's staging copy) instead of dgb_host_alloc memory")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the tile schedule by timing (always on for octree_rk4)")
@@ -390,20 +420,17 @@ def main():
     if not args.no_e2e:
         del du, dr
         torch.cuda.empty_cache()
-        hu = [np.empty(n) for _ in range(24)]
+        hu, kind = e2e_host_arrays(dgb, 24, n, args.e2e_pageable)
         dgb.synth_fill_host(blocks, hu, seed, 1e-6)
-        hr = [np.zeros(n) for _ in range(24)]
-        plan.rhs_host(hr, hu, prec)  # warm-up: allocates the plan's staging
-        t0 = time.perf_counter()
-        for _ in range(max(1, min(args.steps, 3))):
-            plan.rhs_host(hr, hu, prec)
-        e2e_s = (time.perf_counter() - t0) / max(1, min(args.steps, 3))
+        hr, _ = e2e_host_arrays(dgb, 24, n, args.e2e_pageable)
+        e2e_s = time_host_entry(lambda: plan.rhs_host(hr, hu, prec), args.steps)
         e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
-               "h2d_bytes_per_step": 24 * n * 8, "d2h_bytes_per_step": 24 * n * 8,
-               "ms_per_step": e2e_s * 1e3,
+               "h2d_bytes_per_step": 24 * n * 8, "d2h_bytes_per_step": 24 * npts * 8,
+               "ms_per_step": e2e_s * 1e3, "host_arrays": kind,
                "path": "dgb_bssn_rhs_host (reference calling convention, host arrays): chunked "
-                       "pipeline, host threads into pinned staging, uploads and downloads "
-                       "overlapping the kernel, interior points written back"}
+                       "pipeline, uploads (from the caller's arrays when page-locked, else "
+                       "through pinned staging) and downloads overlapping the kernel, interior "
+                       "points written back by host threads"}
         del hu, hr
 
     cpu = None
@@ -497,21 +524,16 @@ def main_ccz4(args, dgb, rank, world, local):
     if not args.no_e2e:
         del du, dr
         torch.cuda.empty_cache()
-        hu = [np.empty(n) for _ in range(25)]
+        hu, kind = e2e_host_arrays(dgb, 25, n, args.e2e_pageable)
         dgb.synth_fill_host(blocks, hu, seed, 1e-6)
-        hr = [np.zeros(n) for _ in range(25)]
-        plan.ccz4_rhs_host(prm, hr, hu, prec)  # warm-up: allocates the plan's staging
-        k = max(1, min(args.steps, 3))
-        t0 = time.perf_counter()
-        for _ in range(k):
-            plan.ccz4_rhs_host(prm, hr, hu, prec)
-        e2e_s = (time.perf_counter() - t0) / k
+        hr, _ = e2e_host_arrays(dgb, 25, n, args.e2e_pageable)
+        e2e_s = time_host_entry(lambda: plan.ccz4_rhs_host(prm, hr, hu, prec), args.steps)
         e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
-               "h2d_bytes_per_step": 25 * n * 8, "d2h_bytes_per_step": 25 * n * 8,
-               "ms_per_step": e2e_s * 1e3,
-               "path": "dgb_ccz4_rhs_host (host arrays): chunked pipeline, host threads into "
-                       "pinned staging, uploads and downloads overlapping the kernel, interior "
-                       "points written back"}
+               "h2d_bytes_per_step": 25 * n * 8, "d2h_bytes_per_step": 25 * npts * 8,
+               "ms_per_step": e2e_s * 1e3, "host_arrays": kind,
+               "path": "dgb_ccz4_rhs_host (host arrays): chunked pipeline, uploads (from the "
+                       "caller's arrays when page-locked, else through pinned staging) and "
+                       "downloads overlapping the kernel, interior points written back"}
         del hu, hr
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -627,21 +649,17 @@ def main_constraints(args, dgb, rank, world, local):
     if not args.no_e2e:
         del du, dc
         torch.cuda.empty_cache()
-        hu = [np.empty(n) for _ in range(24)]
+        hu, kind = e2e_host_arrays(dgb, 24, n, args.e2e_pageable)
         dgb.synth_fill_host(blocks, hu, seed, 1e-6)
-        hc = [np.zeros(n) for _ in range(6)]
-        plan.physical_constraints_host(hc, hu)  # warm-up: builds the plan's pipeline
-        k = max(1, min(args.steps, 3))
-        t0 = time.perf_counter()
-        for _ in range(k):
-            plan.physical_constraints_host(hc, hu)
-        e2e_s = (time.perf_counter() - t0) / k
+        hc, _ = e2e_host_arrays(dgb, 6, n, args.e2e_pageable)
+        e2e_s = time_host_entry(lambda: plan.physical_constraints_host(hc, hu), args.steps)
         e2e = {"value": npts / e2e_s, "unit": "grid-pts/s",
                "h2d_bytes_per_step": 24 * n * 8, "d2h_bytes_per_step": 6 * npts * 8,
-               "ms_per_step": e2e_s * 1e3,
-               "path": "dgb_physical_constraints_host (host arrays): chunked pipeline, host "
-                       "threads into pinned staging, uploads, interior rows packed on the "
-                       "device and downloaded, written back by host threads"}
+               "ms_per_step": e2e_s * 1e3, "host_arrays": kind,
+               "path": "dgb_physical_constraints_host (host arrays): chunked pipeline, uploads "
+                       "(from the caller's arrays when page-locked, else through pinned "
+                       "staging), interior rows packed on the device and downloaded, written "
+                       "back by host threads"}
         del hu, hc
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -92,6 +92,8 @@ void host_scatter_rows(double *const *rhs, const double *src, size_t islot, int 
 //   -> scatter of the interior rows (host)
 // with three device slots, two pinned staging buffers each way and separate
 // upload / compute / download streams, so transfers overlap the kernel.
+// Input fields in dgb_host_alloc memory skip the gather: the upload reads
+// the caller's page-locked arrays directly.
 // Only interior points are written back, so the caller's rhs padding is
 // untouched without uploading rhs.
 struct HostPipe {
@@ -360,9 +362,56 @@ dgb_status dgb::run_rhs_gather(dgb_plan *p, double *const *k, const double *cons
     return DGB_OK;
 }
 
+// Page-locked allocations made by dgb_host_alloc: start address -> bytes.
+// The host-array entries upload fields lying inside one of them directly.
+static std::mutex g_host_mu;
+static std::map<uintptr_t, size_t> g_host_allocs;
+
+static bool in_host_alloc(const void *p, size_t bytes)
+{
+    const uintptr_t a = (uintptr_t)p;
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    auto it = g_host_allocs.upper_bound(a);
+    if (it == g_host_allocs.begin()) return false;
+    --it;
+    return a >= it->first && a - it->first <= it->second && bytes <= it->second - (a - it->first);
+}
+
 extern "C" {
 
 int dgb_version(void) { return 1; }
+
+dgb_status dgb_host_alloc(size_t bytes, void **ptr)
+{
+    if (!ptr || bytes == 0) return DGB_ERR_INVALID;
+    *ptr = nullptr;
+    void *q = nullptr;
+    if (cudaMallocHost(&q, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("cudaMallocHost failed");
+        return DGB_ERR_ALLOC;
+    }
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    g_host_allocs[(uintptr_t)q] = bytes;
+    *ptr = q;
+    return DGB_OK;
+}
+
+dgb_status dgb_host_free(void *ptr)
+{
+    if (!ptr) return DGB_OK;
+    {
+        std::lock_guard<std::mutex> lock(g_host_mu);
+        auto it = g_host_allocs.find((uintptr_t)ptr);
+        if (it == g_host_allocs.end()) {
+            set_error("dgb_host_free: not an allocation of dgb_host_alloc");
+            return DGB_ERR_INVALID;
+        }
+        g_host_allocs.erase(it);
+    }
+    DGB_CUDA(cudaFreeHost(ptr));
+    return DGB_OK;
+}
 
 const char *dgb_last_error(void) { return g_err.c_str(); }
 
@@ -946,8 +995,8 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
 // The pipeline over the chunks for nv fields; compute(sub-plan, rhs, u, stream)
 // runs the kernel of one chunk.
 template <class Compute>
-dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int nv,
-                    Compute compute, int nv_out = -1)
+dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *u, int nv,
+                          Compute compute, int nv_out)
 {
     // nv fields in; nv_out (default nv) fields out
     if (nv_out < 0) nv_out = nv;
@@ -959,6 +1008,18 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
         double *base = h->d_slots + (size_t)(3 * kind + (int)(c % 3)) * slot;
         for (int v = 0; v < NV4; v++) out[v] = base + (size_t)v * h->slot_pts;
     };
+    // input fields inside dgb_host_alloc memory are uploaded straight from
+    // the caller's arrays (no gather into the staging buffers)
+    bool direct = nch > 0;
+    {
+        uint64_t lo = UINT64_MAX, hi = 0;
+        for (long c = 0; c < nch; c++) {
+            lo = std::min(lo, h->start[c]);
+            hi = std::max(hi, h->start[c] + h->span[c]);
+        }
+        for (int v = 0; v < nv && direct; v++)
+            direct = in_host_alloc(u[v] + lo, (size_t)(hi - lo) * sizeof(double));
+    }
     for (long step = 0; step < nch + 3; step++) {
         const long c = step - 1, d = step - 2, a = step, e = step - 3;
         if (c >= 0 && c < nch) {  // compute chunk c once its upload is done
@@ -986,16 +1047,20 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
                                          cudaMemcpyDeviceToHost, h->s_d2h));
             DGB_CUDA(cudaEventRecord(h->ev_d2h[d], h->s_d2h));
         }
-        if (a < nch) {  // gather and upload chunk a
-            if (a >= 2) DGB_CUDA(cudaEventSynchronize(h->ev_h2d[a - 2]));
-            host_gather(h->h_in[a % 2], h->slot_pts, u, nv, h->start[a], h->span[a]);
+        if (a < nch) {  // gather (unless direct) and upload chunk a
+            if (!direct) {
+                if (a >= 2) DGB_CUDA(cudaEventSynchronize(h->ev_h2d[a - 2]));
+                host_gather(h->h_in[a % 2], h->slot_pts, u, nv, h->start[a], h->span[a]);
+            }
             if (a >= 3) DGB_CUDA(cudaStreamWaitEvent(h->s_h2d, h->ev_comp[a - 3], 0));
             double *du[NV4];
             ptrs(0, a, du);
-            for (int v = 0; v < nv; v++)
-                DGB_CUDA(cudaMemcpyAsync(du[v], h->h_in[a % 2] + (size_t)v * h->slot_pts,
-                                         h->span[a] * sizeof(double), cudaMemcpyHostToDevice,
-                                         h->s_h2d));
+            for (int v = 0; v < nv; v++) {
+                const double *src = direct ? u[v] + h->start[a]
+                                           : h->h_in[a % 2] + (size_t)v * h->slot_pts;
+                DGB_CUDA(cudaMemcpyAsync(du[v], src, h->span[a] * sizeof(double),
+                                         cudaMemcpyHostToDevice, h->s_h2d));
+            }
             DGB_CUDA(cudaEventRecord(h->ev_h2d[a], h->s_h2d));
         }
         if (e >= 0 && e < nch) {  // scatter chunk e's interior rows back
@@ -1006,6 +1071,22 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
         }
     }
     return DGB_OK;
+}
+
+// run_pipe_steps, and on an error a wait for the copies still in flight, so
+// that no transfer touches the caller's arrays after the call returns.
+template <class Compute>
+dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int nv,
+                    Compute compute, int nv_out = -1)
+{
+    const dgb_status s = run_pipe_steps(p, rhs, u, nv, compute, nv_out);
+    if (s != DGB_OK) {
+        HostPipe *h = p->pipe;
+        cudaStreamSynchronize(h->s_h2d);
+        cudaStreamSynchronize(h->s_comp);
+        cudaStreamSynchronize(h->s_d2h);
+    }
+    return s;
 }
 
 // The plan's pipeline, built at first use; the sub-plans take the parent's

@@ -112,6 +112,8 @@ _SIGS = {
     "dgb_plan_interior_points": (C.c_uint64, [C.c_void_p]),
     "dgb_bssn_rhs": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int, C.c_void_p]),
     "dgb_bssn_rhs_host": (C.c_int, [C.c_void_p, PtrArr, PtrArr, C.c_int]),
+    "dgb_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "dgb_host_free": (C.c_int, [C.c_void_p]),
     "dgb_bssnrhs_block_host": (C.c_int, [PtrArr, PtrArr, C.c_uint64, C.POINTER(C.c_double),
                                          C.POINTER(C.c_double), C.POINTER(C.c_uint32),
                                          C.c_uint32, C.POINTER(BssnParams), C.c_int]),
@@ -221,6 +223,21 @@ def ptr_array(ptrs):
 
 def host_ptrs(arrays):
     return ptr_array([a.ctypes.data for a in arrays])
+
+
+def host_array(n, dtype=np.float64):
+    """A zeroed numpy array of n elements in page-locked memory from
+    dgb_host_alloc; the host-array entries upload such fields without the
+    staging copy.  The memory is freed when the last view of it is gone."""
+    import weakref
+    dt = np.dtype(dtype)
+    p = C.c_void_p()
+    check(lib().dgb_host_alloc(max(1, n) * dt.itemsize, C.byref(p)), "dgb_host_alloc")
+    buf = (C.c_char * (max(1, n) * dt.itemsize)).from_address(p.value)
+    weakref.finalize(buf, lib().dgb_host_free, p.value)
+    a = np.frombuffer(buf, dtype=dt, count=n)
+    a[...] = 0
+    return a
 
 
 def synth_blocks(which, seed=0):

@@ -93,9 +93,20 @@ dgb_status dgb_bssn_rhs(dgb_plan *plan, double *const *rhs, const double *const 
                         int precision, void *stream);
 
 /* Same call with HOST arrays (the reference's calling convention): copies the
- * fields in, computes, copies the interior of rhs out, synchronously. */
+ * fields in, computes, copies the interior of rhs out, synchronously.
+ * Fields that lie in memory from dgb_host_alloc are uploaded straight from
+ * the caller's arrays; others go through the library's pinned staging. */
 dgb_status dgb_bssn_rhs_host(dgb_plan *plan, double *const *rhs, const double *const *u,
                              int precision);
+
+/* Page-locked host memory for the caller's unzipped field arrays (the
+ * reference allocates them with new[] in Mesh::createUnZippedVector,
+ * include/mesh.tcc:245-262).  The host-array entries (dgb_bssn_rhs_host,
+ * dgb_ccz4_rhs_host, dgb_physical_constraints_host) upload input fields that
+ * lie entirely inside one such allocation without the host-side staging
+ * copy, which halves the host memory traffic of the upload.  Thread-safe. */
+dgb_status dgb_host_alloc(size_t bytes, void **ptr);
+dgb_status dgb_host_free(void *ptr);
 
 /* One block, host arrays: replaces bssnrhs(double**, const double**,
  * const unsigned& offset, const double* ptmin, const double* ptmax,

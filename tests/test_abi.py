@@ -138,3 +138,9 @@ def test_argument_checks_without_device(dgb):
     assert L.dgb_bssn_rhs_host(None, None, None, 0) == INVALID
     assert L.dgb_ccz4_rhs_host(None, None, None, None, 0) == INVALID
     assert L.dgb_physical_constraints_host(None, None, None) == INVALID
+    # page-locked host memory: sizes, null pointers, foreign pointers
+    assert L.dgb_host_alloc(0, C.byref(C.c_void_p())) == INVALID
+    assert L.dgb_host_alloc(8, None) == INVALID
+    assert L.dgb_host_free(None) == 0
+    foreign = np.zeros(4)
+    assert L.dgb_host_free(C.c_void_p(foreign.ctypes.data)) == INVALID

@@ -122,6 +122,34 @@ def test_rhs_host_pipeline_many_chunks(dgb, gpu, precision, monkeypatch):
     plan.close()
 
 
+@pytest.mark.parametrize("all_pinned", [True, False])
+def test_rhs_host_pipeline_pinned_inputs(dgb, gpu, all_pinned, monkeypatch):
+    """Fields in dgb_host_alloc memory are uploaded straight from the caller's
+    arrays (all 24 pinned), or, with one field pageable, through the staging
+    copy: the same bits as the device entry either way, padding untouched."""
+    torch = gpu
+    monkeypatch.setenv("DGB_HOST_CHUNK_PTS", "30000")
+    allb = dgb.synth_blocks(2, SEED2)
+    blocks = repack(dgb, allb, sample_uneven(allb, (6, 3, 2, 0)))
+    u = host_fields(dgb, blocks, SEED2)
+    n = len(u[0])
+    plan = dgb.Plan(blocks, dgb.default_params(0.1))
+    dev = run_device(dgb, torch, plan, u, rhs_init=[np.full(n, 7.0)] * 24)
+    pu = []
+    for v in range(24):
+        a = dgb.host_array(n) if (all_pinned or v != 5) else np.empty(n)
+        a[:] = u[v]
+        pu.append(a)
+    for rep in range(2):
+        host = [dgb.host_array(n) for _ in range(24)]
+        for a in host:
+            a[:] = 7.0
+        plan.rhs_host(host, pu)
+        for v in range(24):
+            assert np.array_equal(dev[v], host[v]), (rep, v)
+    plan.close()
+
+
 def test_block_entry_matches_oracle(dgb, gpu, oracle):
     """dgb_bssnrhs_block_host: the bssnrhs(...) drop-in for one block at an offset."""
     allb = dgb.synth_blocks(2, SEED2)
