@@ -174,10 +174,11 @@ def test_ccz4_mixed_precision(dgb, gpu, oracle, which):
         assert np.all(err <= FP64_TOL), dict(zip(dgb.CCZ4_VAR_NAMES, err))
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_ccz4_host_pipeline_many_chunks(dgb, gpu, precision, monkeypatch):
+@pytest.mark.parametrize("precision,pinned", [("fp64", False), ("mixed", False), ("fp64", True)])
+def test_ccz4_host_pipeline_many_chunks(dgb, gpu, precision, pinned, monkeypatch):
     """dgb_ccz4_rhs_host over many chunks, block list not in offset order and
-    boundary blocks included: the device entry's bits, padding untouched."""
+    boundary blocks included: the device entry's bits, padding untouched;
+    pinned: the fields in dgb_host_alloc memory (uploaded without staging)."""
     torch = gpu
     monkeypatch.setenv("DGB_HOST_CHUNK_PTS", "30000")
     prec = dgb.PREC_MIXED if precision == "mixed" else dgb.PREC_FP64
@@ -197,6 +198,11 @@ def test_ccz4_host_pipeline_many_chunks(dgb, gpu, precision, monkeypatch):
     plan.ccz4_rhs(prm, [t.data_ptr() for t in dr], [t.data_ptr() for t in du], prec)
     torch.cuda.synchronize()
     dev = [t.cpu().numpy() for t in dr]
+    if pinned:
+        pu = [dgb.host_array(n) for _ in range(25)]
+        for v in range(25):
+            pu[v][:] = u[v]
+        u = pu
     for rep in range(2):  # the second call reuses the pipeline
         host = [np.full(n, 7.0) for _ in range(25)]
         plan.ccz4_rhs_host(prm, host, u, prec)

@@ -160,10 +160,12 @@ def test_constraint_pipeline_on_mesh(dgb, gpu, oracle):
     m.close()
 
 
-def test_constraints_host_pipeline_many_chunks(dgb, gpu, monkeypatch):
+@pytest.mark.parametrize("pinned", [False, True])
+def test_constraints_host_pipeline_many_chunks(dgb, gpu, pinned, monkeypatch):
     """dgb_physical_constraints_host over many chunks (24 fields in, 6 out),
     block list not in offset order, boundary blocks included: the device
-    entry's bits, padding of the outputs untouched."""
+    entry's bits, padding of the outputs untouched; pinned: inputs and
+    outputs in dgb_host_alloc memory (uploaded without staging)."""
     torch = gpu
     monkeypatch.setenv("DGB_HOST_CHUNK_PTS", "30000")
     allb = dgb.synth_blocks(2, SEED2)
@@ -175,8 +177,15 @@ def test_constraints_host_pipeline_many_chunks(dgb, gpu, monkeypatch):
     plan = dgb.Plan(dgb.blocks_array(rows[::-1]), dgb.default_params(0.1))
     dev = gpu_constraints(dgb, torch, plan, u)
     n = len(u[0])
+    if pinned:
+        pu = [dgb.host_array(n) for _ in range(24)]
+        for v in range(24):
+            pu[v][:] = u[v]
+        u = pu
     for rep in range(2):  # the second call reuses the pipeline
-        host = [np.full(n, 7.0) for _ in range(6)]
+        host = [dgb.host_array(n) if pinned else np.empty(n) for _ in range(6)]
+        for h in host:
+            h[:] = 7.0
         plan.physical_constraints_host(host, u)
         for c in range(6):
             assert np.array_equal(dev[c], host[c]), (rep, dgb.CONSTRAINT_NAMES[c])
