@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <map>
@@ -113,6 +114,14 @@ struct HostPipe {
     IRow *d_rows = nullptr;
     double *d_packed = nullptr;         // 3 packed slots, NV4 * islot each
     double *h_in[2] = {nullptr, nullptr}, *h_out[2] = {nullptr, nullptr};  // pinned
+    // upload mode per entry kind (nv * 64 + nv_out) for inputs in dgb_host_alloc
+    // memory: the last wall time of a call through the staging (0) and of a
+    // direct call (1), and the number of such calls
+    struct UploadStats {
+        double ms[2] = {0.0, 0.0};
+        uint64_t calls = 0;
+    };
+    std::map<int, UploadStats> upload;
     cudaStream_t s_h2d = nullptr, s_comp = nullptr, s_d2h = nullptr;
     std::vector<cudaEvent_t> ev_h2d, ev_comp, ev_d2h;
 };
@@ -996,10 +1005,9 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
 // runs the kernel of one chunk.
 template <class Compute>
 dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *u, int nv,
-                          Compute compute, int nv_out)
+                          Compute compute, int nv_out, bool direct)
 {
-    // nv fields in; nv_out (default nv) fields out
-    if (nv_out < 0) nv_out = nv;
+    // nv fields in, nv_out fields out; direct: upload from the caller's arrays
     HostPipe *h = p->pipe;
     const long nch = (long)h->members.size();
     const size_t slot = (size_t)NV4 * h->slot_pts;
@@ -1008,18 +1016,6 @@ dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *
         double *base = h->d_slots + (size_t)(3 * kind + (int)(c % 3)) * slot;
         for (int v = 0; v < NV4; v++) out[v] = base + (size_t)v * h->slot_pts;
     };
-    // input fields inside dgb_host_alloc memory are uploaded straight from
-    // the caller's arrays (no gather into the staging buffers)
-    bool direct = nch > 0;
-    {
-        uint64_t lo = UINT64_MAX, hi = 0;
-        for (long c = 0; c < nch; c++) {
-            lo = std::min(lo, h->start[c]);
-            hi = std::max(hi, h->start[c] + h->span[c]);
-        }
-        for (int v = 0; v < nv && direct; v++)
-            direct = in_host_alloc(u[v] + lo, (size_t)(hi - lo) * sizeof(double));
-    }
     for (long step = 0; step < nch + 3; step++) {
         const long c = step - 1, d = step - 2, a = step, e = step - 3;
         if (c >= 0 && c < nch) {  // compute chunk c once its upload is done
@@ -1073,18 +1069,68 @@ dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *
     return DGB_OK;
 }
 
-// run_pipe_steps, and on an error a wait for the copies still in flight, so
-// that no transfer touches the caller's arrays after the call returns.
+// Whether every input field lies inside dgb_host_alloc memory over the
+// pipeline's extent, so that the upload can read the caller's arrays.
+bool inputs_page_locked(const HostPipe *h, const double *const *u, int nv)
+{
+    if (h->members.empty()) return false;
+    uint64_t lo = UINT64_MAX, hi = 0;
+    for (size_t c = 0; c < h->members.size(); c++) {
+        lo = std::min(lo, h->start[c]);
+        hi = std::max(hi, h->start[c] + h->span[c]);
+    }
+    for (int v = 0; v < nv; v++)
+        if (!in_host_alloc(u[v] + lo, (size_t)(hi - lo) * sizeof(double))) return false;
+    return true;
+}
+
+// The upload mode of a call whose inputs are page-locked.  Reading the
+// caller's arrays saves the host the gather, but the DMA rate from a large
+// page-locked region has been seen to vary between hosts and to drift within
+// a process, while the staging copy's does not; so the plan times both: the
+// first two calls go direct (the first one untimed: it warms up), the third
+// through the staging, later calls take the mode whose last call was faster
+// and every eighth call re-times the other.  DGB_HOST_UPLOAD=direct|staged
+// fixes the mode.
+bool choose_direct(HostPipe *h, int key)
+{
+    if (const char *env = getenv("DGB_HOST_UPLOAD")) {
+        if (!strcmp(env, "direct")) return true;
+        if (!strcmp(env, "staged")) return false;
+    }
+    const HostPipe::UploadStats &st = h->upload[key];
+    if (st.calls < 2) return true;
+    if (st.ms[0] == 0.0) return false;
+    const bool best = st.ms[1] <= st.ms[0];
+    return (st.calls % 8 == 7) ? !best : best;
+}
+
+// run_pipe_steps in the chosen upload mode, timed for the mode choice; on an
+// error, a wait for the copies still in flight, so that no transfer touches
+// the caller's arrays after the call returns.
 template <class Compute>
 dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int nv,
                     Compute compute, int nv_out = -1)
 {
-    const dgb_status s = run_pipe_steps(p, rhs, u, nv, compute, nv_out);
+    if (nv_out < 0) nv_out = nv;
+    HostPipe *h = p->pipe;
+    const bool locked = inputs_page_locked(h, u, nv);
+    const int key = nv * 64 + nv_out;
+    const bool direct = locked && choose_direct(h, key);
+    const auto t0 = std::chrono::steady_clock::now();
+    const dgb_status s = run_pipe_steps(p, rhs, u, nv, compute, nv_out, direct);
     if (s != DGB_OK) {
-        HostPipe *h = p->pipe;
         cudaStreamSynchronize(h->s_h2d);
         cudaStreamSynchronize(h->s_comp);
         cudaStreamSynchronize(h->s_d2h);
+        return s;
+    }
+    if (locked) {
+        HostPipe::UploadStats &st = h->upload[key];
+        if (st.calls > 0)
+            st.ms[direct ? 1 : 0] = std::chrono::duration<double, std::milli>(
+                                        std::chrono::steady_clock::now() - t0).count();
+        st.calls++;
     }
     return s;
 }
