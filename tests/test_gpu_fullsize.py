@@ -91,3 +91,6 @@ def test_full_batch_properties(dgb, gpu, oracle):
         num = float((a - b).abs().max())
         assert num <= MIXED_RHS_TOL * den, (dgb.VAR_NAMES[v], num / den)
     plan.close()
+    # hand the ~113 GB back to the device for the tests that follow
+    del du, ra, rb, interior, a, b
+    torch.cuda.empty_cache()
