@@ -2,20 +2,26 @@
 // refined around the punctures, its regular blocks, the continuous-Galerkin
 // node numbering (the "zipped" vector) and the unzip / zip operators.
 //
-// What it restates (the reference's own mesh needs MPI and LAPACK and is not
-// compiled here):
+// What it reproduces of the reference's ot::Mesh (src/mesh.cpp, include/mesh.tcc);
+// the oracle build of that mesh gives the same blocks, offsets, CG numbering
+// and zip, and the same unzip to rounding, on these octrees:
 //   octree + 2:1 balance        ot::Mesh construction (src/mesh.cpp:283),
 //                               balance across faces, edges and corners
-//   blocks                      octree2BlockDecomposition (src/octUtils.cpp:556)
+//   element order               the reference's Hilbert curve (TreeNode::operator<)
+//   blocks                      octree2BlockDecomposition (src/octUtils.cpp:556-741)
 //                               / performBlocksSetup (src/mesh.cpp:8640-8790):
-//                               maximal aligned cubes of 2^k x 2^k x 2^k leaves of
-//                               one level (k <= 3), side p*2^k + 1 + 6 (src/block.cpp:50),
+//                               regular-grid levels passed down the octree in curve
+//                               order, side p*2^k + 1 + 6 (src/block.cpp:50),
 //                               offsets = exclusive prefix sum (src/mesh.cpp:8667-8672),
-//                               bflag = domain faces touched (src/mesh.cpp:8701-8738)
-//   zipped vector               one value per independent element node: a node
-//                               position is independent when it lies on the node
-//                               lattice of every leaf whose closure contains it;
-//                               the others are hanging
+//                               bflag = domain faces touched (src/mesh.cpp:8701-8738);
+//                               max_block_refine >= 0 selects maximal aligned cubes of
+//                               at most 2^max_block_refine leaves per side instead
+//   zipped vector               one value per independent element node (a node
+//   (Mesh::buildE2NMap,         position is independent when it lies on the node
+//   src/mesh.cpp:3895-3960)     lattice of every leaf whose closure contains it);
+//                               owner = the coarsest element holding it, first in
+//                               element order on ties; CG order = (owner, place in
+//                               the owner, x fastest)
 //   Mesh::unzip                 every padded point inside the domain gets the mesh
 //   (include/mesh.tcc:7436-8690) field at its position: an independent node's value,
 //                               or the degree-p Lagrange interpolant of the coarsest
@@ -27,9 +33,8 @@
 //                               parent->child interpolation (FEM/include/refel.h:249-296),
 //                               finer-neighbour child->parent injection
 //                               (mesh.tcc:7399-7433) and edge/corner padding, as one rule.
-//   Mesh::zip                   every independent node takes the block value at its
-//   (include/mesh.tcc:3775-3822) position from one owning block (the finest block
-//                               holding it in its interior, first in block order on ties).
+//   Mesh::zip                   every independent node takes the value at its
+//   (include/mesh.tcc:3775-3822) position in its owner's block.
 //
 // Operator encoding (see dgb_unzip_plan_create): a node reference is a 64-bit
 // word; bit 63 clear: copy independent node (low 32 bits); bit 63 set:
@@ -41,6 +46,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <string>
 #include <unordered_map>
@@ -70,7 +76,101 @@ inline uint64_t key(int lev, uint32_t x, uint32_t y, uint32_t z)
 }
 inline uint64_t pkey(uint64_t x, uint64_t y, uint64_t z) { return (x << 32) | (y << 16) | z; }
 
+// The reference's space-filling curve (Hilbert ordering, on by default:
+// CMakeLists.txt:32; tables in src/hcurvedata.cpp, used by
+// TreeNode::operator< and octree2BlockDecomposition, src/octUtils.cpp:556).
+// A state of the curve is a symmetry of the cube (an axis permutation with
+// reflections) applied to the base visiting order of the eight children;
+// child c = x | y << 1 | z << 2.  The base order and the symmetry each visited
+// child takes relative to its parent define the reference's particular curve:
+// the 24 states they generate give the same visiting orders and transitions
+// as the reference's tables (a test builds both and compares them).
+struct CubeSym {
+    uint8_t perm[3], flip[3];  // bit a of the image = bit perm[a] of the input ^ flip[a]
+    int apply(int c) const
+    {
+        int w = 0;
+        for (int a = 0; a < 3; a++) w |= (((c >> perm[a]) & 1) ^ flip[a]) << a;
+        return w;
+    }
+    CubeSym then(const CubeSym &inner) const  // this o inner
+    {
+        CubeSym r;
+        for (int a = 0; a < 3; a++) {
+            r.perm[a] = inner.perm[perm[a]];
+            r.flip[a] = (uint8_t)(inner.flip[perm[a]] ^ flip[a]);
+        }
+        return r;
+    }
+    bool operator==(const CubeSym &o) const { return memcmp(this, &o, sizeof o) == 0; }
+};
+
+struct HilbertCurve {
+    static constexpr int kBase[8] = {0, 2, 3, 1, 5, 7, 6, 4};
+    std::vector<CubeSym> state;
+    std::vector<std::array<uint8_t, 8>> order;  // [state][i] = child visited i-th
+    std::vector<std::array<uint8_t, 8>> pos;    // [state][child] = its place in the visit
+    std::vector<std::array<uint8_t, 8>> next;   // [state][child] = the child's state
+    HilbertCurve()
+    {
+        const CubeSym visit[8] = {{{0, 2, 1}, {0, 0, 0}}, {{2, 1, 0}, {0, 0, 0}}, {{0, 1, 2}, {0, 0, 0}},
+                                  {{2, 0, 1}, {0, 1, 1}}, {{2, 0, 1}, {1, 1, 0}}, {{0, 1, 2}, {0, 0, 0}},
+                                  {{2, 1, 0}, {1, 0, 1}}, {{0, 2, 1}, {0, 1, 1}}};
+        state.push_back(CubeSym{{0, 1, 2}, {0, 0, 0}});
+        for (size_t s = 0; s < state.size(); s++) {
+            std::array<uint8_t, 8> o, p, n;
+            for (int i = 0; i < 8; i++) {
+                const int c = state[s].apply(kBase[i]);
+                o[i] = (uint8_t)c;
+                p[c] = (uint8_t)i;
+                const CubeSym cs = state[s].then(visit[i]);
+                size_t id = 0;
+                while (id < state.size() && !(state[id] == cs)) id++;
+                if (id == state.size()) state.push_back(cs);
+                n[c] = (uint8_t)id;
+            }
+            order.push_back(o);
+            pos.push_back(p);
+            next.push_back(n);
+        }
+    }
+    // Key of the octant at level lev whose anchor has integer coordinates a
+    // (units of the finest level D): three bits per level from the root,
+    // left-aligned to D levels, so that disjoint octants sort in curve order.
+    uint64_t key(const uint32_t a[3], int lev, int D) const
+    {
+        uint64_t k = 0;
+        int s = 0;
+        for (int l = 1; l <= lev; l++) {
+            const int sh = D - l;
+            const int c = (int)((a[0] >> sh) & 1u) | (int)(((a[1] >> sh) & 1u) << 1) | (int)(((a[2] >> sh) & 1u) << 2);
+            k = (k << 3) | pos[s][c];
+            s = next[s][c];
+        }
+        return k << (3 * (D - lev));
+    }
+};
+constexpr int HilbertCurve::kBase[8];
+
+const HilbertCurve &hilbert()
+{
+    static const HilbertCurve h;
+    return h;
+}
+
 }  // namespace
+
+extern "C" dgb_status dgb_mesh_hilbert_tables(uint8_t *order, uint8_t *next, int *nstates)
+{
+    const HilbertCurve &h = hilbert();
+    if (nstates) *nstates = (int)h.state.size();
+    for (size_t s = 0; s < h.state.size(); s++)
+        for (int i = 0; i < 8; i++) {
+            if (order) order[8 * s + i] = h.order[s][i];
+            if (next) next[8 * s + i] = h.next[s][i];
+        }
+    return DGB_OK;
+}
 
 struct dgb_mesh {
     dgb_mesh_params prm;
@@ -82,8 +182,9 @@ struct dgb_mesh {
     std::vector<dgb_block_desc> blocks;
     std::vector<int> block_lev;
     std::vector<uint32_t> block_anchor;  // 3 per block (lattice units)
-    std::vector<uint64_t> dof_keys;      // positions of the independent nodes: sorted while the
-                                         // operators are built, zip-owner order afterwards
+    std::vector<uint64_t> dof_keys;      // positions of the independent nodes, in CG order
+    std::vector<uint64_t> own_mask;      // 6 words per leaf: the nodal points the leaf owns
+    std::vector<uint64_t> first_dof;     // per leaf: CG index of its first owned node
     // unzip operator
     std::vector<uint32_t> copy_src;      // per padded point: dof, or 0xFFFFFFFF
     std::vector<uint64_t> interp_dst, interp_ref;
@@ -136,7 +237,8 @@ struct dgb_mesh {
             if ((q[a] - (int64_t)e.a[a]) % s != 0) return false;
         return true;
     }
-    // Coarsest leaf whose closure holds q; also whether q is an independent node.
+    // Coarsest leaf whose closure holds q, first in element order on ties
+    // (the owner of q when it is a node); also whether q is an independent node.
     int64_t coarsest_at(const int64_t q[3], bool *independent, int hint = -1) const
     {
         int64_t best = -1;
@@ -147,16 +249,31 @@ struct dgb_mesh {
             if (e < 0) continue;
             hint = leaves[e].lev;
             if (!on_lattice(leaves[e], q)) indep = false;
-            if (best < 0 || leaves[e].lev < leaves[best].lev) best = e;
+            if (best < 0 || leaves[e].lev < leaves[best].lev || (leaves[e].lev == leaves[best].lev && e < best))
+                best = e;
         }
         if (independent) *independent = indep;
         return best;
     }
-    int64_t dof(const int64_t q[3]) const
+    // CG index of the independent node q owned by leaf e: e's first index plus
+    // the number of nodes e owns before q's place in it.
+    int64_t dof(int64_t e, const int64_t q[3]) const
     {
-        const uint64_t k = pkey(q[0], q[1], q[2]);
-        auto it = std::lower_bound(dof_keys.begin(), dof_keys.end(), k);
-        return (it != dof_keys.end() && *it == k) ? (int64_t)(it - dof_keys.begin()) : -1;
+        const Leaf &L = leaves[e];
+        const int64_t s = sp(L.lev);
+        int loc[3];
+        for (int a = 0; a < 3; a++) {
+            const int64_t d = q[a] - (int64_t)L.a[a];
+            if (d < 0 || d % s != 0 || d / s > P) return -1;
+            loc[a] = (int)(d / s);
+        }
+        const int l = loc[0] + (P + 1) * (loc[1] + (P + 1) * loc[2]);
+        const uint64_t *m = &own_mask[6 * e];
+        if (!((m[l >> 6] >> (l & 63)) & 1)) return -1;
+        uint64_t before = 0;
+        for (int w = 0; w < (l >> 6); w++) before += (uint64_t)__builtin_popcountll(m[w]);
+        if (l & 63) before += (uint64_t)__builtin_popcountll(m[l >> 6] & ((1ull << (l & 63)) - 1));
+        return (int64_t)(first_dof[e] + before);
     }
     // Reference for the field at lattice point q (kNone outside the domain);
     // interpolation references carry the LEAF index until sources are numbered.
@@ -166,7 +283,7 @@ struct dgb_mesh {
         const int64_t e = coarsest_at(q, &indep, hint);
         if (e < 0) return kNone;
         if (indep) {
-            const int64_t d = dof(q);
+            const int64_t d = dof(e, q);
             return d < 0 ? kNone : (uint64_t)d;
         }
         const Leaf &L = leaves[e];
@@ -227,7 +344,8 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
     *out = nullptr;
     if (prm->ele_order != P || prm->max_level < prm->min_level || prm->max_level > 12 ||
         prm->min_level < 1 || prm->num_punctures < 0 || prm->num_punctures > 4 ||
-        prm->max_block_refine < 0 || prm->max_block_refine > 3)
+        prm->max_block_refine < -1 || prm->max_block_refine > 3 ||
+        (prm->octree_depth != 0 && (prm->octree_depth < prm->max_level + 3 || prm->octree_depth > 30)))
         return DGB_ERR_INVALID;
     for (int a = 0; a < 3; a++)
         if (!(prm->domain_max[a] > prm->domain_min[a])) return DGB_ERR_INVALID;
@@ -297,112 +415,261 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
         }
         leaves.swap(next);
     }
-    // Morton order of the leaves
-    auto morton = [&](const Leaf &l) {
-        uint64_t m = 0;
-        for (int b = 15; b >= 0; b--)
-            for (int a = 2; a >= 0; a--) m = (m << 1) | ((l.a[a] / P) >> b & 1u);
-        return m;
-    };
-    std::sort(leaves.begin(), leaves.end(),
-              [&](const Leaf &x, const Leaf &y) { return morton(x) < morton(y); });
+    // ---- element order: the reference's space-filling curve (its
+    // m_uiAllElements order, so leaf indices are element indices)
+    {
+        const HilbertCurve &hc = hilbert();
+        std::vector<std::pair<uint64_t, uint32_t>> hk(leaves.size());
+        for (size_t i = 0; i < leaves.size(); i++) {
+            const uint32_t a[3] = {leaves[i].a[0] / P, leaves[i].a[1] / P, leaves[i].a[2] / P};
+            hk[i] = {hc.key(a, leaves[i].lev, M->D), (uint32_t)i};
+        }
+        std::sort(hk.begin(), hk.end());
+        std::vector<Leaf> sorted(leaves.size());
+        for (size_t i = 0; i < leaves.size(); i++) sorted[i] = leaves[hk[i].second];
+        leaves.swap(sorted);
+    }
     rebuild_index();
 
-    // ---- blocks: maximal aligned cubes of 2^k leaves of one level
-    std::vector<char> used(leaves.size(), 0);
-    uint64_t off = 0;
-    const int kmax = prm->max_block_refine;
-    for (size_t i = 0; i < leaves.size(); i++) {
-        if (used[i]) continue;
-        const Leaf e = leaves[i];
-        int kbest = 0;
-        uint32_t anc[3] = {e.a[0], e.a[1], e.a[2]};
-        for (int k = std::min(kmax, e.lev); k >= 1; k--) {
-            const uint32_t sa = M->S(e.lev - k);
-            const uint32_t A[3] = {e.a[0] / sa * sa, e.a[1] / sa * sa, e.a[2] / sa * sa};
-            if (A[0] != e.a[0] || A[1] != e.a[1] || A[2] != e.a[2]) continue;  // e must be the first leaf
-            const uint32_t s = M->S(e.lev), m = 1u << k;
-            bool ok = true;
-            for (uint32_t z = 0; z < m && ok; z++)
-                for (uint32_t y = 0; y < m && ok; y++)
-                    for (uint32_t x = 0; x < m && ok; x++) {
-                        auto it = M->leaf_of.find(key(e.lev, A[0] + x * s, A[1] + y * s, A[2] + z * s));
-                        if (it == M->leaf_of.end() || used[it->second]) ok = false;
-                    }
-            if (ok) {
-                kbest = k;
-                break;
-            }
+    // ---- blocks
+    struct BlockNode {
+        uint32_t a[3];  // anchor, lattice units
+        int node_lev, reg_lev;
+    };
+    std::vector<BlockNode> bnodes;
+    if (prm->max_block_refine < 0) {
+        // octree2BlockDecomposition (src/octUtils.cpp:556-741) with no tags,
+        // coarsest block level 0 (src/mesh.cpp:290), its constants
+        // OCT2BLK_DECOMP_LEV_GAP = 0 and fill ratio 0.5 (include/octUtils.h:39-40)
+        // and the octree depth m_uiMaxDepth of the reference's coordinates:
+        // a node whose leaves all have its regular-grid level r is a block of
+        // 2^(r - node level) leaves per side; otherwise each child is examined in
+        // curve order with level r if it holds a leaf of level r, else r + 1.
+        // The root starts at the coarsest leaf level.  Visiting the children in
+        // curve order lists the blocks in the order the reference's stack and
+        // final reversal leave them.
+        const HilbertCurve &hc = hilbert();
+        const int md = prm->octree_depth > 0 ? prm->octree_depth : M->D + 4;  // m_uiMaxDepth
+        int dmin = M->D, dmax = 0;
+        for (const Leaf &l : leaves) {
+            dmin = std::min(dmin, l.lev);
+            dmax = std::max(dmax, l.lev);
         }
-        const uint32_t s = M->S(e.lev), m = 1u << kbest;
-        for (uint32_t z = 0; z < m; z++)
-            for (uint32_t y = 0; y < m; y++)
-                for (uint32_t x = 0; x < m; x++)
-                    used[M->leaf_of[key(e.lev, anc[0] + x * s, anc[1] + y * s, anc[2] + z * s)]] = 1;
+        struct Item {
+            uint32_t a[3];
+            int lev, reg, rot;
+            size_t b, e;  // leaf range
+        };
+        std::vector<Item> stack{Item{{0, 0, 0}, 0, dmin, 0, 0, leaves.size()}};
+        while (!stack.empty()) {
+            const Item it = stack.back();
+            stack.pop_back();
+            bool uniform = true;
+            for (size_t i = it.b; i < it.e && uniform; i++) uniform = leaves[i].lev == it.reg;
+            // the volume test octVolume == blockVolume (src/octUtils.cpp:620-662)
+            // in the reference's arithmetic: each term is 1u << 3*(maxDepth - level)
+            // in 32-bit unsigned int, a shift that only keeps its count mod 32
+            // (the x86-64 and AArch64 shift instructions), summed in 128 bits; so
+            // a node of 2^32 octree units or more is never accepted whole
+            if (uniform && it.lev != it.reg) {
+                const unsigned __int128 count = (unsigned __int128)1 << (3 * (it.reg - it.lev));
+                const uint32_t vol_leaf = 1u << ((3 * (md - it.reg)) & 31);
+                const uint32_t vol_node = 1u << ((3 * (md - it.lev)) & 31);
+                uniform = count * vol_leaf == (unsigned __int128)vol_node;
+            }
+            if (uniform) {
+                bnodes.push_back(BlockNode{{it.a[0], it.a[1], it.a[2]}, it.lev, it.reg});
+                continue;
+            }
+            // children of the node: contiguous leaf ranges in curve order
+            const uint32_t half = M->S(it.lev + 1);
+            Item kids[8];
+            int nk = 0;
+            size_t i = it.b;
+            for (int v = 0; v < 8; v++) {
+                const int c = hc.order[it.rot][v];
+                Item k;
+                for (int a = 0; a < 3; a++) k.a[a] = it.a[a] + (((c >> a) & 1) ? half : 0);
+                k.lev = it.lev + 1;
+                k.rot = hc.next[it.rot][c];
+                k.b = i;
+                bool has_reg = false;
+                while (i < it.e) {
+                    const Leaf &l = leaves[i];
+                    bool in = true;
+                    for (int a = 0; a < 3; a++) in = in && l.a[a] >= k.a[a] && l.a[a] < k.a[a] + half;
+                    if (!in) break;
+                    has_reg = has_reg || l.lev == it.reg;
+                    i++;
+                }
+                k.e = i;
+                if (k.e == k.b) continue;
+                k.reg = has_reg ? it.reg : it.reg + 1;
+                if (k.reg > dmax) continue;
+                kids[nk++] = k;
+            }
+            if (i != it.e) {  // the leaves are not in curve order: cannot happen
+                delete M;
+                return DGB_ERR_INVALID;
+            }
+            for (int v = nk - 1; v >= 0; v--) stack.push_back(kids[v]);  // first child on top
+        }
+    } else {
+        // maximal aligned cubes of 2^k leaves of one level (k <= max_block_refine),
+        // found in Morton order and then listed in curve order
+        std::vector<uint32_t> morder(leaves.size());
+        for (size_t i = 0; i < leaves.size(); i++) morder[i] = (uint32_t)i;
+        auto morton = [&](const Leaf &l) {
+            uint64_t m = 0;
+            for (int b = 15; b >= 0; b--)
+                for (int a = 2; a >= 0; a--) m = (m << 1) | ((l.a[a] / P) >> b & 1u);
+            return m;
+        };
+        std::sort(morder.begin(), morder.end(),
+                  [&](uint32_t x, uint32_t y) { return morton(leaves[x]) < morton(leaves[y]); });
+        std::vector<char> used(leaves.size(), 0);
+        const int kmax = prm->max_block_refine;
+        std::vector<std::pair<uint64_t, BlockNode>> found;
+        for (uint32_t i : morder) {
+            if (used[i]) continue;
+            const Leaf e = leaves[i];
+            int kbest = 0;
+            for (int k = std::min(kmax, e.lev); k >= 1; k--) {
+                const uint32_t sa = M->S(e.lev - k);
+                const uint32_t A[3] = {e.a[0] / sa * sa, e.a[1] / sa * sa, e.a[2] / sa * sa};
+                if (A[0] != e.a[0] || A[1] != e.a[1] || A[2] != e.a[2]) continue;  // e must be the first leaf
+                const uint32_t s = M->S(e.lev), m = 1u << k;
+                bool ok = true;
+                for (uint32_t z = 0; z < m && ok; z++)
+                    for (uint32_t y = 0; y < m && ok; y++)
+                        for (uint32_t x = 0; x < m && ok; x++) {
+                            auto it = M->leaf_of.find(key(e.lev, A[0] + x * s, A[1] + y * s, A[2] + z * s));
+                            if (it == M->leaf_of.end() || used[it->second]) ok = false;
+                        }
+                if (ok) {
+                    kbest = k;
+                    break;
+                }
+            }
+            const uint32_t s = M->S(e.lev), m = 1u << kbest;
+            for (uint32_t z = 0; z < m; z++)
+                for (uint32_t y = 0; y < m; y++)
+                    for (uint32_t x = 0; x < m; x++)
+                        used[M->leaf_of[key(e.lev, e.a[0] + x * s, e.a[1] + y * s, e.a[2] + z * s)]] = 1;
+            const uint32_t a[3] = {e.a[0] / P, e.a[1] / P, e.a[2] / P};
+            found.push_back({hilbert().key(a, e.lev - kbest, M->D),
+                             BlockNode{{e.a[0], e.a[1], e.a[2]}, e.lev - kbest, e.lev}});
+        }
+        std::sort(found.begin(), found.end(),
+                  [](const std::pair<uint64_t, BlockNode> &x, const std::pair<uint64_t, BlockNode> &y) {
+                      return x.first < y.first;
+                  });
+        for (auto &f : found) bnodes.push_back(f.second);
+    }
+    // block descriptors (src/block.cpp:38-55), offsets = exclusive prefix sum
+    // (src/mesh.cpp:8661-8675), face flags (src/mesh.cpp:8701-8738)
+    std::vector<uint32_t> leaf_block(leaves.size(), 0xFFFFFFFFu);
+    uint64_t off = 0;
+    for (size_t bi = 0; bi < bnodes.size(); bi++) {
+        const BlockNode &bn = bnodes[bi];
+        const uint32_t m = 1u << (bn.reg_lev - bn.node_lev);
+        const uint32_t s = M->S(bn.reg_lev);
         dgb_block_desc b;
         memset(&b, 0, sizeof b);
         const uint32_t side = (uint32_t)P * m + 1 + 6;
-        const double h = M->sp(e.lev) * M->unit;
+        const double h = M->sp(bn.reg_lev) * M->unit;
         for (int a = 0; a < 3; a++) {
             b.sz[a] = side;
-            const double x0 = prm->domain_min[a] + anc[a] * M->unit;
+            const double x0 = prm->domain_min[a] + bn.a[a] * M->unit;
             b.ptmin[a] = x0 - 3 * h;
             b.ptmax[a] = x0 + (double)(P * m) * h + 3 * h;
-            if (anc[a] == 0) b.bflag |= 1u << (2 * a);
-            if (anc[a] + s * m == M->N) b.bflag |= 1u << (2 * a + 1);
+            if (bn.a[a] == 0) b.bflag |= 1u << (2 * a);
+            if (bn.a[a] + s * m == M->N) b.bflag |= 1u << (2 * a + 1);
         }
         b.offset = off;
         off += (uint64_t)side * side * side;
         M->blocks.push_back(b);
-        M->block_lev.push_back(e.lev);
-        M->block_anchor.insert(M->block_anchor.end(), anc, anc + 3);
+        M->block_lev.push_back(bn.reg_lev);
+        M->block_anchor.insert(M->block_anchor.end(), bn.a, bn.a + 3);
+        for (uint32_t z = 0; z < m; z++)
+            for (uint32_t y = 0; y < m; y++)
+                for (uint32_t x = 0; x < m; x++) {
+                    auto it = M->leaf_of.find(key(bn.reg_lev, bn.a[0] + x * s, bn.a[1] + y * s, bn.a[2] + z * s));
+                    if (it == M->leaf_of.end() || leaf_block[it->second] != 0xFFFFFFFFu) {
+                        delete M;
+                        return DGB_ERR_INVALID;
+                    }
+                    leaf_block[it->second] = (uint32_t)bi;
+                }
     }
+    for (uint32_t lb : leaf_block)
+        if (lb == 0xFFFFFFFFu) {
+            delete M;
+            return DGB_ERR_INVALID;
+        }
 
-    // ---- independent nodes: candidates per leaf, then sort + unique
-    {
-        std::vector<std::vector<uint64_t>> part;
-        int nt = 1;
-#ifdef _OPENMP
-        nt = omp_get_max_threads();
-#endif
-        part.resize(nt);
-#pragma omp parallel
-        {
-            int t = 0;
-#ifdef _OPENMP
-            t = omp_get_thread_num();
-#endif
-            std::vector<uint64_t> &mine = part[t];
-#pragma omp for schedule(dynamic, 256)
-            for (long long i = 0; i < (long long)leaves.size(); i++) {
-                const Leaf &e = leaves[i];
-                const int64_t s = M->sp(e.lev);
-                for (int k = 0; k <= P; k++)
-                    for (int j = 0; j <= P; j++)
-                        for (int ii = 0; ii <= P; ii++) {
-                            const int64_t q[3] = {(int64_t)e.a[0] + s * ii, (int64_t)e.a[1] + s * j,
-                                                  (int64_t)e.a[2] + s * k};
-                            bool indep = true;
-                            if (ii == 0 || ii == P || j == 0 || j == P || k == 0 || k == P)
-                                M->coarsest_at(q, &indep, e.lev);  // inner nodes belong to e alone
-                            if (indep) mine.push_back(pkey(q[0], q[1], q[2]));
-                        }
-            }
-        }
-        size_t tot = 0;
-        for (auto &v : part) tot += v.size();
-        M->dof_keys.reserve(tot);
-        for (auto &v : part) {
-            M->dof_keys.insert(M->dof_keys.end(), v.begin(), v.end());
-            std::vector<uint64_t>().swap(v);
-        }
-        std::sort(M->dof_keys.begin(), M->dof_keys.end());
-        M->dof_keys.erase(std::unique(M->dof_keys.begin(), M->dof_keys.end()), M->dof_keys.end());
+    // ---- independent nodes and their numbering (Mesh::buildE2NMap,
+    // src/mesh.cpp:3895-3960): a node is owned by the coarsest element that
+    // has it as a nodal point, the one first in element order on ties; the CG
+    // vector lists the nodes by owner, then by the node's place in the owner
+    // (x fastest).  Per leaf: a 343-bit mask of the nodes it owns and the index
+    // of its first one.
+    M->own_mask.assign(leaves.size() * 6, 0);
+    M->first_dof.assign(leaves.size() + 1, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long i = 0; i < (long long)leaves.size(); i++) {
+        const Leaf &e = leaves[i];
+        const int64_t s = M->sp(e.lev);
+        uint64_t *mask = &M->own_mask[6 * i];
+        uint64_t cnt = 0;
+        for (int k = 0; k <= P; k++)
+            for (int j = 0; j <= P; j++)
+                for (int ii = 0; ii <= P; ii++) {
+                    bool mine = true;
+                    if (ii == 0 || ii == P || j == 0 || j == P || k == 0 || k == P) {
+                        const int64_t q[3] = {(int64_t)e.a[0] + s * ii, (int64_t)e.a[1] + s * j,
+                                              (int64_t)e.a[2] + s * k};
+                        bool indep = true;
+                        mine = M->coarsest_at(q, &indep, e.lev) == (int64_t)i && indep;
+                    }
+                    if (mine) {
+                        const int l = ii + (P + 1) * (j + (P + 1) * k);
+                        mask[l >> 6] |= 1ull << (l & 63);
+                        cnt++;
+                    }
+                }
+        M->first_dof[i + 1] = cnt;
     }
-    const uint64_t ndof = M->dof_keys.size();
+    for (size_t i = 0; i < leaves.size(); i++) M->first_dof[i + 1] += M->first_dof[i];
+    const uint64_t ndof = M->first_dof[leaves.size()];
     if (ndof >= 0xFFFFFFFFull) {
         delete M;
         return DGB_ERR_INVALID;
+    }
+    // positions and zip sources (Mesh::zip, include/mesh.tcc:3775-3822: a node
+    // is read from its owner's block)
+    M->dof_keys.resize(ndof);
+    M->zip_src.resize(ndof);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long i = 0; i < (long long)leaves.size(); i++) {
+        const Leaf &e = leaves[i];
+        const int64_t s = M->sp(e.lev);
+        const uint64_t *mask = &M->own_mask[6 * i];
+        const uint32_t b = leaf_block[i];
+        const dgb_block_desc &B = M->blocks[b];
+        const uint32_t *A = &M->block_anchor[3 * b];
+        const uint64_t n = B.sz[0];
+        uint64_t d = M->first_dof[i];
+        for (int l = 0; l < NPE; l++) {
+            if (!((mask[l >> 6] >> (l & 63)) & 1)) continue;
+            const int ii = l % (P + 1), j = (l / (P + 1)) % (P + 1), k = l / ((P + 1) * (P + 1));
+            const uint64_t q[3] = {e.a[0] + (uint64_t)s * ii, e.a[1] + (uint64_t)s * j, e.a[2] + (uint64_t)s * k};
+            M->dof_keys[d] = pkey(q[0], q[1], q[2]);
+            uint64_t p[3];
+            for (int a = 0; a < 3; a++) p[a] = (q[a] - A[a]) / (uint64_t)s + 3;
+            M->zip_src[d] = B.offset + p[0] + n * (p[1] + n * p[2]);
+            d++;
+        }
     }
 
     // ---- padded points: copy or interpolation reference (parallel over blocks)
@@ -516,59 +783,6 @@ dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **out)
             M->interp_ref.push_back(remap(dr.second));
         }
         std::vector<std::pair<uint64_t, uint64_t>>().swap(part);
-    }
-    // ---- zip owners: finest block holding the node in its interior, first on ties
-    M->zip_src.assign(ndof, ~0ull);
-    std::vector<int8_t> owner_lev(ndof, -1);
-    for (size_t b = 0; b < M->blocks.size(); b++) {
-        const dgb_block_desc &B = M->blocks[b];
-        const int lev = M->block_lev[b];
-        const int n = (int)B.sz[0];
-        for (int k = 3; k < n - 3; k++)
-            for (int j = 3; j < n - 3; j++)
-                for (int i = 3; i < n - 3; i++) {
-                    const uint64_t dst = B.offset + (uint64_t)i + (uint64_t)n * (j + (uint64_t)n * k);
-                    const uint32_t d = M->copy_src[dst];
-                    if (d != SENT && lev > owner_lev[d]) {
-                        owner_lev[d] = (int8_t)lev;
-                        M->zip_src[d] = dst;
-                    }
-                }
-    }
-    for (uint64_t d = 0; d < ndof; d++)
-        if (M->zip_src[d] == ~0ull) {
-            delete M;
-            return DGB_ERR_INVALID;  // an independent node without an owning block
-        }
-    // ---- renumber the independent nodes in the order their owners are laid
-    // out (block by block, x fastest): the zip then reads and writes runs of
-    // consecutive addresses, and the unzip copies of a block's own interior
-    // read them, instead of gathering across the whole zipped vector.  From
-    // here on dof_keys is in that order (the lookup above needs no more).
-    {
-        std::vector<uint32_t> owner_of(off, SENT);
-        for (uint64_t d = 0; d < ndof; d++) owner_of[M->zip_src[d]] = (uint32_t)d;
-        std::vector<uint32_t> newid(ndof);
-        std::vector<uint64_t> keys2(ndof), zip2(ndof);
-        uint32_t next = 0;
-        for (uint64_t p = 0; p < off; p++) {
-            const uint32_t d = owner_of[p];
-            if (d == SENT) continue;
-            newid[d] = next;
-            keys2[next] = M->dof_keys[d];
-            zip2[next] = p;
-            next++;
-        }
-        M->dof_keys.swap(keys2);
-        M->zip_src.swap(zip2);
-#pragma omp parallel for schedule(static)
-        for (long long p = 0; p < (long long)off; p++)
-            if (M->copy_src[p] != SENT) M->copy_src[p] = newid[M->copy_src[p]];
-#pragma omp parallel for schedule(static)
-        for (long long q = 0; q < (long long)M->src_refs.size(); q++) {
-            const uint64_t r = M->src_refs[q];
-            if (!(r & kInterp)) M->src_refs[q] = newid[r];
-        }
     }
     *out = M;
     return DGB_OK;

@@ -151,6 +151,7 @@ _SIGS = {
     "dgb_mesh_blocks": (C.c_int, [C.c_void_p, C.POINTER(BlockDesc)]),
     "dgb_mesh_dof_coords": (C.c_int, [C.c_void_p, C.c_void_p]),
     "dgb_mesh_leaf_levels": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "dgb_mesh_hilbert_tables": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "dgb_mesh_unzip_operator": (C.c_int, [C.c_void_p] + [C.c_void_p] * 6),
     "dgb_mesh_leaf_patches": (C.c_int, [C.c_void_p] + [C.c_void_p] * 5),
     "dgb_wavelet_tol_radial": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double, C.c_double,
@@ -422,11 +423,12 @@ class MeshParams(C.Structure):
     _fields_ = [("domain_min", C.c_double * 3), ("domain_max", C.c_double * 3),
                 ("max_level", C.c_int), ("min_level", C.c_int), ("ele_order", C.c_int),
                 ("num_punctures", C.c_int), ("puncture", (C.c_double * 3) * 4),
-                ("fine_radius", C.c_double), ("max_block_refine", C.c_int)]
+                ("fine_radius", C.c_double), ("max_block_refine", C.c_int),
+                ("octree_depth", C.c_int)]
 
 
-def mesh_params(max_level=10, min_level=4, fine_radius=1.0, domain=32.0, max_block_refine=3,
-                punctures=((1.0, 0.0, 0.00123), (-1.0, 0.0, 0.00123))):
+def mesh_params(max_level=10, min_level=4, fine_radius=1.0, domain=32.0, max_block_refine=-1,
+                punctures=((1.0, 0.0, 0.00123), (-1.0, 0.0, 0.00123)), octree_depth=0):
     """Two-puncture octree on [-domain, domain]^3 (Brill-Lindquist masses at
     (+-1, 0, 0.00123))."""
     p = MeshParams()
@@ -438,13 +440,39 @@ def mesh_params(max_level=10, min_level=4, fine_radius=1.0, domain=32.0, max_blo
         p.puncture[i][:] = list(c)
     p.fine_radius = fine_radius
     p.max_block_refine = max_block_refine
+    p.octree_depth = octree_depth
     return p
+
+
+def hilbert_tables():
+    """The element order's curve: (order[state, i], next[state, child])."""
+    n = C.c_int()
+    check(lib().dgb_mesh_hilbert_tables(None, None, C.byref(n)), "dgb_mesh_hilbert_tables")
+    order = np.zeros((n.value, 8), dtype=np.uint8)
+    nxt = np.zeros((n.value, 8), dtype=np.uint8)
+    check(lib().dgb_mesh_hilbert_tables(order.ctypes.data, nxt.ctypes.data, C.byref(n)),
+          "dgb_mesh_hilbert_tables")
+    return order, nxt
+
+
+def block_node(b, params):
+    """(anchor of the block's node in units of the finest level, node level,
+    regular-grid level) of a block descriptor of a mesh made with params."""
+    D = params.max_level
+    L = params.domain_max[0] - params.domain_min[0]
+    h = (b.ptmax[0] - b.ptmin[0]) / (b.sz[0] - 1)
+    reg = D - int(round(np.log2(h * (6 << D) / L)))
+    k = int(round(np.log2((b.sz[0] - 7) // 6)))
+    anchor = tuple(int(round((b.ptmin[a] + 3 * h - params.domain_min[a]) / (L / (1 << D))))
+                   for a in range(3))
+    return anchor, reg - k, reg
 
 
 class Mesh:
     """Host octree mesh and its unzip / zip operators (numpy arrays)."""
 
     def __init__(self, params):
+        self.params = params
         h = C.c_void_p()
         check(lib().dgb_mesh_create(C.byref(params), C.byref(h)), "dgb_mesh_create")
         self.h = h
@@ -466,6 +494,11 @@ class Mesh:
         check(lib().dgb_mesh_leaf_levels(self.h, lev.ctypes.data, anc.ctypes.data),
               "dgb_mesh_leaf_levels")
         return lev, anc
+
+    def block_levels(self):
+        """Per block: (anchor in units of the finest level, node level, regular-grid
+        level), from its descriptor and the mesh's finest level."""
+        return [block_node(b, self.params) for b in self.blocks]
 
     def leaf_patches(self):
         """Per leaf: patch_base, block_side, boundary, corner (n x 3), hx."""

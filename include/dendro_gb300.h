@@ -253,16 +253,30 @@ dgb_status dgb_synth_blocks(int which, uint64_t seed, dgb_block_desc *blocks, si
 
 /* Synthetic 2:1-balanced octree on a cubic domain, refined to max_level
  * within fine_radius of each puncture and one level coarser per doubling of
- * the distance, down to min_level; leaves merged into blocks of up to
- * 2^max_block_refine leaves per side.  Host-side; replaces the mesh the
- * reference builds in ot::Mesh (src/mesh.cpp:283, :8640-8790). */
+ * the distance, down to min_level.  Host-side; replaces the mesh the
+ * reference builds in ot::Mesh (src/mesh.cpp:283).  With max_block_refine =
+ * -1 the leaves are ordered, grouped into blocks and numbered as the
+ * reference's mesh does: elements in its Hilbert order, blocks of
+ * octree2BlockDecomposition (src/octUtils.cpp:556-741) in the same order with
+ * the same offsets and face flags (src/mesh.cpp:8640-8790), the CG vector in
+ * the order of Mesh::buildE2NMap (src/mesh.cpp:3895-3960), zip from each
+ * node's owning element.  max_block_refine = 0..3 instead groups maximal
+ * aligned cubes of up to 2^max_block_refine leaves per side (not the
+ * reference's blocks; same element order and CG numbering rule). */
 typedef struct {
     double domain_min[3], domain_max[3];
     int max_level, min_level, ele_order; /* ele_order must be 6 */
     int num_punctures;
     double puncture[4][3];
     double fine_radius;
-    int max_block_refine; /* 0..3 */
+    int max_block_refine; /* -1 (the reference's blocks) or 0..3 */
+    /* The reference's octree depth (m_uiMaxDepth, BSSN_MAXDEPTH in its
+     * parameter files): its block decomposition depends on it (volumes of
+     * 2^32 octree units or more are never one block); max_level + 3..30 (the
+     * reference needs leaves of at least 8 octree units, where the 7 nodes of
+     * an order-6 element fall on distinct integer positions), or 0 for
+     * max_level + 4. */
+    int octree_depth;
 } dgb_mesh_params;
 typedef struct dgb_mesh dgb_mesh;
 dgb_status dgb_mesh_create(const dgb_mesh_params *prm, dgb_mesh **mesh);
@@ -274,6 +288,11 @@ dgb_status dgb_mesh_sizes(const dgb_mesh *mesh, uint64_t *sizes);
 dgb_status dgb_mesh_blocks(const dgb_mesh *mesh, dgb_block_desc *blocks);
 dgb_status dgb_mesh_dof_coords(const dgb_mesh *mesh, double *xyz);
 dgb_status dgb_mesh_leaf_levels(const dgb_mesh *mesh, uint8_t *level, uint32_t *anchor);
+/* The element order's space-filling curve: per state s (nstates of them),
+ * order[8s + i] = the child (x | y << 1 | z << 2) visited i-th and
+ * next[8s + c] = child c's state; state 0 at the root.  Any pointer may be
+ * NULL.  The reference holds the same curve as tables (src/hcurvedata.cpp). */
+dgb_status dgb_mesh_hilbert_tables(uint8_t *order, uint8_t *next, int *nstates);
 /* The mesh's unzip / zip operators in the form dgb_unzip_plan_create takes
  * (array lengths from dgb_mesh_sizes; src_refs holds 343 per source). */
 dgb_status dgb_mesh_unzip_operator(const dgb_mesh *mesh, uint32_t *copy_src, uint64_t *interp_dst,

@@ -1,8 +1,8 @@
 """ORACLE binding — test infrastructure only (tests/, smoke(), bench.py's
 CPU-baseline leg).  Loads oracle/_build/liboracle.so (the C restatement,
-built by `make -f oracle/Makefile`) and, where it was built,
-oracle/_ref/libdendro_ref.so (the reference's own sources,
-`make -f oracle/Makefile.ref`)."""
+built by `make -f oracle/Makefile`) and, where they were built,
+oracle/_ref/libdendro_ref.so, libccz4_ref.so and libmesh_ref.so (the
+reference's own sources, `make -f oracle/Makefile.ref`)."""
 import ctypes as C
 import os
 import subprocess
@@ -13,6 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libdendro_ref.so")
 CCZ4_REF_SO = os.path.join(HERE, "_ref", "libccz4_ref.so")
+MESH_REF_SO = os.path.join(HERE, "_ref", "libmesh_ref.so")
+# where the reference tree lies (read-only); DENDRO_REF overrides the default
+REF_ROOT = os.environ.get("DENDRO_REF", "/root/reference")
 
 _D = C.POINTER(C.c_double)
 _PP = C.POINTER(C.c_void_p)
@@ -23,8 +26,9 @@ def build_oracle():
     return ORACLE_SO
 
 
-def build_ref(ref_root="/root/reference"):
+def build_ref(ref_root=None):
     """Compile the reference's own sources (only where the tree exists)."""
+    ref_root = ref_root or REF_ROOT
     if not os.path.isdir(ref_root):
         return None
     subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), f"REF={ref_root}"],
@@ -435,3 +439,81 @@ def rk4_step_pipeline(oracle, blocks, op, nunzipped, state, dt, prm, chi_floor=1
         oracle.rk4_stage(s, dst, prev, ks, dt, chi_floor)
         im = dst
     return im
+
+
+class MeshReference:
+    """The reference's own ot::Mesh (oracle/ref_mesh.cpp over src/mesh.cpp,
+    include/mesh.tcc, src/octUtils.cpp ... built by oracle/Makefile.ref with a
+    single-rank MPI stand-in and an own dgesv_), built from a leaf list."""
+
+    def __init__(self, path=MESH_REF_SO):
+        L = C.CDLL(path)
+        V = C.c_void_p
+        L.refmesh_build.argtypes = [V, V, C.c_uint64, C.c_uint, C.c_uint]
+        for nm in ("refmesh_sizes", "refmesh_blocks", "refmesh_elements", "refmesh_cg_coords",
+                   "refmesh_zip_owner"):
+            getattr(L, nm).argtypes = [V]
+        L.refmesh_unzip.argtypes = [V, V]
+        L.refmesh_zip.argtypes = [V, V]
+        L.refmesh_wavelets.argtypes = [C.c_uint, V, V, C.c_int, V, V]
+        L.refmesh_destroy.restype = None
+        self.L = L
+
+    def build(self, anchors, levels, max_depth, order=6):
+        """anchors: (n, 3) in octree units of max_depth; levels: (n,)."""
+        a = np.ascontiguousarray(anchors, dtype=np.uint32)
+        lv = np.ascontiguousarray(levels, dtype=np.uint8)
+        assert self.L.refmesh_build(a.ctypes.data, lv.ctypes.data, len(lv), max_depth, order) == 0
+        s = (C.c_uint64 * 8)()
+        self.L.refmesh_sizes(s)
+        (self.nelem, self.nblocks, self.nunzipped, self.ncg, self.node_begin, self.node_end,
+         self.elem_begin, self.elem_end) = [int(x) for x in s]
+        return self
+
+    def blocks(self):
+        """(nblocks, 12): node x, y, z, level, regular level, sizes x, y, z,
+        offset, face flags, element range."""
+        b = np.zeros((self.nblocks, 12), dtype=np.int64)
+        self.L.refmesh_blocks(b.ctypes.data)
+        return b
+
+    def elements(self):
+        e = np.zeros((self.nelem, 4), dtype=np.uint32)
+        self.L.refmesh_elements(e.ctypes.data)
+        return e
+
+    def cg_coords(self):
+        """CG node coordinates in octree units (n, 3)."""
+        x = np.zeros((self.ncg, 3))
+        self.L.refmesh_cg_coords(x.ctypes.data)
+        return x
+
+    def zip_owner(self):
+        o = np.zeros(self.ncg, dtype=np.int64)
+        self.L.refmesh_zip_owner(o.ctypes.data)
+        return o
+
+    def unzip(self, cg):
+        out = np.full(self.nunzipped, np.nan)
+        c = np.ascontiguousarray(cg, dtype=np.float64)
+        self.L.refmesh_unzip(c.ctypes.data, out.ctypes.data)
+        return out
+
+    def zip(self, uz):
+        out = np.full(self.ncg, np.nan)
+        u = np.ascontiguousarray(uz, dtype=np.float64)
+        self.L.refmesh_zip(u.ctypes.data, out.ctypes.data)
+        return out
+
+    def wavelets(self, patch, shape, boundary, order=6):
+        """WaveletEl::compute_wavelets_3D on one patch (shape x, y, z)."""
+        p = np.ascontiguousarray(patch, dtype=np.float64)
+        isz = np.array(shape, dtype=np.uint32)
+        wc = np.zeros(4096)
+        n = C.c_uint()
+        self.L.refmesh_wavelets(order, p.ctypes.data, isz.ctypes.data, int(boundary), wc.ctypes.data,
+                                C.addressof(n))
+        return wc[:n.value].copy()
+
+    def close(self):
+        self.L.refmesh_destroy()

@@ -41,7 +41,7 @@ def oracle():
 @pytest.fixture(scope="session")
 def reference():
     import oracle_py
-    if not os.path.isdir("/root/reference") and not os.path.exists(oracle_py.REF_SO):
+    if not os.path.isdir(oracle_py.REF_ROOT) and not os.path.exists(oracle_py.REF_SO):
         pytest.skip("reference tree not present on this machine")
     try:
         oracle_py.build_ref()

@@ -189,5 +189,66 @@ def ccz4_goldens(dgb):
     print("wrote", os.path.join(HERE, "ccz4_reference.npz"))
 
 
+def mesh_goldens(dgb):
+    """The reference's own ot::Mesh (oracle/ref_mesh.cpp over src/mesh.cpp,
+    include/mesh.tcc, src/octUtils.cpp, FEM/src/refel.cpp ...) built from
+    this library's level-6 octree: its element order, block list
+    (octree2BlockDecomposition + performBlocksSetup), CG numbering (owner
+    element and place in it, Mesh::buildE2NMap), Mesh::unzip of a smooth
+    field (full padded grids of a few blocks and per-block checksums of all)
+    and Mesh::zip of a seeded unzipped vector (checksum and head), and the
+    reference's Hilbert tables (src/hcurvedata.cpp)."""
+    import ctypes as C
+
+    from meshref import (GOLDEN_FULL_BLOCKS, GOLDEN_MESH, checksums, field,
+                         leaves_in_octree_units)
+    mesh = dgb.Mesh(dgb.mesh_params(**GOLDEN_MESH))
+    anc, lev, md = leaves_in_octree_units(mesh)
+    R = oracle_py.MeshReference().build(anc, lev, md)
+    bl = R.blocks()
+    el = R.elements()
+    own = R.zip_owner()
+    xyz = R.cg_coords()
+    key = np.rint(xyz * 6).astype(np.int64)
+    ex = el[own].astype(np.int64)
+    ln = 1 << (md - ex[:, 3])
+    loc = np.stack([(key[:, a] - 6 * ex[:, a]) // ln for a in range(3)], axis=1)
+    local = loc[:, 0] + 7 * (loc[:, 1] + 7 * loc[:, 2])
+    # unzip of the smooth field given at the reference's own CG nodes
+    f = field(xyz / (1 << md) * 64.0 - 32.0)
+    uz = R.unzip(f)
+    cs = checksums(uz, bl[:, [0, 1, 2, 5, 6, 7, 8, 9]])
+    # full grids: the domain-corner block, the blocks with most and fewest
+    # NaN-free points that take interpolated values ... chosen by a fixed rule
+    sizes = bl[:, 5]
+    small = np.nonzero(sizes == 13)[0]
+    mid = np.nonzero(sizes == 19)[0]
+    picks = [int(small[0]), int(small[len(small) // 2]), int(small[-1]), int(mid[len(mid) // 2])]
+    assert len(picks) == GOLDEN_FULL_BLOCKS
+    full = np.concatenate([uz[bl[i, 8]:bl[i, 8] + bl[i, 5] * bl[i, 6] * bl[i, 7]] for i in picks])
+    rng = np.random.default_rng(7)
+    u = rng.standard_normal(R.nunzipped)
+    z = R.zip(u)
+    rot = C.cast(C.c_void_p.in_dll(R.L, "rotations"), C.POINTER(C.c_char))
+    ht = C.cast(C.c_void_p.in_dll(R.L, "HILBERT_TABLE"), C.POINTER(C.c_char))
+    rot_t = np.array([[rot[r * 16 + i][0] - 48 for i in range(16)] for r in range(24)], np.uint8)
+    ht_t = np.array([[ht[r * 8 + c][0] for c in range(8)] for r in range(24)], np.uint8)
+    np.savez_compressed(
+        os.path.join(HERE, "mesh_reference.npz"),
+        octree_depth=np.array(md), leaves=np.column_stack([anc, lev]).astype(np.uint32),
+        elements=el, blocks=bl, cg_owner_step=np.diff(own, prepend=0).astype(np.uint8),
+        cg_local=local.astype(np.int16), unzip_checksums=cs, unzip_full_blocks=np.array(picks),
+        unzip_full=full, zip_seed=np.array(7), zip_sum=np.array(np.sum(z)),
+        zip_wsum=np.array(np.sum(z * np.cos(0.7 * np.arange(len(z))))), zip_head=z[:4096],
+        hilbert_rotations=rot_t, hilbert_table=ht_t)
+    R.close()
+    print("wrote", os.path.join(HERE, "mesh_reference.npz"))
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["mesh"]:
+        oracle_py.build_ref()
+        mesh_goldens(load_dgb())
+    else:
+        main()
+        mesh_goldens(load_dgb())

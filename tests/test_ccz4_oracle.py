@@ -22,7 +22,7 @@ def golden():
 @pytest.fixture(scope="session")
 def ccz4_reference():
     import oracle_py
-    if not os.path.isdir("/root/reference") and not os.path.exists(oracle_py.CCZ4_REF_SO):
+    if not os.path.isdir(oracle_py.REF_ROOT) and not os.path.exists(oracle_py.CCZ4_REF_SO):
         pytest.skip("reference tree not present on this machine")
     try:
         oracle_py.build_ref()

@@ -52,6 +52,48 @@ def test_unzip_zip_match_host_operator(dgb, gpu, small_mesh):
     uz.close()
 
 
+def test_unzip_matches_reference_goldens(dgb, gpu, small_mesh):
+    """The GPU unzip on the level-6 mesh against the reference's own
+    Mesh::unzip of the same field (tests/golden/mesh_reference.npz): the
+    stored padded grids within 1e-14 normwise, every block's checksums within
+    1e-13; where the reference leaves a point beyond the domain untouched the
+    GPU writes 0."""
+    import os
+
+    from meshref import GOLDEN_MESH, checksums, field
+    torch = gpu
+    m = small_mesh
+    assert (m.params.max_level, m.params.min_level) == (GOLDEN_MESH["max_level"],
+                                                        GOLDEN_MESH["min_level"])
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "mesh_reference.npz"))
+    rows = g["blocks"][:, [0, 1, 2, 5, 6, 7, 8, 9]]
+    uz = dgb.UnzipPlan(m.operator(), m.ndof)
+    dz = torch.from_numpy(field(m.dof_coords())).cuda()
+    du = torch.full((m.nunzipped,), 7.0, dtype=torch.float64, device="cuda")
+    uz.unzip([dz.data_ptr()], [du.data_ptr()])
+    torch.cuda.synchronize()
+    got = du.cpu().numpy()
+    off = 0
+    nan_mask = np.zeros(m.nunzipped, dtype=bool)
+    full = g["unzip_full"]
+    for b in g["unzip_full_blocks"]:
+        r = rows[int(b)]
+        n = int(np.prod(r[3:6]))
+        ref, mine = full[off:off + n], got[r[6]:r[6] + n]
+        off += n
+        fin = np.isfinite(ref)
+        assert np.all(mine[~fin] == 0.0)
+        assert np.max(np.abs(mine[fin] - ref[fin])) <= 1e-14 * np.max(np.abs(ref[fin]))
+    for r in rows:  # points the reference leaves untouched: the GPU's zeros
+        n = int(np.prod(r[3:6]))
+        nan_mask[r[6]:r[6] + n] = got[r[6]:r[6] + n] == 0.0
+    cs = checksums(np.where(nan_mask, np.nan, got), rows)
+    cs_ref = g["unzip_checksums"]
+    assert np.array_equal(cs[:, 0], cs_ref[:, 0])
+    assert np.max(np.abs(cs[:, 1:] - cs_ref[:, 1:])) <= 1e-13 * np.max(np.abs(cs_ref[:, 1:]))
+    uz.close()
+
+
 @pytest.mark.parametrize("nsteps", [1, 2, 10])
 def test_rk4_step_matches_oracle(dgb, gpu, oracle, small_mesh, nsteps):
     torch = gpu

@@ -1,11 +1,10 @@
-"""CPU tests of the octree mesh and its unzip / zip operators.
-
-The reference's own mesh (ot::Mesh) needs MPI and LAPACK and cannot be
-compiled here, so these are property checks in the style of the reference's
-mesh tests (test/include/meshTestUtils.h: isUnzipValid :290 checks that
-unzip reproduces a smooth function in the padding): 2:1 balance, blocks
-cover the leaves, unzip reproduces any polynomial of degree <= 6 per axis
-exactly (the element interpolant is exact for it), and zip(unzip(z)) = z."""
+"""CPU tests of the octree mesh and its unzip / zip operators: property
+checks in the style of the reference's mesh tests
+(test/include/meshTestUtils.h: isUnzipValid :290 checks that unzip
+reproduces a smooth function in the padding): 2:1 balance, blocks cover the
+leaves, unzip reproduces any polynomial of degree <= 6 per axis exactly (the
+element interpolant is exact for it), and zip(unzip(z)) = z.  The comparison
+with the reference's own ot::Mesh is tests/test_mesh_reference.py."""
 import numpy as np
 import pytest
 
