@@ -453,6 +453,7 @@ class MeshReference:
         for nm in ("refmesh_sizes", "refmesh_blocks", "refmesh_elements", "refmesh_cg_coords",
                    "refmesh_zip_owner"):
             getattr(L, nm).argtypes = [V]
+        L.refmesh_element_patches.argtypes = [V, V, V, V]
         L.refmesh_unzip.argtypes = [V, V]
         L.refmesh_zip.argtypes = [V, V]
         L.refmesh_wavelets.argtypes = [C.c_uint, V, V, C.c_int, V, V]
@@ -504,6 +505,18 @@ class MeshReference:
         u = np.ascontiguousarray(uz, dtype=np.float64)
         self.L.refmesh_zip(u.ctypes.data, out.ctypes.data)
         return out
+
+    def element_patches(self, uz, with_patches=True):
+        """Per local element in isReMeshUnzip's order: (element index, its
+        13^3 padded patches of uz or None, isBoundaryOctant)."""
+        n = self.elem_end - self.elem_begin
+        e = np.zeros(n, dtype=np.int64)
+        bd = np.zeros(n, dtype=np.uint8)
+        pt = np.zeros((n, 13 ** 3)) if with_patches else None
+        u = np.ascontiguousarray(uz, dtype=np.float64)
+        self.L.refmesh_element_patches(u.ctypes.data, e.ctypes.data,
+                                       pt.ctypes.data if with_patches else None, bd.ctypes.data)
+        return e, pt, bd
 
     def wavelets(self, patch, shape, boundary, order=6):
         """WaveletEl::compute_wavelets_3D on one patch (shape x, y, z)."""

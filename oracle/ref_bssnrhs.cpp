@@ -12,15 +12,18 @@
  * 6th-order family through QuadGrav/include/derivs.h
  * (QUADGRAV_USE_6TH_ORDER_DERIVS), i.e. QuadGrav/src/derivs.cpp.
  * Domain-boundary blocks (bflag != 0) get the reference's one-sided
- * closures (they live in derivs.cpp) but NOT bssn_bcs, which lives in a
- * translation unit that needs the mesh and MPI; callers compare against a
- * restatement run without the boundary condition.
+ * closures (they live in derivs.cpp) and its outgoing-radiation condition
+ * bssn_bcs, extracted verbatim from BSSN_GR/src/rhs.cpp at build time
+ * (oracle/Makefile.ref), called with the reference's falloff and asymptotic
+ * values per variable (rhs.cpp:265-324).
  */
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 
 #include "derivs.h"
+
+#include "bssn_bcs.inc"
 
 namespace {
 enum { V_ALPHA = 0, V_CHI, V_K, V_GT0, V_GT1, V_GT2, V_BETA0, V_BETA1, V_BETA2,
@@ -85,6 +88,41 @@ extern "C" int ref_bssnrhs(double **unzipVarsRHS, const double **uZipVars,
 #include "bssneqs_eta_const_standard_gauge.cpp"
             }
         }
+    }
+
+    if (bflag != 0) {
+        struct Bc {
+            double *rhs;
+            const double *f, *dx, *dy, *dz;
+            double falloff, asymptotic;
+        };
+        const Bc bcs[24] = {
+            {a_rhs, alpha, grad_0_alpha, grad_1_alpha, grad_2_alpha, 1.0, 1.0},
+            {chi_rhs, chi, grad_0_chi, grad_1_chi, grad_2_chi, 1.0, 1.0},
+            {K_rhs, K, grad_0_K, grad_1_K, grad_2_K, 1.0, 0.0},
+            {b_rhs0, beta0, grad_0_beta0, grad_1_beta0, grad_2_beta0, 1.0, 0.0},
+            {b_rhs1, beta1, grad_0_beta1, grad_1_beta1, grad_2_beta1, 1.0, 0.0},
+            {b_rhs2, beta2, grad_0_beta2, grad_1_beta2, grad_2_beta2, 1.0, 0.0},
+            {Gt_rhs0, Gt0, grad_0_Gt0, grad_1_Gt0, grad_2_Gt0, 2.0, 0.0},
+            {Gt_rhs1, Gt1, grad_0_Gt1, grad_1_Gt1, grad_2_Gt1, 2.0, 0.0},
+            {Gt_rhs2, Gt2, grad_0_Gt2, grad_1_Gt2, grad_2_Gt2, 2.0, 0.0},
+            {B_rhs0, B0, grad_0_B0, grad_1_B0, grad_2_B0, 1.0, 0.0},
+            {B_rhs1, B1, grad_0_B1, grad_1_B1, grad_2_B1, 1.0, 0.0},
+            {B_rhs2, B2, grad_0_B2, grad_1_B2, grad_2_B2, 1.0, 0.0},
+            {At_rhs00, At0, grad_0_At0, grad_1_At0, grad_2_At0, 2.0, 0.0},
+            {At_rhs01, At1, grad_0_At1, grad_1_At1, grad_2_At1, 2.0, 0.0},
+            {At_rhs02, At2, grad_0_At2, grad_1_At2, grad_2_At2, 2.0, 0.0},
+            {At_rhs11, At3, grad_0_At3, grad_1_At3, grad_2_At3, 2.0, 0.0},
+            {At_rhs12, At4, grad_0_At4, grad_1_At4, grad_2_At4, 2.0, 0.0},
+            {At_rhs22, At5, grad_0_At5, grad_1_At5, grad_2_At5, 2.0, 0.0},
+            {gt_rhs00, gt0, grad_0_gt0, grad_1_gt0, grad_2_gt0, 1.0, 1.0},
+            {gt_rhs01, gt1, grad_0_gt1, grad_1_gt1, grad_2_gt1, 1.0, 0.0},
+            {gt_rhs02, gt2, grad_0_gt2, grad_1_gt2, grad_2_gt2, 1.0, 0.0},
+            {gt_rhs11, gt3, grad_0_gt3, grad_1_gt3, grad_2_gt3, 1.0, 1.0},
+            {gt_rhs12, gt4, grad_0_gt4, grad_1_gt4, grad_2_gt4, 1.0, 0.0},
+            {gt_rhs22, gt5, grad_0_gt5, grad_1_gt5, grad_2_gt5, 1.0, 1.0}};
+        for (const Bc &c : bcs)
+            bssn_bcs(c.rhs, c.f, c.dx, c.dy, c.dz, pmin, pmax, c.falloff, c.asymptotic, sz, bflag);
     }
 
 #include "bssnrhs_ko_derivs.h"

@@ -10,16 +10,19 @@
  * of CCZ4_GR/src/derivs.cpp (the binding of CCZ4_GR/include/rhs.h:14-28),
  * the generated point algebra CCZ4_GR/src/ccz4eqs.cpp inside the interior
  * loop with eta(r), the KO drivers and the KO accumulate loop (which leaves
- * theta_z4 out, rhs.cpp:241-283).  ccz4_bcs lives in the same translation
- * unit as the solver globals, so domain-boundary blocks get the one-sided
- * stencils but not the boundary condition; callers compare against a
- * restatement run without it.
+ * theta_z4 out, rhs.cpp:241-283).  Domain-boundary blocks get the one-sided
+ * stencils and the outgoing-radiation condition ccz4_bcs, extracted verbatim
+ * from CCZ4_GR/src/rhs.cpp at build time (oracle/Makefile.ref), called for
+ * every variable but theta_z4 with the falloff and asymptotic values of the
+ * solver's ccz4rhs (rhs.cpp:170-228).
  */
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 
 #include "derivs.h"
+
+#include "ccz4_bcs.inc"
 
 #define deriv_x deriv42_x
 #define deriv_y deriv42_y
@@ -104,6 +107,41 @@ extern "C" int ref_ccz4rhs(double **unzipVarsRHS, const double **uZipVars, unsig
 #include "ccz4eqs.cpp"
             }
         }
+    }
+
+    if (bflag != 0) {
+        struct Bc {
+            double *rhs;
+            const double *f, *dx, *dy, *dz;
+            double falloff, asymptotic;
+        };
+        const Bc bcs[24] = {
+            {a_rhs, alpha, grad_0_alpha, grad_1_alpha, grad_2_alpha, 1.0, 1.0},
+            {psi_rhs, psi, grad_0_psi, grad_1_psi, grad_2_psi, 1.0, 1.0},
+            {K_rhs, K, grad_0_K, grad_1_K, grad_2_K, 1.0, 0.0},
+            {b_rhs0, beta0, grad_0_beta0, grad_1_beta0, grad_2_beta0, 1.0, 0.0},
+            {b_rhs1, beta1, grad_0_beta1, grad_1_beta1, grad_2_beta1, 1.0, 0.0},
+            {b_rhs2, beta2, grad_0_beta2, grad_1_beta2, grad_2_beta2, 1.0, 0.0},
+            {Gh_rhs0, Gh0, grad_0_Gh0, grad_1_Gh0, grad_2_Gh0, 2.0, 0.0},
+            {Gh_rhs1, Gh1, grad_0_Gh1, grad_1_Gh1, grad_2_Gh1, 2.0, 0.0},
+            {Gh_rhs2, Gh2, grad_0_Gh2, grad_1_Gh2, grad_2_Gh2, 2.0, 0.0},
+            {B_rhs0, B0, grad_0_B0, grad_1_B0, grad_2_B0, 1.0, 0.0},
+            {B_rhs1, B1, grad_0_B1, grad_1_B1, grad_2_B1, 1.0, 0.0},
+            {B_rhs2, B2, grad_0_B2, grad_1_B2, grad_2_B2, 1.0, 0.0},
+            {At_rhs00, At0, grad_0_At0, grad_1_At0, grad_2_At0, 2.0, 0.0},
+            {At_rhs01, At1, grad_0_At1, grad_1_At1, grad_2_At1, 2.0, 0.0},
+            {At_rhs02, At2, grad_0_At2, grad_1_At2, grad_2_At2, 2.0, 0.0},
+            {At_rhs11, At3, grad_0_At3, grad_1_At3, grad_2_At3, 2.0, 0.0},
+            {At_rhs12, At4, grad_0_At4, grad_1_At4, grad_2_At4, 2.0, 0.0},
+            {At_rhs22, At5, grad_0_At5, grad_1_At5, grad_2_At5, 2.0, 0.0},
+            {gt_rhs00, gt0, grad_0_gt0, grad_1_gt0, grad_2_gt0, 1.0, 1.0},
+            {gt_rhs01, gt1, grad_0_gt1, grad_1_gt1, grad_2_gt1, 1.0, 0.0},
+            {gt_rhs02, gt2, grad_0_gt2, grad_1_gt2, grad_2_gt2, 1.0, 0.0},
+            {gt_rhs11, gt3, grad_0_gt3, grad_1_gt3, grad_2_gt3, 1.0, 1.0},
+            {gt_rhs12, gt4, grad_0_gt4, grad_1_gt4, grad_2_gt4, 1.0, 0.0},
+            {gt_rhs22, gt5, grad_0_gt5, grad_1_gt5, grad_2_gt5, 1.0, 1.0}};
+        for (const Bc &c : bcs)
+            ccz4_bcs(c.rhs, c.f, c.dx, c.dy, c.dz, pmin, pmax, c.falloff, c.asymptotic, sz, bflag);
     }
 
 #include "ccz4rhs_ko_derivs.h"

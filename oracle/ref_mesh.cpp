@@ -167,8 +167,30 @@ int refmesh_zip_owner(int64_t *owner)
     return 0;
 }
 
+// Per local element, in the order Mesh::isReMeshUnzip visits them (blocks,
+// then each block's elements, include/mesh.tcc:2066-2085): its index, its
+// (2p+1)^3 padded patch of the unzipped vector uz from
+// getUnzipElementalNodalValues (include/mesh.tcc:9136-9176) into patches
+// (13^3 doubles each at p = 6, x fastest; NULL skips them) and
+// isBoundaryOctant (include/mesh.h:1482-1486) into bdy.
+int refmesh_element_patches(const double *uz, int64_t *elem, double *patches, uint8_t *bdy)
+{
+    if (!g_mesh) return 1;
+    const std::vector<ot::Block> &bl = g_mesh->getLocalBlockList();
+    const unsigned p = g_mesh->getElementOrder();
+    const size_t np = (size_t)(2 * p + 1) * (2 * p + 1) * (2 * p + 1);
+    size_t q = 0;
+    for (unsigned b = 0; b < bl.size(); b++)
+        for (unsigned e = bl[b].getLocalElementBegin(); e < bl[b].getLocalElementEnd(); e++, q++) {
+            elem[q] = e;
+            if (patches) g_mesh->getUnzipElementalNodalValues(uz, b, e, patches + q * np, true);
+            bdy[q] = g_mesh->isBoundaryOctant(e) ? 1 : 0;
+        }
+    return 0;
+}
+
 // WaveletEl::compute_wavelets_3D on one padded element patch (side
-// 2*order+1 points per axis... as Mesh::isReMeshUnzip passes it):
+// 2*order+1 points per axis, as Mesh::isReMeshUnzip passes it):
 // wc receives the wavelet coefficients (count returned in *nwc).
 int refmesh_wavelets(unsigned order, const double *patch, const unsigned *isz, int is_bdy, double *wc, unsigned *nwc)
 {

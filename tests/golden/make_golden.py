@@ -196,12 +196,13 @@ def mesh_goldens(dgb):
     (octree2BlockDecomposition + performBlocksSetup), CG numbering (owner
     element and place in it, Mesh::buildE2NMap), Mesh::unzip of a smooth
     field (full padded grids of a few blocks and per-block checksums of all)
-    and Mesh::zip of a seeded unzipped vector (checksum and head), and the
-    reference's Hilbert tables (src/hcurvedata.cpp)."""
+    and Mesh::zip of a seeded unzipped vector (checksum and head), the
+    reference's Hilbert tables (src/hcurvedata.cpp), and the wavelets of
+    WaveletEl on seeded patches and on every element's unzipped patch."""
     import ctypes as C
 
     from meshref import (GOLDEN_FULL_BLOCKS, GOLDEN_MESH, checksums, field,
-                         leaves_in_octree_units)
+                         leaves_in_octree_units, wavelet_test_patches)
     mesh = dgb.Mesh(dgb.mesh_params(**GOLDEN_MESH))
     anc, lev, md = leaves_in_octree_units(mesh)
     R = oracle_py.MeshReference().build(anc, lev, md)
@@ -229,6 +230,16 @@ def mesh_goldens(dgb):
     rng = np.random.default_rng(7)
     u = rng.standard_normal(R.nunzipped)
     z = R.zip(u)
+    # WaveletEl::compute_wavelets_3D (src/waveletRefEl.cpp:92-271) on seeded
+    # patches (interior, then boundary), and per element of the mesh the
+    # reference's own patch (getUnzipElementalNodalValues) wavelets of the
+    # smooth field and of chi-like 1/(1+r) data
+    wp = wavelet_test_patches()
+    half = len(wp) // 2
+    wav = np.stack([R.wavelets(p.ravel(), (13, 13, 13), i >= half) for i, p in enumerate(wp)])
+    elem, patches, bdy = R.element_patches(uz)
+    rms = np.array([np.sqrt(np.sum(w * w)) / 8.0 for w in
+                    (R.wavelets(patches[q], (13, 13, 13), bool(bdy[q])) for q in range(len(elem)))])
     rot = C.cast(C.c_void_p.in_dll(R.L, "rotations"), C.POINTER(C.c_char))
     ht = C.cast(C.c_void_p.in_dll(R.L, "HILBERT_TABLE"), C.POINTER(C.c_char))
     rot_t = np.array([[rot[r * 16 + i][0] - 48 for i in range(16)] for r in range(24)], np.uint8)
@@ -240,7 +251,9 @@ def mesh_goldens(dgb):
         cg_local=local.astype(np.int16), unzip_checksums=cs, unzip_full_blocks=np.array(picks),
         unzip_full=full, zip_seed=np.array(7), zip_sum=np.array(np.sum(z)),
         zip_wsum=np.array(np.sum(z * np.cos(0.7 * np.arange(len(z))))), zip_head=z[:4096],
-        hilbert_rotations=rot_t, hilbert_table=ht_t)
+        hilbert_rotations=rot_t, hilbert_table=ht_t,
+        wavelet_patch_seed=np.array(5), wavelet_wc=wav, element_order=elem.astype(np.int32),
+        element_boundary=bdy, element_wavelet_rms=rms)
     R.close()
     print("wrote", os.path.join(HERE, "mesh_reference.npz"))
 

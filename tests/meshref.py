@@ -66,3 +66,32 @@ def checksums(uz, blocks_rows):
         w = np.cos(0.7 * np.arange(n))
         out[i] = [np.count_nonzero(~fin), np.sum(v[fin]), np.sum((v * w)[fin])]
     return out
+
+
+def wavelet_test_patches(n=16, seed=5):
+    """Seeded 13^3 patches for the wavelet comparison: smooth products plus
+    x^7 terms, half of them with 1e-3 noise; the second half is used as
+    boundary elements."""
+    rng = np.random.default_rng(seed)
+    g = np.arange(13) / 12.0
+    Z, Y, X = np.meshgrid(g, g, g, indexing="ij")
+    out = []
+    for t in range(n):
+        a = rng.normal(size=6)
+        p = (np.sin(a[0] * X + a[1]) * np.cos(a[2] * Y + a[3]) * np.exp(a[4] * Z) + a[5] * X ** 7
+             + (rng.normal(size=X.shape) * 1e-3 if t % 2 else 0.0))
+        out.append(p)
+    return out
+
+
+def element_wmax(patches_per_var, boundary, tol):
+    """isReMeshUnzip's per-element value from given wavelet slots: the
+    largest RMS over the variables, stopping once it passes tol
+    (include/mesh.tcc:2130-2150)."""
+    wm = 0.0
+    for wc in patches_per_var:
+        l = np.sqrt(np.sum(wc * wc)) / np.sqrt(len(wc))
+        wm = max(wm, l)
+        if wm > tol:
+            break
+    return wm

@@ -66,7 +66,7 @@ def test_oracle_ccz4_matches_golden(dgb, oracle, golden):
     blocks, u = golden_blocks(dgb, golden)
     n = len(u[0])
     r = [np.zeros(n) for _ in range(25)]
-    assert oracle.ccz4rhs_blocks(r, u, blocks, golden["params"], apply_bcs=False) == 0
+    assert oracle.ccz4rhs_blocks(r, u, blocks, golden["params"]) == 0
     mask = interior_mask(blocks, n)
     err = normwise([x[mask] for x in r], list(golden["rhs"]), np.ones(int(mask.sum()), dtype=bool))
     assert err.max() <= 1e-13, dict(zip(dgb.CCZ4_VAR_NAMES, err))

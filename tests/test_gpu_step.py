@@ -56,8 +56,7 @@ def test_unzip_matches_reference_goldens(dgb, gpu, small_mesh):
     """The GPU unzip on the level-6 mesh against the reference's own
     Mesh::unzip of the same field (tests/golden/mesh_reference.npz): the
     stored padded grids within 1e-14 normwise, every block's checksums within
-    1e-13; where the reference leaves a point beyond the domain untouched the
-    GPU writes 0."""
+    1e-13; points beyond the domain are left untouched by both."""
     import os
 
     from meshref import GOLDEN_MESH, checksums, field
@@ -82,11 +81,11 @@ def test_unzip_matches_reference_goldens(dgb, gpu, small_mesh):
         ref, mine = full[off:off + n], got[r[6]:r[6] + n]
         off += n
         fin = np.isfinite(ref)
-        assert np.all(mine[~fin] == 0.0)
+        assert np.all(mine[~fin] == 7.0)
         assert np.max(np.abs(mine[fin] - ref[fin])) <= 1e-14 * np.max(np.abs(ref[fin]))
-    for r in rows:  # points the reference leaves untouched: the GPU's zeros
+    for r in rows:  # points left untouched keep the fill value
         n = int(np.prod(r[3:6]))
-        nan_mask[r[6]:r[6] + n] = got[r[6]:r[6] + n] == 0.0
+        nan_mask[r[6]:r[6] + n] = got[r[6]:r[6] + n] == 7.0
     cs = checksums(np.where(nan_mask, np.nan, got), rows)
     cs_ref = g["unzip_checksums"]
     assert np.array_equal(cs[:, 0], cs_ref[:, 0])

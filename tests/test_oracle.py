@@ -162,9 +162,9 @@ def test_oracle_boundary_closures_bit_exact(oracle, reference, kind):
 
 
 def test_oracle_boundary_rhs_matches_reference(dgb, oracle, reference):
-    """Boundary blocks: closures in the derivatives, the mixed compositions and
-    KO agree with the reference harness (which cannot apply bssn_bcs, so both
-    run without it here)."""
+    """Boundary blocks: closures in the derivatives, the mixed compositions,
+    the outgoing-radiation condition bssn_bcs (the reference's own function,
+    BSSN_GR/src/rhs.cpp:838-982) and KO agree with the reference harness."""
     blocks = boundary_blocks(dgb)
     u = host_fields(dgb, blocks, SEED1)
     prm = dgb.params_vector(dgb.default_params(0.1))
@@ -172,7 +172,7 @@ def test_oracle_boundary_rhs_matches_reference(dgb, oracle, reference):
     r1 = [np.zeros(n) for _ in range(24)]
     r2 = [np.zeros(n) for _ in range(24)]
     for b in blocks:
-        assert oracle.bssnrhs_block(r1, u, b, prm, apply_bcs=False) == 0
+        assert oracle.bssnrhs_block(r1, u, b, prm) == 0
         assert reference.bssnrhs(r2, u, b, prm) == 0
     err = normwise(r1, r2, interior_mask(blocks, n))
     assert err.max() <= 1e-13, dict(zip(dgb.VAR_NAMES, err))

@@ -2,16 +2,102 @@
 include/mesh.tcc:2035-2197; WaveletEl::compute_wavelets_3D,
 src/waveletRefEl.cpp:92-271) and of the mesh's per-leaf patch table.
 
-The reference's wavelet element needs its RefElement (LAPACK) and MPI and is
-not compiled here, so the oracle is pinned by known answers: the wavelets of
-an interior element vanish for every polynomial of degree <= 6 per axis (the
-parent interpolant reproduces it) and those of a boundary element for degree
-<= 3; for the monic x^7 (interior) and x^4 (boundary) they equal the
-interpolation error prod(x - x_b) over the parent nodes x_b, relative to
-max(1, |u|)."""
+The oracle is pinned against the reference's own WaveletEl (built with its
+RefElement into oracle/_ref/libmesh_ref.so; goldens in
+tests/golden/mesh_reference.npz): wavelets within 1e-14 of the data's scale
+(both sides interpolate with Lagrange weights of the uniform nodes, the
+reference's from a LAPACK solve, so they differ by rounding, and a wavelet is
+a small difference of O(1) values); the per-leaf patches and boundary flags
+equal the reference's getUnzipElementalNodalValues and isBoundaryOctant.
+Known answers pin it further: the wavelets of an interior element vanish for
+every polynomial of degree <= 6 per axis (the parent interpolant reproduces
+it) and those of a boundary element for degree <= 3; for the monic x^7
+(interior) and x^4 (boundary) they equal the interpolation error
+prod(x - x_b) over the parent nodes x_b, relative to max(1, |u|)."""
 import math
+import os
 
 import numpy as np
+import pytest
+
+from meshref import GOLDEN_MESH, field, wavelet_test_patches
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "mesh_reference.npz")
+WAVELET_TOL = 1e-14  # of max |data|
+
+
+def test_wavelets_equal_reference_goldens(oracle):
+    g = np.load(GOLDEN)
+    wp = wavelet_test_patches(seed=int(g["wavelet_patch_seed"]))
+    half = len(wp) // 2
+    for i, p in enumerate(wp):
+        wc, _ = oracle.wavelet_patch(p, boundary=i >= half)
+        assert np.max(np.abs(wc - g["wavelet_wc"][i])) <= WAVELET_TOL * np.max(np.abs(p)), i
+
+
+def test_leaf_patches_and_wavelets_equal_reference_goldens(dgb, oracle):
+    """On the level-6 mesh: every leaf's patch of the unzipped smooth field,
+    its boundary flag and its wavelet RMS against the reference's own
+    (getUnzipElementalNodalValues, isBoundaryOctant, compute_wavelets_3D)."""
+    from oracle_py import unzip_apply
+    g = np.load(GOLDEN)
+    m = dgb.Mesh(dgb.mesh_params(**GOLDEN_MESH))
+    uz = unzip_apply(m.operator(), field(m.dof_coords()), m.nunzipped)
+    lp = m.leaf_patches()
+    elem = g["element_order"].astype(np.int64)
+    assert np.array_equal(lp["boundary"][elem], g["element_boundary"])
+    n = lp["block_side"]
+    rms = np.zeros(len(elem))
+    for q, e in enumerate(elem):
+        b, s = int(lp["patch_base"][e]), int(n[e])
+        idx = b + np.arange(13)[None, None, :] + s * (np.arange(13)[None, :, None]
+                                                      + s * np.arange(13)[:, None, None])
+        _, rms[q] = oracle.wavelet_patch(uz[idx], boundary=bool(lp["boundary"][e]))
+    assert np.max(np.abs(rms - g["element_wavelet_rms"])) <= WAVELET_TOL * np.nanmax(np.abs(uz))
+
+
+@pytest.fixture(scope="module")
+def refmesh():
+    import oracle_py
+    if not os.path.isdir(oracle_py.REF_ROOT) and not os.path.exists(oracle_py.MESH_REF_SO):
+        pytest.skip("reference tree not present on this machine")
+    oracle_py.build_ref()
+    return oracle_py.MeshReference()
+
+
+def test_wavelets_equal_reference_live(oracle, refmesh):
+    for i, p in enumerate(wavelet_test_patches(n=64, seed=11)):
+        for bd in (False, True):
+            wc, _ = oracle.wavelet_patch(p, boundary=bd)
+            wr = refmesh.wavelets(p.ravel(), (13, 13, 13), bd)
+            assert np.max(np.abs(wc - wr)) <= WAVELET_TOL * np.max(np.abs(p)), (i, bd)
+
+
+def test_leaf_patches_equal_reference_live(dgb, refmesh):
+    """Per leaf of a level-8 mesh, the 13^3 patch at patch_base (rows of
+    block_side) equals the reference's getUnzipElementalNodalValues bit for
+    bit on a random unzipped vector, and the boundary flags agree.  On a leaf
+    touching the domain boundary the reference overwrites the padding beyond
+    it with the face values (include/mesh.tcc:9178-9246), which the boundary
+    wavelets never read (they use points 3..9 per axis): there the 7^3
+    nodes are compared."""
+    from meshref import leaves_in_octree_units
+    m = dgb.Mesh(dgb.mesh_params(max_level=8, min_level=4, fine_radius=1.0))
+    anc, lev, md = leaves_in_octree_units(m)
+    R = refmesh.build(anc, lev, md)
+    u = np.random.default_rng(9).standard_normal(m.nunzipped)
+    elem, patches, bdy = R.element_patches(u)
+    lp = m.leaf_patches()
+    assert np.array_equal(lp["boundary"][elem], bdy)
+    ax = np.arange(13)
+    for q, e in enumerate(elem):
+        b, s = int(lp["patch_base"][e]), int(lp["block_side"][e])
+        idx = b + ax[None, None, :] + s * (ax[None, :, None] + s * ax[:, None, None])
+        if bdy[q]:
+            assert np.array_equal(u[idx][3:10, 3:10, 3:10],
+                                  patches[q].reshape(13, 13, 13)[3:10, 3:10, 3:10]), q
+        else:
+            assert np.array_equal(u[idx].ravel(), patches[q]), q
 
 IDX = np.arange(13, dtype=np.float64)
 
