@@ -76,11 +76,31 @@ def first_blocks(dgb, blocks, nmax):
 MAX_BLOCKS = 0  # --max-blocks
 
 
-def workload(dgb, name):
+def timing_oracle():
+    """The oracle port built for this host's CPU (oracle/Makefile's
+    liboracle_bench.so: -O3, the host's instruction set, no floating-point
+    contraction): what the CPU legs time.  Built here if it is missing."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    if not os.path.exists(oracle_py.ORACLE_BENCH_SO):
+        oracle_py.build_oracle()
+    return oracle_py.Oracle(oracle_py.ORACLE_BENCH_SO)
+
+
+def synth_blocks(dgb, which, seed, ora=None):
+    """The synthetic block list from the library, or from the oracle's
+    restatement of the same generator when ora is given (the reference arms
+    build their inputs without the CUDA library; both give the same bits)."""
+    if ora is not None:
+        return ora.synth_blocks(which, seed, dgb.BlockDesc)
+    return dgb.synth_blocks(which, seed)
+
+
+def workload(dgb, name, ora=None):
     if name == "uneven20k":
-        return first_blocks(dgb, dgb.synth_blocks(2, SEED2), MAX_BLOCKS), SEED2, 0.1
+        return first_blocks(dgb, synth_blocks(dgb, 2, SEED2, ora), MAX_BLOCKS), SEED2, 0.1
     if name == "uniform512":
-        return dgb.synth_blocks(1), SEED1, 0.1
+        return synth_blocks(dgb, 1, 0, ora), SEED1, 0.1
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -217,12 +237,11 @@ def e2e_host_arrays(dgb, count, n, pageable):
 
 def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="bssn"):
     """Times the oracle port of the reference CPU path on all host cores
-    (system "bssn": bssnrhs; "ccz4": ccz4rhs with its 25 variables)."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle_py
+    (system "bssn": bssnrhs; "ccz4": ccz4rhs with its 25 variables), on
+    inputs from the oracle's own copy of the synthetic generator."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from workloads import repack
-    ora = oracle_py.Oracle()
+    ora = timing_oracle()
     cores = os.cpu_count() or 1
     nv = 25 if system == "ccz4" else 24
     if system == "ccz4":
@@ -242,7 +261,7 @@ def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="b
         idx = cpu_sample(blocks, frac)
         sub = repack(dgb, blocks, idx)
         u = [np.zeros(dgb.unzipped_size(sub)) for _ in range(nv)]
-        dgb.synth_fill_host(sub, u, seed, 1e-6)
+        ora.synth_fill(sub, u, seed, 1e-6)
         r = [np.zeros_like(u[0]) for _ in range(nv)]
         t0 = time.perf_counter()
         assert call(r, u, sub) == 0
@@ -255,7 +274,7 @@ def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="b
     idx1 = cpu_sample(sub, 1.0 / 16)
     sub1 = repack(dgb, sub, idx1)
     u1 = [np.zeros(dgb.unzipped_size(sub1)) for _ in range(nv)]
-    dgb.synth_fill_host(sub1, u1, seed, 1e-6)
+    ora.synth_fill(sub1, u1, seed, 1e-6)
     r1 = [np.zeros_like(u1[0]) for _ in range(nv)]
     one_core = dict(bssn=lambda: ora.bssnrhs_blocks(r1, u1, sub1, prm, 1),
                     ccz4=lambda: ora.ccz4rhs_blocks(r1, u1, sub1, prm, True, 1))[system]
@@ -334,7 +353,8 @@ def main():
         return main_constraints(args, dgb, rank, world, local)
     if args.workload == "wavelet_octree":
         return main_wavelets(args, dgb, rank, world, local)
-    blocks, seed, sigma = workload(dgb, args.workload)
+    blocks, seed, sigma = workload(dgb, args.workload,
+                                   timing_oracle() if args.impl == "reference" else None)
     npts = interior_points(blocks)
     units = npts * 24
     wl = {"workload": f"{args.workload}: {len(blocks)} padded blocks "
@@ -454,7 +474,9 @@ def main():
 def main_ccz4(args, dgb, rank, world, local):
     """CCZ4 right-hand side (25 variables, kappa = (0.1, 0), KO sigma 0.4) over
     the uneven 20,000-block batch, one persistent launch per step."""
-    blocks = first_blocks(dgb, dgb.synth_blocks(2, SEED2), MAX_BLOCKS)
+    blocks = first_blocks(dgb, synth_blocks(dgb, 2, SEED2,
+                                            timing_oracle() if args.impl == "reference" else None),
+                          MAX_BLOCKS)
     seed, sigma = 20261203 + 5, 0.4
     npts = interior_points(blocks)
     units = npts * 25
@@ -554,17 +576,15 @@ def main_ccz4(args, dgb, rank, world, local):
 
 def cpu_constraints_baseline(dgb, blocks, seed, target_s=12.0, steps=1):
     """Oracle port of physical_constraints on all host cores, stratified sample."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle_py
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from workloads import repack
-    ora = oracle_py.Oracle()
+    ora = timing_oracle()
     cores = os.cpu_count() or 1
     frac = 1.0 / 400
     for attempt in range(3):
         sub = repack(dgb, blocks, cpu_sample(blocks, frac))
         u = [np.zeros(dgb.unzipped_size(sub)) for _ in range(24)]
-        dgb.synth_fill_host(sub, u, seed, 1e-6)
+        ora.synth_fill(sub, u, seed, 1e-6)
         c = [np.zeros_like(u[0]) for _ in range(6)]
         t0 = time.perf_counter()
         assert ora.physcon_blocks(c, u, sub, cores) == 0
@@ -586,7 +606,8 @@ def cpu_constraints_baseline(dgb, blocks, seed, target_s=12.0, steps=1):
 def main_constraints(args, dgb, rank, world, local):
     """Constraint diagnostics (Hamiltonian, momentum, Psi4; physical_constraints)
     over the uneven 20,000-block batch; units = interior points per second."""
-    blocks, seed, _ = workload(dgb, "uneven20k")
+    blocks, seed, _ = workload(dgb, "uneven20k",
+                               timing_oracle() if args.impl == "reference" else None)
     npts = interior_points(blocks)
     wl = {"workload": f"constraints_uneven20k: physical_constraints on {len(blocks)} padded "
                       + ("blocks (14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)" if len(blocks) == 20000
@@ -690,7 +711,7 @@ def cpu_rk4_baseline(dgb, seed, sigma, steps=1):
     4-8, the same refinement rule) on all host cores."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
-    ora = oracle_py.Oracle()
+    ora = timing_oracle()
     cores = os.cpu_count() or 1
     m = dgb.Mesh(dgb.mesh_params(max_level=8, min_level=4, fine_radius=1.0))
     op = m.operator()
@@ -854,9 +875,7 @@ def cpu_wavelet_baseline(dgb, mesh, host_unzipped, var_ids, tables, tol, fac, ta
                          steps=1):
     """Oracle port of isReMeshUnzip (eight-child interpolation per element, as
     the reference computes it) over a leaf sample, OpenMP over leaves."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle_py
-    ora = oracle_py.Oracle()
+    ora = timing_oracle()
     cores = os.cpu_count() or 1
     n = mesh.num_leaves
     k = 64

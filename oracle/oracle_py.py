@@ -11,6 +11,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+# the same sources built -O3 for the host's own CPU: the CPU timing legs
+ORACLE_BENCH_SO = os.path.join(HERE, "_build", "liboracle_bench.so")
 REF_SO = os.path.join(HERE, "_ref", "libdendro_ref.so")
 CCZ4_REF_SO = os.path.join(HERE, "_ref", "libccz4_ref.so")
 MESH_REF_SO = os.path.join(HERE, "_ref", "libmesh_ref.so")
@@ -84,6 +86,11 @@ class Oracle:
         L.orc_wavelet_patch.argtypes = [_D, C.c_int, _D]
         L.orc_wavelet_rms.restype = C.c_double
         L.orc_wavelet_rms.argtypes = [_D]
+        L.orc_synth_blocks.restype = C.c_long
+        L.orc_synth_blocks.argtypes = [C.c_int, C.c_uint64, C.c_void_p]
+        L.orc_synth_fill.restype = None
+        L.orc_synth_fill.argtypes = [C.c_void_p, C.c_long, _PP, C.c_int, C.c_uint64, C.c_double,
+                                     C.c_int]
         L.orc_remesh_wavelets.restype = C.c_uint64
         L.orc_remesh_wavelets.argtypes = [_PP, C.POINTER(C.c_uint32), C.c_int, C.c_uint64,
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -94,6 +101,21 @@ class Oracle:
             f.restype = None
             f.argtypes = [C.c_int, _D, _D, C.c_double, C.POINTER(C.c_uint), C.c_uint]
         self.L = L
+
+    def synth_blocks(self, which, seed, block_type):
+        """The synthetic block list (which = 1: 512 uniform 13^3 blocks, 2: the
+        uneven 20,000-block batch) as an array of block_type (a ctypes
+        structure with the dgb_block_desc layout)."""
+        n = self.L.orc_synth_blocks(which, seed, None)
+        arr = (block_type * n)()
+        self.L.orc_synth_blocks(which, seed, C.addressof(arr))
+        return arr
+
+    def synth_fill(self, blocks, fields, seed, noise=1e-6, nthreads=0):
+        """Brill-Lindquist + seeded noise into fields (24 or 25 arrays)."""
+        pp, keep = _ptrs(fields)
+        self.L.orc_synth_fill(C.addressof(blocks), len(blocks), pp, len(fields), seed, noise,
+                              nthreads or (os.cpu_count() or 1))
 
     def bssnrhs_blocks(self, rhs, u, blocks, prm, nthreads=0):
         """bssnRHS over a block list (list of dgb BlockDesc)."""

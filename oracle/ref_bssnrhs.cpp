@@ -158,6 +158,22 @@ extern "C" int ref_bssnrhs(double **unzipVarsRHS, const double **uZipVars,
     return 0;
 }
 
+/* bssnRHS over a block list with OpenMP over blocks, the loop the
+ * reference's test bed times (BSSN_GR/src/rhsTestBed.cpp:181-215); each
+ * call allocates and frees its 210 scratch arrays as bssnrhs does. */
+extern "C" int ref_bssnrhs_blocks(double **rhs, const double **uz, long nblk,
+                                  const unsigned long *offsets, const unsigned *sizes,
+                                  const unsigned *bflags, const double *pmins, const double *pmaxs,
+                                  const double *prm, int nthreads)
+{
+    int err = 0;
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads > 0 ? nthreads : 1) reduction(| : err)
+    for (long b = 0; b < nblk; b++)
+        err |= ref_bssnrhs(rhs, uz, (unsigned)offsets[b], pmins + 3 * b, pmaxs + 3 * b, sizes + 3 * b,
+                           bflags[b], prm);
+    return err;
+}
+
 /* The reference's per-node RK update closure (BSSN_GR/src/bssn_constraints.cpp). */
 namespace bssn { double CHI_FLOOR = 1e-4; }
 void enforce_bssn_constraints(double **uiVar, const unsigned int offset);
