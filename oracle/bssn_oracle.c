@@ -12,8 +12,13 @@
  * What follows which reference lines:
  *   stencils      QuadGrav/src/derivs.cpp:2141-2953 (deriv64_*, centred
  *                 "advective" = deriv64), BSSN_GR/src/derivs.cpp:914-1410
- *                 (ko_deriv42_*), with the reference loop ranges; only the
- *                 bflag == 0 (interior-block) branch.
+ *                 (ko_deriv42_*), with the reference loop ranges and the
+ *                 one-sided closures of flagged faces; for the BSSN_GR
+ *                 solver's 4th-order binding (BSSN_GR/include/rhs.h:23-37)
+ *                 deriv42_* and the upwinded deriv42adv_* (BSSN_GR/src/
+ *                 derivs.cpp:11-913, restated in physcon_oracle.c and
+ *                 ccz4_oracle.c).
+ *   BCs           bssn_bcs (BSSN_GR/src/rhs.cpp:838-982) on flagged faces.
  *   rhs driver    BSSN_GR/src/rhs.cpp:86-392 (bssnrhs: h = (pmax-pmin)/(n-1),
  *                 derivative staging per BSSN_GR/scripts/bssnrhs_derivs.h,
  *                 eta(r) at rhs.cpp:219-223, KO accumulate at :336-373).
@@ -233,6 +238,11 @@ typedef struct {
     double da[3], dchi[3], dK[3], dGt[3][3], db[3][3], dB[3][3];  /* [component][dir] */
     double dgt[3][3][3], dAt[3][3][3];                           /* [i][j][dir] */
     double ddgt[3][3][3][3], ddchi[3][3], dda[3][3], ddb[3][3][3]; /* [..][l][m] */
+    /* upwind != 0: the advection terms beta^j d_j f of every field f are
+     * adv[f] (VAR order), from the upwinded derivatives of the 4th-order
+     * binding; otherwise they use the centred first derivatives above */
+    int upwind;
+    double adv[24];
 } orc_point;
 
 /* out[] in variable order (grDef.h:31). */
@@ -329,12 +339,14 @@ void orc_bssn_point(const orc_point *P, const double *prm, double eta, double *o
 
     /* lapse, shift (bssn.py:65-72) */
     double adva = 0.0;
-    for (int i = 0; i < 3; i++) adva += P->b[i] * P->da[i];
+    if (P->upwind) adva = P->adv[A_];
+    else for (int i = 0; i < 3; i++) adva += P->b[i] * P->da[i];
     const double a_rhs = l1 * adva - 2.0 * a * K;
     double b_rhs[3];
     for (int i = 0; i < 3; i++) {
         double s = 0.0;
-        for (int j = 0; j < 3; j++) s += P->b[j] * P->db[i][j];
+        if (P->upwind) s = P->adv[BETA0_ + i];
+        else for (int j = 0; j < 3; j++) s += P->b[j] * P->db[i][j];
         b_rhs[i] = 3.0 / 4.0 * (lf0 + lf1 * a) * P->B[i] + l2 * s;
     }
 
@@ -344,17 +356,28 @@ void orc_bssn_point(const orc_point *P, const double *prm, double eta, double *o
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
             double sg = 0.0, sa = 0.0;
-            for (int k = 0; k < 3; k++) {
-                sg += P->b[k] * P->dgt[i][j][k] + g[i][k] * P->db[k][j] + g[k][j] * P->db[k][i]
-                    + w * g[i][j] * P->db[k][k];
-                sa += P->b[k] * P->dAt[i][j][k] + P->At[i][k] * P->db[k][j]
-                    + P->At[k][j] * P->db[k][i] + w * P->At[i][j] * P->db[k][k];
+            if (P->upwind) {
+                sg = P->adv[SGT0_ + SYM[i][j]];
+                sa = P->adv[SAT0_ + SYM[i][j]];
+                for (int k = 0; k < 3; k++) {
+                    sg += g[i][k] * P->db[k][j] + g[k][j] * P->db[k][i] + w * g[i][j] * P->db[k][k];
+                    sa += P->At[i][k] * P->db[k][j] + P->At[k][j] * P->db[k][i]
+                        + w * P->At[i][j] * P->db[k][k];
+                }
+            } else {
+                for (int k = 0; k < 3; k++) {
+                    sg += P->b[k] * P->dgt[i][j][k] + g[i][k] * P->db[k][j] + g[k][j] * P->db[k][i]
+                        + w * g[i][j] * P->db[k][k];
+                    sa += P->b[k] * P->dAt[i][j][k] + P->At[i][k] * P->db[k][j]
+                        + P->At[k][j] * P->db[k][i] + w * P->At[i][j] * P->db[k][k];
+                }
             }
             gt_rhs[i][j] = sg - 2.0 * a * P->At[i][j];
             At_rhs[i][j] = sa;
         }
     double advchi = 0.0;
-    for (int i = 0; i < 3; i++) advchi += P->b[i] * P->dchi[i];
+    if (P->upwind) advchi = P->adv[CHI_];
+    else for (int i = 0; i < 3; i++) advchi += P->b[i] * P->dchi[i];
     const double chi_rhs = advchi + w * chi * divb + 2.0 / 3.0 * (chi * a * K);
 
     /* At: chi * TF(a R - DiDj a) + a (K At - 2 At_ik At^k_j)  (bssn.py:78-80) */
@@ -393,14 +416,16 @@ void orc_bssn_point(const orc_point *P, const double *prm, double eta, double *o
             lap += chi * ig[i][j] * DDa[i][j];
             sqrA += P->At[i][j] * AUU[i][j];
         }
-    for (int i = 0; i < 3; i++) advK += P->b[i] * P->dK[i];
+    if (P->upwind) advK = P->adv[K_];
+    else for (int i = 0; i < 3; i++) advK += P->b[i] * P->dK[i];
     const double K_rhs = advK - lap + a * (K * K / 3.0 + sqrA);
 
     /* Gt, B (bssn.py:86-104) */
     double Gt_rhs[3], B_rhs[3];
     for (int i = 0; i < 3; i++) {
         double s = 0.0;
-        for (int j = 0; j < 3; j++) s += P->b[j] * P->dGt[i][j];
+        if (P->upwind) s = P->adv[GT0_ + i];
+        else for (int j = 0; j < 3; j++) s += P->b[j] * P->dGt[i][j];
         for (int j = 0; j < 3; j++) s -= CalGt[j] * P->db[i][j];
         s += 2.0 / 3.0 * CalGt[i] * divb;
         for (int j = 0; j < 3; j++)
@@ -415,9 +440,14 @@ void orc_bssn_point(const orc_point *P, const double *prm, double eta, double *o
     }
     for (int i = 0; i < 3; i++) {
         double sB = 0.0, sG = 0.0;
-        for (int j = 0; j < 3; j++) {
-            sB += P->b[j] * P->dB[i][j];
-            sG += P->b[j] * P->dGt[i][j];
+        if (P->upwind) {
+            sB = P->adv[B0_ + i];
+            sG = P->adv[GT0_ + i];
+        } else {
+            for (int j = 0; j < 3; j++) {
+                sB += P->b[j] * P->dB[i][j];
+                sG += P->b[j] * P->dGt[i][j];
+            }
         }
         B_rhs[i] = Gt_rhs[i] - eta * P->B[i] + l3 * sB - l4 * sG;
     }
@@ -449,37 +479,67 @@ static const double BC_FALLOFF[NV] = {1, 1, 1, 2, 2, 2, 1, 1, 1, 1, 1, 1,
 static const double BC_ASYM[NV] = {1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
                                    1, 0, 0, 1, 0, 1, 0, 0, 0, 0, 0, 0};
 
-/* apply_bcs = 0 skips bssn_bcs (used to pin the closures alone against the
- * reference harness, which cannot compile bssn_bcs). */
-int orc_bssnrhs_ex(double **rhs, const double **uz, unsigned long offset,
-                   const double *pmin, const double *pmax, const unsigned *sz,
-                   unsigned bflag, const double *prm, int apply_bcs)
+void orc_deriv42(int dir, double *D, const double *u, double h, const unsigned *sz, unsigned bflag);
+void orc_deriv42_2(int dir, double *D, const double *u, double h, const unsigned *sz, unsigned bflag);
+void orc_bssn_adv42(int dir, double *D, const double *u, double h, const unsigned *sz,
+                    const double *beta, unsigned bflag);
+
+/* apply_bcs = 0 skips bssn_bcs.  order 6: the QuadGrav binding
+ * (QuadGrav/include/derivs.h:80-97: deriv64 first and second derivatives,
+ * the centred deriv64adv as advective derivative, ko_deriv42); order 4: the
+ * BSSN_GR solver's own binding (BSSN_GR/include/rhs.h:23-37: deriv42,
+ * upwinded deriv42adv, ko_deriv42). */
+int orc_bssnrhs_ex2(double **rhs, const double **uz, unsigned long offset,
+                    const double *pmin, const double *pmax, const unsigned *sz,
+                    unsigned bflag, const double *prm, int apply_bcs, int order)
 {
     if (bflag != 0 && (sz[0] < 13 || sz[1] < 13 || sz[2] < 13)) return -1;
+    if (order != 4 && order != 6) return -3;
     const int nx = sz[0], ny = sz[1], nz = sz[2];
     const size_t n = (size_t)nx * ny * nz;
     const double h[3] = {(pmax[0] - pmin[0]) / (nx - 1), (pmax[1] - pmin[1]) / (ny - 1),
                          (pmax[2] - pmin[2]) / (nz - 1)};
-    /* grad[v][d] and, for HAS_D2 fields, grad2[v][0..5] = xx,xy,xz,yy,yz,zz */
-    double *grad[NV][3], *grad2[NV][6];
-    double *pool = (double *)malloc(sizeof(double) * n * (NV * 3 + 11 * 6));
+    /* grad[v][d] and, for HAS_D2 fields, grad2[v][0..5] = xx,xy,xz,yy,yz,zz;
+     * at order 4 also the upwinded agrad[v][d] */
+    double *grad[NV][3], *grad2[NV][6], *agrad[NV][3];
+    const size_t narr = NV * 3 + 11 * 6 + (order == 4 ? NV * 3 : 0);
+    double *pool = (double *)malloc(sizeof(double) * n * narr);
     if (!pool) return -2;
     double *p = pool;
     for (int v = 0; v < NV; v++) {
         for (int d = 0; d < 3; d++) { grad[v][d] = p; p += n; }
         for (int q = 0; q < 6; q++) grad2[v][q] = NULL;
         if (HAS_D2[v]) for (int q = 0; q < 6; q++) { grad2[v][q] = p; p += n; }
+        for (int d = 0; d < 3; d++) {
+            agrad[v][d] = order == 4 ? p : NULL;
+            if (order == 4) p += n;
+        }
     }
     for (int v = 0; v < NV; v++) {
         const double *u = uz[v] + offset;
-        for (int d = 0; d < 3; d++) orc_deriv64(d, grad[v][d], u, h[d], sz, bflag);
-        if (HAS_D2[v]) {
-            orc_deriv64_2(0, grad2[v][0], u, h[0], sz, bflag);
-            orc_deriv64_2(1, grad2[v][3], u, h[1], sz, bflag);
-            orc_deriv64_2(2, grad2[v][5], u, h[2], sz, bflag);
-            orc_deriv64(1, grad2[v][1], grad[v][0], h[1], sz, bflag); /* d_y(d_x u) */
-            orc_deriv64(2, grad2[v][2], grad[v][0], h[2], sz, bflag); /* d_z(d_x u) */
-            orc_deriv64(2, grad2[v][4], grad[v][1], h[2], sz, bflag); /* d_z(d_y u) */
+        if (order == 6) {
+            for (int d = 0; d < 3; d++) orc_deriv64(d, grad[v][d], u, h[d], sz, bflag);
+            if (HAS_D2[v]) {
+                orc_deriv64_2(0, grad2[v][0], u, h[0], sz, bflag);
+                orc_deriv64_2(1, grad2[v][3], u, h[1], sz, bflag);
+                orc_deriv64_2(2, grad2[v][5], u, h[2], sz, bflag);
+                orc_deriv64(1, grad2[v][1], grad[v][0], h[1], sz, bflag); /* d_y(d_x u) */
+                orc_deriv64(2, grad2[v][2], grad[v][0], h[2], sz, bflag); /* d_z(d_x u) */
+                orc_deriv64(2, grad2[v][4], grad[v][1], h[2], sz, bflag); /* d_z(d_y u) */
+            }
+        } else {
+            for (int d = 0; d < 3; d++) {
+                orc_deriv42(d, grad[v][d], u, h[d], sz, bflag);
+                orc_bssn_adv42(d, agrad[v][d], u, h[d], sz, uz[BETA0_ + d] + offset, bflag);
+            }
+            if (HAS_D2[v]) {
+                orc_deriv42_2(0, grad2[v][0], u, h[0], sz, bflag);
+                orc_deriv42_2(1, grad2[v][3], u, h[1], sz, bflag);
+                orc_deriv42_2(2, grad2[v][5], u, h[2], sz, bflag);
+                orc_deriv42(1, grad2[v][1], grad[v][0], h[1], sz, bflag);
+                orc_deriv42(2, grad2[v][2], grad[v][0], h[2], sz, bflag);
+                orc_deriv42(2, grad2[v][4], grad[v][1], h[2], sz, bflag);
+            }
         }
     }
     static const int Q[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
@@ -530,6 +590,13 @@ int orc_bssnrhs_ex(double **rhs, const double **uz, unsigned long offset,
                             for (int b2 = 0; b2 < 3; b2++)
                                 P.ddgt[a2][b2][l][m] = grad2[SGT0_ + SYM[a2][b2]][q][pp];
                     }
+                P.upwind = order == 4;
+                if (P.upwind)
+                    for (int v = 0; v < NV; v++) {
+                        double t = 0.0;
+                        for (int d = 0; d < 3; d++) t += P.b[d] * agrad[v][d][pp];
+                        P.adv[v] = t;
+                    }
                 double out[NV];
                 orc_bssn_point(&P, prm, eta, out);
                 for (int v = 0; v < NV; v++) rhs[v][offset + pp] = out[v];
@@ -557,19 +624,26 @@ int orc_bssnrhs_ex(double **rhs, const double **uz, unsigned long offset,
     return 0;
 }
 
+int orc_bssnrhs_ex(double **rhs, const double **uz, unsigned long offset,
+                   const double *pmin, const double *pmax, const unsigned *sz,
+                   unsigned bflag, const double *prm, int apply_bcs)
+{
+    return orc_bssnrhs_ex2(rhs, uz, offset, pmin, pmax, sz, bflag, prm, apply_bcs, 6);
+}
+
 int orc_bssnrhs(double **rhs, const double **uz, unsigned long offset, const double *pmin,
                 const double *pmax, const unsigned *sz, unsigned bflag, const double *prm)
 {
-    return orc_bssnrhs_ex(rhs, uz, offset, pmin, pmax, sz, bflag, prm, 1);
+    return orc_bssnrhs_ex2(rhs, uz, offset, pmin, pmax, sz, bflag, prm, 1, 6);
 }
 
 /* bssnRHS over a block list (BSSN_GR/src/rhs.cpp:9-76), OpenMP over blocks
  * as the reference test bed does (BSSN_GR/src/rhsTestBed.cpp:181-215).
  * blk[] rows: offset, sz0, sz1, sz2, bflag (as doubles are avoided: ulong). */
-int orc_bssnrhs_blocks(double **rhs, const double **uz, long nblk,
-                       const unsigned long *offsets, const unsigned *sizes /*3 per block*/,
-                       const unsigned *bflags, const double *pmins, const double *pmaxs,
-                       const double *prm, int nthreads)
+int orc_bssnrhs_blocks_ex(double **rhs, const double **uz, long nblk,
+                          const unsigned long *offsets, const unsigned *sizes /*3 per block*/,
+                          const unsigned *bflags, const double *pmins, const double *pmaxs,
+                          const double *prm, int nthreads, int order)
 {
     int err = 0;
 #ifdef _OPENMP
@@ -577,10 +651,19 @@ int orc_bssnrhs_blocks(double **rhs, const double **uz, long nblk,
 #pragma omp parallel for schedule(dynamic) reduction(|:err)
 #endif
     for (long b = 0; b < nblk; b++)
-        err |= -orc_bssnrhs(rhs, uz, offsets[b], pmins + 3 * b, pmaxs + 3 * b,
-                            sizes + 3 * b, bflags[b], prm);
+        err |= -orc_bssnrhs_ex2(rhs, uz, offsets[b], pmins + 3 * b, pmaxs + 3 * b,
+                                sizes + 3 * b, bflags[b], prm, 1, order);
     (void)nthreads;
     return -err;
+}
+
+int orc_bssnrhs_blocks(double **rhs, const double **uz, long nblk,
+                       const unsigned long *offsets, const unsigned *sizes /*3 per block*/,
+                       const unsigned *bflags, const double *pmins, const double *pmaxs,
+                       const double *prm, int nthreads)
+{
+    return orc_bssnrhs_blocks_ex(rhs, uz, nblk, offsets, sizes, bflags, pmins, pmaxs, prm,
+                                 nthreads, 6);
 }
 
 /* ---------------- RK4 stage update + constraints ---------------- */

@@ -35,10 +35,14 @@ void orc_bssn_bcs(double *f_rhs, const double *f, const double *dxf, const doubl
                   const double *dzf, const double *pmin, const double *pmax,
                   double falloff, double asym, const unsigned *sz, unsigned bflag);
 
-/* Upwind advective derivative along dir (CCZ4_GR/src/derivs.cpp:495-915):
- * interior points of the block, biased by the sign of beta_dir. */
-void orc_ccz4_adv42(int dir, double *D, const double *u, double h, const unsigned *sz,
-                    const double *beta, unsigned bflag)
+/* Upwind advective derivative along dir (CCZ4_GR/src/derivs.cpp:495-915;
+ * BSSN_GR/src/derivs.cpp:494-913 and its copy in QuadGrav/src/derivs.cpp):
+ * interior points of the block, biased by the sign of beta_dir.  The two
+ * solvers' files differ in one test only, at the point ie-3 of a flagged high
+ * face: the CCZ4 file takes the one-sided forward form where beta < 0
+ * (ccz4_hi != 0), the BSSN file where beta > 0. */
+static void adv42(int dir, double *D, const double *u, double h, const unsigned *sz,
+                  const double *beta, unsigned bflag, int ccz4_hi)
 {
     const int nx = sz[0], ny = sz[1], nz = sz[2];
     const double idx = 1.0 / h, half = 0.50 * idx, c12 = idx / 12.0;
@@ -78,7 +82,7 @@ void orc_ccz4_adv42(int dir, double *D, const double *u, double h, const unsigne
                     : (U(3) - 4.0 * U(4) + 3.0 * U(5)) * half;
             }
             if (hi) {
-                O[(ie - 3) * s] = B[(ie - 3) * s] < 0.0
+                O[(ie - 3) * s] = (ccz4_hi ? B[(ie - 3) * s] < 0.0 : B[(ie - 3) * s] > 0.0)
                     ? (-3.0 * U(ie - 3) + 4.0 * U(ie - 2) - U(ie - 1)) * half
                     : (-U(ie - 6) + 6.0 * U(ie - 5) - 18.0 * U(ie - 4) + 10.0 * U(ie - 3)
                        + 3.0 * U(ie - 2)) * c12;
@@ -88,6 +92,18 @@ void orc_ccz4_adv42(int dir, double *D, const double *u, double h, const unsigne
             }
 #undef U
         }
+}
+
+void orc_ccz4_adv42(int dir, double *D, const double *u, double h, const unsigned *sz,
+                    const double *beta, unsigned bflag)
+{
+    adv42(dir, D, u, h, sz, beta, bflag, 1);
+}
+
+void orc_bssn_adv42(int dir, double *D, const double *u, double h, const unsigned *sz,
+                    const double *beta, unsigned bflag)
+{
+    adv42(dir, D, u, h, sz, beta, bflag, 0);
 }
 
 /* Kreiss-Oliger dissipation of the CCZ4 solver (CCZ4_GR/src/derivs.cpp:917-1347):

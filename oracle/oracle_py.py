@@ -53,6 +53,13 @@ class Oracle:
         L.orc_bssnrhs_ex.restype = C.c_int
         L.orc_bssnrhs_ex.argtypes = [_PP, _PP, C.c_ulong, _D, _D, C.POINTER(C.c_uint), C.c_uint,
                                      _D, C.c_int]
+        L.orc_bssnrhs_ex2.restype = C.c_int
+        L.orc_bssnrhs_ex2.argtypes = [_PP, _PP, C.c_ulong, _D, _D, C.POINTER(C.c_uint), C.c_uint,
+                                      _D, C.c_int, C.c_int]
+        L.orc_bssnrhs_blocks_ex.restype = C.c_int
+        L.orc_bssnrhs_blocks_ex.argtypes = [_PP, _PP, C.c_long, C.POINTER(C.c_ulong),
+                                            C.POINTER(C.c_uint), C.POINTER(C.c_uint), _D, _D, _D,
+                                            C.c_int, C.c_int]
         L.orc_bssnrhs_blocks.restype = C.c_int
         L.orc_bssnrhs_blocks.argtypes = [_PP, _PP, C.c_long, C.POINTER(C.c_ulong),
                                          C.POINTER(C.c_uint), C.POINTER(C.c_uint), _D, _D, _D,
@@ -117,8 +124,9 @@ class Oracle:
         self.L.orc_synth_fill(C.addressof(blocks), len(blocks), pp, len(fields), seed, noise,
                               nthreads or (os.cpu_count() or 1))
 
-    def bssnrhs_blocks(self, rhs, u, blocks, prm, nthreads=0):
-        """bssnRHS over a block list (list of dgb BlockDesc)."""
+    def bssnrhs_blocks(self, rhs, u, blocks, prm, nthreads=0, order=6):
+        """bssnRHS over a block list (list of dgb BlockDesc); order 6: the
+        QuadGrav binding, 4: the BSSN_GR solver's (upwinded advection)."""
         n = len(blocks)
         off = (C.c_ulong * n)(*[b.offset for b in blocks])
         sz = (C.c_uint * (3 * n))(*[s for b in blocks for s in b.sz])
@@ -128,8 +136,9 @@ class Oracle:
         r, k1 = _ptrs(rhs)
         uu, k2 = _ptrs(u)
         p = np.ascontiguousarray(prm, dtype=np.float64)
-        return self.L.orc_bssnrhs_blocks(r, uu, n, off, sz, bf, pmin.ctypes.data_as(_D),
-                                         pmax.ctypes.data_as(_D), p.ctypes.data_as(_D), nthreads)
+        return self.L.orc_bssnrhs_blocks_ex(r, uu, n, off, sz, bf, pmin.ctypes.data_as(_D),
+                                            pmax.ctypes.data_as(_D), p.ctypes.data_as(_D),
+                                            nthreads, order)
 
     def stencil(self, kind, dirn, u3, h, bflag=0):
         """kind in {'d1','d2','ko'} on a 3-D array u3[z][y][x]; returns D (zeros
@@ -218,16 +227,16 @@ class Oracle:
                                              nthreads or os.cpu_count())
         return wmax, flags, int(changed)
 
-    def bssnrhs_block(self, rhs, u, block, prm, apply_bcs=True):
+    def bssnrhs_block(self, rhs, u, block, prm, apply_bcs=True, order=6):
         r, k1 = _ptrs(rhs)
         uu, k2 = _ptrs(u)
         pmin = np.array(list(block.ptmin), dtype=np.float64)
         pmax = np.array(list(block.ptmax), dtype=np.float64)
         sz = (C.c_uint * 3)(*block.sz)
         p = np.ascontiguousarray(prm, dtype=np.float64)
-        return self.L.orc_bssnrhs_ex(r, uu, block.offset, pmin.ctypes.data_as(_D),
-                                     pmax.ctypes.data_as(_D), sz, block.bflag,
-                                     p.ctypes.data_as(_D), 1 if apply_bcs else 0)
+        return self.L.orc_bssnrhs_ex2(r, uu, block.offset, pmin.ctypes.data_as(_D),
+                                      pmax.ctypes.data_as(_D), sz, block.bflag,
+                                      p.ctypes.data_as(_D), 1 if apply_bcs else 0, order)
 
     def rk4_stage(self, s, dst, prev, k, dt, chi_floor):
         n = dst[0].size
@@ -304,6 +313,10 @@ class Reference:
         L = C.CDLL(path)
         L.ref_bssnrhs.restype = C.c_int
         L.ref_bssnrhs.argtypes = [_PP, _PP, C.c_uint, _D, _D, C.POINTER(C.c_uint), C.c_uint, _D]
+        L.ref_bssnrhs42.restype = C.c_int
+        L.ref_bssnrhs42.argtypes = [_PP, _PP, C.c_uint, _D, _D, C.POINTER(C.c_uint), C.c_uint, _D]
+        L.ref_deriv42adv.restype = None
+        L.ref_deriv42adv.argtypes = [C.c_int, _D, _D, C.c_double, C.POINTER(C.c_uint), _D, C.c_uint]
         L.ref_enforce_bssn_constraints.restype = None
         L.ref_enforce_bssn_constraints.argtypes = [_PP, C.c_uint, C.c_double]
         L.ref_physical_constraints.restype = C.c_int
@@ -318,15 +331,28 @@ class Reference:
             f.argtypes = [_D, _D, C.c_double, C.POINTER(C.c_uint), C.c_uint]
         self.L = L
 
-    def bssnrhs(self, rhs, u, block, prm):
+    def bssnrhs(self, rhs, u, block, prm, order=6):
+        """The reference's bssnrhs on one block; order 6: QuadGrav's binding,
+        4: the BSSN_GR solver's (ref_bssnrhs42)."""
         r, k1 = _ptrs(rhs)
         uu, k2 = _ptrs(u)
         pmin = np.array(list(block.ptmin), dtype=np.float64)
         pmax = np.array(list(block.ptmax), dtype=np.float64)
         sz = (C.c_uint * 3)(*block.sz)
         p = np.ascontiguousarray(prm, dtype=np.float64)
-        return self.L.ref_bssnrhs(r, uu, block.offset, pmin.ctypes.data_as(_D),
-                                  pmax.ctypes.data_as(_D), sz, block.bflag, p.ctypes.data_as(_D))
+        fn = self.L.ref_bssnrhs42 if order == 4 else self.L.ref_bssnrhs
+        return fn(r, uu, block.offset, pmin.ctypes.data_as(_D), pmax.ctypes.data_as(_D), sz,
+                  block.bflag, p.ctypes.data_as(_D))
+
+    def adv42(self, dirn, u3, h, beta3, bflag=0):
+        """The BSSN_GR solver's upwinded deriv42adv along dirn on u3[z][y][x]."""
+        u = np.ascontiguousarray(u3, dtype=np.float64)
+        b = np.ascontiguousarray(beta3, dtype=np.float64)
+        D = np.zeros_like(u)
+        sz = (C.c_uint * 3)(u.shape[2], u.shape[1], u.shape[0])
+        self.L.ref_deriv42adv(dirn, D.ctypes.data_as(_D), u.ctypes.data_as(_D), h, sz,
+                              b.ctypes.data_as(_D), bflag)
+        return D
 
     def stencil(self, kind, dirn, u3, h, bflag=0):
         nm = {"d1": ["ref_deriv64_x", "ref_deriv64_y", "ref_deriv64_z"],

@@ -103,6 +103,44 @@ def main():
     print("wrote", os.path.join(HERE, "bssn_reference.npz"))
     constraint_goldens(dgb, ref)
     ccz4_goldens(dgb)
+    bssn42_goldens(dgb, ref)
+
+
+def shifted_fields(dgb, blocks, seed):
+    """Seeded synthetic fields with an oscillating shift of size 0.3 added,
+    so that every upwinded stencil form is taken."""
+    n = dgb.unzipped_size(blocks)
+    u = [np.zeros(n) for _ in range(24)]
+    dgb.synth_fill_host(blocks, u, seed, 1e-6)
+    for d in range(3):
+        u[6 + d] += 0.3 * np.sin(np.arange(n) * (0.37 + d))
+    return u
+
+
+def bssn42_goldens(dgb, ref):
+    """bssnrhs with the BSSN_GR solver's own binding (deriv42, upwinded
+    deriv42adv, ko_deriv42; BSSN_GR/include/rhs.h:23-37) from the reference
+    build (oracle/ref_bssnrhs42.cpp) on the puncture block, a generic block
+    and two domain-boundary corner blocks (closures and bssn_bcs)."""
+    allb = dgb.synth_blocks(1)
+    picks = [(288, 0), (100, 0), (0, 1 | 4 | 16), (511, 2 | 8 | 32)]
+    rows, off = [], 0
+    for i, f in picks:
+        b = allb[i]
+        rows.append((off, tuple(b.sz), f, tuple(b.ptmin), tuple(b.ptmax)))
+        off += b.sz[0] * b.sz[1] * b.sz[2]
+    blocks = dgb.blocks_array(rows)
+    u = shifted_fields(dgb, blocks, SEED1)
+    n = len(u[0])
+    prm = dgb.params_vector(dgb.default_params(SIGMA))
+    r = [np.zeros(n) for _ in range(24)]
+    for b in blocks:
+        assert ref.bssnrhs(r, u, b, prm, order=4) == 0
+    mask = interior_mask(blocks, n)
+    np.savez_compressed(
+        os.path.join(HERE, "bssn42_reference.npz"), picks=np.array(picks), seed=np.array(SEED1),
+        sigma=np.array(SIGMA), input_sha256=np.array(sha(u)), rhs=np.stack([x[mask] for x in r]))
+    print("wrote", os.path.join(HERE, "bssn42_reference.npz"))
 
 
 def axis_block(dgb, blocks):
@@ -262,6 +300,9 @@ if __name__ == "__main__":
     if sys.argv[1:] == ["mesh"]:
         oracle_py.build_ref()
         mesh_goldens(load_dgb())
+    elif sys.argv[1:] == ["bssn42"]:
+        oracle_py.build_ref()
+        bssn42_goldens(load_dgb(), oracle_py.Reference())
     else:
         main()
         mesh_goldens(load_dgb())
