@@ -22,7 +22,16 @@ Accessors the including kernel supplies on `io`:
   io.out(v, x)   right-hand side of field v before KO dissipation
 and a `prm` object with l1..l4, lf0, lf1.
 
+With --upwind it emits csrc/bssn_algebra42.cuh instead: the same system for
+the BSSN_GR solver's 4th-order binding, where the advective derivative of
+every field is the upwinded one (BSSN_GR/include/rhs.h:23-37).  The system
+uses advective derivatives only as beta^j ad(j, f) (dendro.py lie :225-248,
+vec_j_ad_j :348-353; bssn.py Gt_rhs :86 and B_rhs :100-104), so the kernel
+supplies that sum per field, io.d(ADV0 + v), and the algebra reads it in
+place of beta^j d_j f.
+
 Run:  python gen_bssn_algebra.py > ../csrc/bssn_algebra.cuh
+      python gen_bssn_algebra.py --upwind > ../csrc/bssn_algebra42.cuh
 """
 import sys
 
@@ -39,6 +48,8 @@ NUM_GRAD = 72
 NUM_D2 = 6 * len(D2_FIELDS)       # xx, xy, xz, yy, yz, zz per field
 NUM_DERIV = NUM_GRAD + NUM_D2      # 138
 NUM_SLOTS = NUM_DERIV + 24         # + KO sums
+ADV0 = NUM_SLOTS                   # upwind form: advection sums beta^j ad_j f per field
+NUM_SLOTS_UPWIND = ADV0 + 24
 
 
 def slot_grad(var, d):
@@ -84,8 +95,15 @@ def sum_terms(terms):
     return out
 
 
-def generate():
+def generate(upwind=False):
     e = Emitter()
+
+    def adv_of(var, centred):
+        """beta^j ad(j, var): the kernel's upwinded sum, or the centred terms
+        (centred is called only then, so no unused derivative is loaded)."""
+        if upwind:
+            return [e.d(ADV0 + V[var])]
+        return centred()
     f = {n: f"u_{n}" for n in VARS}
     for n in VARS:
         e.let(f[n], f"io.u({V[n]})")
@@ -220,20 +238,20 @@ def generate():
     e.let("w_divb", "(-2.0 / 3.0) * divb")
 
     e.comment("lapse and shift (bssn.py:65-72)")
-    adv_a = sum_terms([f"{b[i]} * {da[i]}" for i in range(3)])
+    adv_a = sum_terms(adv_of("alpha", lambda: [f"{b[i]} * {da[i]}" for i in range(3)]))
     e.lines.append(f"    io.out(0, prm.l1 * ({adv_a}) - 2.0 * {a} * {K});")
     e.let("bfac", f"0.75 * (prm.lf0 + prm.lf1 * {a})")
     for i in range(3):
-        adv = sum_terms([f"{b[j]} * {dvec('beta', i, j)}" for j in range(3)])
+        adv = sum_terms(adv_of(f"beta{i}", lambda: [f"{b[j]} * {dvec('beta', i, j)}" for j in range(3)]))
         e.lines.append(f"    io.out({V['beta0'] + i}, bfac * {B[i]} + prm.l2 * ({adv}));")
 
     e.comment("chi (bssn.py:76)")
-    adv = sum_terms([f"{b[i]} * {dchi[i]}" for i in range(3)])
+    adv = sum_terms(adv_of("chi", lambda: [f"{b[i]} * {dchi[i]}" for i in range(3)]))
     e.lines.append(f"    io.out(1, {adv} + w_divb * {chi} + (2.0 / 3.0) * ({chi} * {a} * {K}));")
 
     e.comment("gt: Lie derivative of weight -2/3 minus 2 alpha At (bssn.py:74)")
     for (i, j) in PAIRS:
-        terms = [f"{b[k]} * {dg(i, j, k)}" for k in range(3)]
+        terms = adv_of(gtname[SYM[i][j]], lambda: [f"{b[k]} * {dg(i, j, k)}" for k in range(3)])
         terms += [f"{g[i][k]} * {dvec('beta', k, j)}" for k in range(3)]
         terms += [f"{g[k][j]} * {dvec('beta', k, i)}" for k in range(3)]
         terms += [f"w_divb * {g[i][j]}", f"-2.0 * {a} * {A[i][j]}"]
@@ -249,7 +267,7 @@ def generate():
         for j in range(3):
             AUd[k][j] = e.let(f"AUd_{k}{j}", sum_terms([f"{ig[k][l]} * {A[l][j]}" for l in range(3)]))
     for (i, j) in PAIRS:
-        lie = [f"{b[k]} * {dA(i, j, k)}" for k in range(3)]
+        lie = adv_of(Atname[SYM[i][j]], lambda: [f"{b[k]} * {dA(i, j, k)}" for k in range(3)])
         lie += [f"{A[i][k]} * {dvec('beta', k, j)}" for k in range(3)]
         lie += [f"{A[k][j]} * {dvec('beta', k, i)}" for k in range(3)]
         lie += [f"w_divb * {A[i][j]}"]
@@ -266,7 +284,7 @@ def generate():
     # sqr(At) = sum_ij At_ij At^ij (dendro.py:305)
     e.let("sqrA", symcontract_plain(A, AUU))
     e.let("lapa", f"{chi} * ({symcontract(DDa)})")
-    advK = sum_terms([f"{b[i]} * {dK[i]}" for i in range(3)])
+    advK = sum_terms(adv_of("K", lambda: [f"{b[i]} * {dK[i]}" for i in range(3)]))
     e.lines.append(f"    io.out(2, {advK} - lapa + {a} * ({K} * {K} * (1.0 / 3.0) + sqrA));")
 
     e.comment("Gt and B (bssn.py:86-104)")
@@ -278,7 +296,7 @@ def generate():
     for j in range(3):
         ddb_div.append(e.let(f"ddbdiv{j}", sum_terms([dd(f"beta{k}", j, k) for k in range(3)])))
     for i in range(3):
-        terms = [f"{b[j]} * {dvec('Gt', i, j)}" for j in range(3)]
+        terms = adv_of(f"Gt{i}", lambda: [f"{b[j]} * {dvec('Gt', i, j)}" for j in range(3)])
         terms += [f"-{CalGt[j]} * {dvec('beta', i, j)}" for j in range(3)]
         terms += [f"{CalGt[i]} * CalGt_divb"]
         terms += [symcontract([[dd(f"beta{i}", l, m) for m in range(3)] for l in range(3)])]
@@ -289,8 +307,8 @@ def generate():
         e.let(f"Gtr{i}", sum_terms(terms))
         e.lines.append(f"    io.out({V['Gt0'] + i}, Gtr{i});")
     for i in range(3):
-        advB = sum_terms([f"{b[j]} * {dvec('B', i, j)}" for j in range(3)])
-        advG = sum_terms([f"{b[j]} * {dvec('Gt', i, j)}" for j in range(3)])
+        advB = sum_terms(adv_of(f"B{i}", lambda: [f"{b[j]} * {dvec('B', i, j)}" for j in range(3)]))
+        advG = sum_terms(adv_of(f"Gt{i}", lambda: [f"{b[j]} * {dvec('Gt', i, j)}" for j in range(3)]))
         e.lines.append(f"    io.out({V['B0'] + i}, Gtr{i} - eta * {B[i]} + prm.l3 * ({advB})"
                        f" - prm.l4 * ({advG}));")
     return e
@@ -326,9 +344,34 @@ __device__ __forceinline__ void dgb_bssn_algebra(IO &io, const PRM &prm, const d
 """
 
 
+HEADER_UPWIND = """// GENERATED by codegen/gen_bssn_algebra.py --upwind -- do not edit by hand.
+// Per-point BSSN right-hand side (eta constant, standard gauge) of the
+// reference's CodeGen/bssn.py:36-96 for the BSSN_GR solver's 4th-order binding
+// (BSSN_GR/include/rhs.h:23-37): the advection terms beta^j ad(j, f) are read
+// from slot {adv} + v (the kernel's sums of upwinded derivatives).
+#pragma once
+
+#define DGB_B42_ADV0 {adv}
+#define DGB_B42_NUM_SLOTS {ns}
+// grad slot of (var v, direction d) = 3 v + d; second derivatives of the
+// D2 fields (alpha, chi, beta0..2, gt0..5, in that order q) at
+// {ng} + 6 q + (xx, xy, xz, yy, yz, zz); KO sums at {nd} + v; advection
+// sums at {adv} + v.
+
+template <class IO, class PRM>
+__device__ __forceinline__ void dgb_bssn_algebra_upwind(IO &io, const PRM &prm, const double eta)
+{{
+"""
+
+
 def main():
-    e = generate()
-    sys.stdout.write(HEADER.format(ng=NUM_GRAD, nd2=NUM_D2, nd=NUM_DERIV, ns=NUM_SLOTS))
+    upwind = "--upwind" in sys.argv[1:]
+    e = generate(upwind)
+    if upwind:
+        sys.stdout.write(HEADER_UPWIND.format(ng=NUM_GRAD, nd=NUM_DERIV, adv=ADV0,
+                                              ns=NUM_SLOTS_UPWIND))
+    else:
+        sys.stdout.write(HEADER.format(ng=NUM_GRAD, nd2=NUM_D2, nd=NUM_DERIV, ns=NUM_SLOTS))
     sys.stdout.write("\n".join(e.lines))
     sys.stdout.write("\n}\n")
 

@@ -70,6 +70,7 @@ struct dgb_plan {
     int pc_occupancy = 0;      // constraint kernel, resident CTAs per SM (0 = not yet known)
     // CCZ4 kernel: its own workspace (241 slots per point), allocated at first use
     int c4_occupancy[2] = {0, 0};  // per precision
+    int b4_occupancy = 0;          // the 4th-order BSSN kernel (same workspace buffer)
     double *d_scratch4 = nullptr;
     size_t scratch4_doubles = 0;
     // host-array entry point: chunked pipeline, built at first use
@@ -287,6 +288,9 @@ RhsParams rhs_params(const dgb_bssn_params &q)
 dgb_status run_rhs_on(dgb_plan *p, double *const *rhs, const double *const *u, int precision,
                       int variant, const WorkItem *items, uint32_t nitems, cudaStream_t st);
 
+dgb_status run_rhs42(dgb_plan *p, double *const *rhs, const double *const *u, int precision,
+                     cudaStream_t st);
+
 dgb_status run_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int precision,
                    int variant, cudaStream_t st)
 {
@@ -294,6 +298,7 @@ dgb_status run_rhs(dgb_plan *p, double *const *rhs, const double *const *u, int 
         set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
         return DGB_ERR_INVALID;
     }
+    if (p->prm.fd_order == 4) return run_rhs42(p, rhs, u, precision, st);
     const WorkItem *items = nullptr;
     uint32_t nitems = 0;
     dgb_status s = rhs_items(p, variant, precision == DGB_PREC_MIXED ? 1 : 0, &items, &nitems);
@@ -333,6 +338,11 @@ dgb_status dgb::run_rhs_gather(dgb_plan *p, double *const *k, const double *cons
     if (precision != DGB_PREC_FP64 && precision != DGB_PREC_MIXED) {
         set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
         return DGB_ERR_INVALID;
+    }
+    if (p->prm.fd_order == 4) {
+        set_error("the fused-unzip stepper runs the 6th-order binding only (fd_order 4: use the "
+                  "unfused stepper)");
+        return DGB_ERR_UNSUPPORTED;
     }
     const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
     const int variant = p->variant[prec];
@@ -463,10 +473,21 @@ dgb_status dgb_plan_create(const dgb_block_desc *blocks, size_t nblk, const dgb_
         set_error("too many blocks");
         return DGB_ERR_INVALID;
     }
+    if (prm->fd_order != 0 && prm->fd_order != 4 && prm->fd_order != 6) {
+        set_error("dgb_plan_create: fd_order must be 4 or 6 (0 = 6)");
+        return DGB_ERR_INVALID;
+    }
+    if (prm->gauge != DGB_GAUGE_ETA_CONST) {
+        set_error("dgb_plan_create: only the standard gauge with constant eta "
+                  "(bssneqs_eta_const_standard_gauge) is built; the eta-function and "
+                  "Rochester-gauge equations are not");
+        return DGB_ERR_UNSUPPORTED;
+    }
     dgb_plan *p = new dgb_plan();
     p->device = g_device;
     p->nsm = g_nsm;
     p->prm = *prm;
+    if (p->prm.fd_order == 0) p->prm.fd_order = 6;
     p->blocks.assign(blocks, blocks + nblk);
     std::vector<DevBlock> db(nblk);
     std::vector<uint64_t> first(nblk);
@@ -626,6 +647,63 @@ dgb_status dgb_physical_constraints(dgb_plan *p, double *const *cons, const doub
 
 namespace {
 
+// The 4th-order BSSN kernel's residency and workspace (the buffer the CCZ4
+// kernel also uses: a plan runs one kernel at a time), at first use.
+dgb_status b4_workspace(dgb_plan *p)
+{
+    if (p->b4_occupancy != 0) return DGB_OK;
+    const int occ = b4_max_ctas_per_sm();
+    if (occ < 1) {
+        set_error("dgb_bssn_rhs (fd_order 4): kernel cannot be resident");
+        return DGB_ERR_CUDA;
+    }
+    const size_t need = b4_scratch_per_cta() * (size_t)occ * (size_t)p->nsm;
+    if (need > p->scratch4_doubles) {
+        if (p->borrowed_scratch) {
+            set_error("dgb_bssn_rhs (fd_order 4): a chunk plan's borrowed workspace is too small");
+            return DGB_ERR_INVALID;
+        }
+        cudaFree(p->d_scratch4);
+        p->d_scratch4 = nullptr;
+        p->scratch4_doubles = 0;
+        p->c4_occupancy[0] = p->c4_occupancy[1] = 0;  // re-checked against the new buffer
+        DGB_CUDA(cudaMalloc(&p->d_scratch4, need * sizeof(double)));
+        p->scratch4_doubles = need;
+    }
+    p->b4_occupancy = occ;
+    return DGB_OK;
+}
+
+// The BSSN right-hand side with the BSSN_GR solver's 4th-order binding.
+dgb_status run_rhs42(dgb_plan *p, double *const *rhs, const double *const *u, int precision,
+                     cudaStream_t st)
+{
+    if (precision != DGB_PREC_FP64) {
+        set_error("dgb_bssn_rhs: fd_order 4 runs in FP64 only");
+        return DGB_ERR_UNSUPPORTED;
+    }
+    dgb_status s = build_items(p, 0);  // the 8x8x8 schedule
+    if (s != DGB_OK) return s;
+    if (p->nitems[0] == 0) return DGB_OK;
+    s = b4_workspace(p);
+    if (s != DGB_OK) return s;
+    DGB_CUDA(b4_configure());
+    RhsArgs a{};
+    for (int v = 0; v < NV; v++) {
+        a.u[v] = u[v];
+        a.rhs[v] = rhs[v];
+    }
+    a.blocks = p->d_blocks;
+    a.items = p->d_items[0];
+    a.nitems = p->nitems[0];
+    a.queue = p->d_queue;
+    a.scratch = p->d_scratch4;
+    a.prm = rhs_params(p->prm);
+    DGB_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned int), st));
+    DGB_CUDA(b4_launch(a, p->nsm * p->b4_occupancy, st));
+    return DGB_OK;
+}
+
 // The CCZ4 kernel's residency and workspace, at first use per precision.
 dgb_status c4_workspace(dgb_plan *p, int precision)
 {
@@ -761,6 +839,8 @@ dgb_status dgb_plan_autotune(dgb_plan *p, double *const *rhs, const double *cons
         set_error("precision must be DGB_PREC_FP64 or DGB_PREC_MIXED");
         return DGB_ERR_INVALID;
     }
+    // the 4th-order kernel has one compiled schedule (8^3 tiles): nothing to choose
+    if (p->prm.fd_order == 4) return DGB_OK;
     cudaStream_t st = (cudaStream_t)stream;
     const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
     // block-size classes
@@ -1203,8 +1283,20 @@ dgb_status dgb_bssn_rhs_host(dgb_plan *p, double *const *rhs, const double *cons
         return DGB_ERR_INVALID;
     }
     if (p->blocks.empty()) return DGB_OK;
-    dgb_status s = ensure_pipe(p);
+    if (p->prm.fd_order == 4 && precision != DGB_PREC_FP64) {
+        set_error("dgb_bssn_rhs_host: fd_order 4 runs in FP64 only");
+        return DGB_ERR_UNSUPPORTED;
+    }
+    // fd_order 4: the chunks run one after another on the parent's workspace
+    dgb_status s = p->prm.fd_order == 4 ? b4_workspace(p) : DGB_OK;
+    if (s == DGB_OK) s = ensure_pipe(p);
     if (s != DGB_OK) return s;
+    if (p->prm.fd_order == 4)
+        for (dgb_plan *sp : p->pipe->sub) {
+            sp->d_scratch4 = p->d_scratch4;
+            sp->scratch4_doubles = p->scratch4_doubles;
+            sp->b4_occupancy = p->b4_occupancy;
+        }
     const int variant = p->variant[precision == DGB_PREC_MIXED ? 1 : 0];
     s = run_pipe(p, rhs, u, NV,
                  [&](dgb_plan *sp, double *const *dr, const double *const *du, cudaStream_t st) {

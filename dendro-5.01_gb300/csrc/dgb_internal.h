@@ -106,6 +106,14 @@ struct C4Args {
     double *scratch;
     C4Params prm;
 };
+// BSSN right-hand side with the BSSN_GR 4th-order binding (bssn42_rhs.cu);
+// the RhsArgs fields of the 6th-order kernel, 8x8x8 schedule, FP64.
+size_t b4_smem_bytes();
+size_t b4_scratch_per_cta();  // doubles
+cudaError_t b4_configure();
+int b4_max_ctas_per_sm();
+cudaError_t b4_launch(const RhsArgs &args, int grid, cudaStream_t stream);
+
 size_t c4_smem_bytes(int precision);
 size_t c4_scratch_per_cta();  // doubles
 cudaError_t c4_configure(int precision);

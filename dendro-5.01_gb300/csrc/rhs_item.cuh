@@ -23,7 +23,9 @@
 //                      advective slots alias the first-derivative slots
 //   KO                 ko_deriv42_{x,y,z} (BSSN_GR/src/derivs.cpp:914-1410),
 //                      rhs += sigma * (kx + ky + kz) (rhs.cpp:336-373)
-// Only interior (bflag == 0) blocks; the host rejects others.
+// Domain-boundary blocks (bflag != 0) take the one-sided closures in phase D
+// and the outgoing-radiation condition bssn_bcs on their flagged faces in
+// phase A (BSSN_GR/src/rhs.cpp:838-982), in FP64 in both precisions.
 //
 // The mixed-precision variant (MIXED = true) splits each staged FP64 value
 // into a float pair hi + lo by integer bit operations (no FP64 pipe work)

@@ -40,7 +40,9 @@ std::mutex g_ws_mutex;
 double *g_ws_ptr[kMaxDevices] = {};
 
 // Device address of the workspace on the current device, looked up once per
-// device (the array's name is only a host-side stand-in in host code).
+// device (the array's name is only a host-side stand-in in host code) and
+// kept for the life of the process: after cudaDeviceReset the kept address
+// belongs to a destroyed context, so the entry must not be used after one.
 dgb_status workspace_on_current_device(double **out)
 {
     int dev = -1;
@@ -105,9 +107,16 @@ extern "C" dgb_status dgb_bssnrhs_block_noalloc(double *const *rhs, const double
             set_error("dgb_bssnrhs_block_noalloc: null field pointer");
             return DGB_ERR_INVALID;
         }
-    if (bflag != 0) {
-        set_error("dgb_bssnrhs_block_noalloc: domain-boundary blocks (bflag != 0) are not "
-                  "supported by this build");
+    if (bflag > 63u) {
+        set_error("dgb_bssnrhs_block_noalloc: bflag has bits beyond the six faces");
+        return DGB_ERR_INVALID;
+    }
+    if (prm->fd_order != 0 && prm->fd_order != 6) {
+        set_error("dgb_bssnrhs_block_noalloc: the 6th-order binding only (fd_order 6 or 0)");
+        return DGB_ERR_UNSUPPORTED;
+    }
+    if (prm->gauge != DGB_GAUGE_ETA_CONST) {
+        set_error("dgb_bssnrhs_block_noalloc: only the constant-eta standard gauge is built");
         return DGB_ERR_UNSUPPORTED;
     }
     NaTiles t;
@@ -116,6 +125,14 @@ extern "C" dgb_status dgb_bssnrhs_block_noalloc(double *const *rhs, const double
     for (int a = 0; a < 3; a++) {
         if (sz[a] < 7 || sz[a] > 4096) {
             set_error("dgb_bssnrhs_block_noalloc: each block side must be in [7, 4096]");
+            return DGB_ERR_INVALID;
+        }
+        if (bflag != 0 && sz[a] < 13) {
+            // the one-sided closures read interior points 3..8 from each flagged
+            // face; with 13 or more points per side the 6^3 cut below gives tiles
+            // of at least 3 points, whose 3-point halo holds those taps
+            set_error("dgb_bssnrhs_block_noalloc: domain-boundary blocks need at least 13 "
+                      "points per side");
             return DGB_ERR_INVALID;
         }
         const int m = (int)sz[a] - 6;
@@ -139,7 +156,7 @@ extern "C" dgb_status dgb_bssnrhs_block_noalloc(double *const *rhs, const double
         return DGB_ERR_INVALID;
     }
     blk.offset = offset;
-    blk.bflag = 0;
+    blk.bflag = bflag;
     double *ws = nullptr;
     dgb_status s = workspace_on_current_device(&ws);
     if (s != DGB_OK) return s;

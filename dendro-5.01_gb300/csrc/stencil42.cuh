@@ -9,8 +9,9 @@
 //   d1_42_at    deriv42_{x,y,z}  (BSSN_GR/src/derivs.cpp:11-242; identical in
 //               CCZ4_GR/src/derivs.cpp), closures at 3,4 / n-5,n-4
 //   d2_42_at    deriv42_{xx,yy,zz} (:244-490)
-//   adv42_at    the CCZ4 solver's upwind deriv42adv_{x,y,z}
-//               (CCZ4_GR/src/derivs.cpp:495-915), biased by sign(beta)
+//   adv42_at    the upwind deriv42adv_{x,y,z} (CCZ4_GR/src/derivs.cpp:495-915;
+//               BSSN_GR/src/derivs.cpp:494-913 differs in one closure test),
+//               biased by sign(beta)
 //   ko42c_at    the CCZ4 solver's ko_deriv42_{x,y,z}
 //               (CCZ4_GR/src/derivs.cpp:917-1347): the centred stencil of
 //               the neighbouring point at the first and last interior
@@ -124,8 +125,11 @@ __device__ __forceinline__ double adv42_neg(const double *c, int s, double c12)
     t = __dadd_rn(t, dgb_mul_const<3>(c[s]));
     return __dmul_rn(t, c12);
 }
+// ccz4_hi: the CCZ4 file's test at the point ie-3 of a flagged high face
+// (forward form where beta < 0); false: the BSSN_GR / QuadGrav files' test
+// (forward form where beta > 0, BSSN_GR/src/derivs.cpp:579).
 __device__ __forceinline__ double adv42_at(const double *c, int s, int pos, int n, bool lo, bool hi,
-                                           double beta, const Ax4 &a)
+                                           double beta, const Ax4 &a, bool ccz4_hi = true)
 {
     const int ie = n - 3;
     if (lo && pos <= 5) {
@@ -134,7 +138,8 @@ __device__ __forceinline__ double adv42_at(const double *c, int s, int pos, int 
         return beta > 0.0 ? adv42_pos(c, s, a.c12) : bwd3(c, s, a.half);
     }
     if (hi && pos >= ie - 3) {
-        if (pos == ie - 3) return beta < 0.0 ? fwd3(c, s, a.half) : adv42_neg(c, s, a.c12);
+        if (pos == ie - 3)
+            return (ccz4_hi ? beta < 0.0 : beta > 0.0) ? fwd3(c, s, a.half) : adv42_neg(c, s, a.c12);
         if (pos == ie - 2) return beta > 0.0 ? ctr2(c, s, a.half) : bwd3(c, s, a.half);
         return bwd3(c, s, a.half);
     }

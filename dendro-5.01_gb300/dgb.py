@@ -35,10 +35,13 @@ class BssnParams(C.Structure):
     _fields_ = [("lambda_", C.c_double * 4), ("lambda_f", C.c_double * 2),
                 ("eta_const", C.c_double), ("eta_r0", C.c_double),
                 ("eta_damping_exp", C.c_double), ("ko_sigma", C.c_double),
-                ("chi_floor", C.c_double)]
+                ("chi_floor", C.c_double), ("fd_order", C.c_int), ("gauge", C.c_int)]
 
 
-def default_params(ko_sigma=0.1):
+GAUGE_ETA_CONST, GAUGE_ETA_FUNC, GAUGE_ROCHESTER_ETA_CONST, GAUGE_ROCHESTER_ETA_FUNC = 0, 1, 2, 3
+
+
+def default_params(ko_sigma=0.1, fd_order=6):
     """lambda = {1,1,1,1}, lambda_f = {1,0}, eta = 2 (R0 = 30, exponent 1),
     chi_floor = 1e-4 (BSSN_GR/pars/bbh.par.json:103-129)."""
     p = BssnParams()
@@ -49,6 +52,8 @@ def default_params(ko_sigma=0.1):
     p.eta_damping_exp = 1.0
     p.ko_sigma = ko_sigma
     p.chi_floor = 1e-4
+    p.fd_order = fd_order
+    p.gauge = GAUGE_ETA_CONST
     return p
 
 

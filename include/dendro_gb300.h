@@ -34,7 +34,8 @@ typedef enum {
     DGB_ERR_CUDA = 2,        /* a CUDA runtime call failed */
     DGB_ERR_ALLOC = 3,       /* device or pinned allocation failed */
     DGB_ERR_NOT_INIT = 4,    /* dgb_init not called / no device */
-    DGB_ERR_TIMEOUT = 5,     /* a bounded device wait expired */
+    DGB_ERR_TIMEOUT = 5,     /* reserved: no entry of this build waits on the device with a
+                                bound, so none returns it */
     DGB_ERR_NONFINITE = 6,   /* NaN/Inf found by a checking entry point */
     DGB_ERR_CONSTRAINT = 7,  /* det(gt) <= 0 in the RK constraint step */
     DGB_ERR_UNSUPPORTED = 8  /* valid request this build does not implement */
@@ -63,7 +64,23 @@ typedef struct {
     double eta_damping_exp;  /* ETA_DAMPING_EXP */
     double ko_sigma;         /* KO_DISS_SIGMA */
     double chi_floor;        /* CHI_FLOOR */
+    /* Finite-difference binding of the right-hand side: 6 (or 0) = the
+     * QuadGrav 6th-order one (QuadGrav/include/derivs.h:80-97: deriv64,
+     * centred advective derivative, ko_deriv42); 4 = the BSSN_GR solver's own
+     * (BSSN_GR/include/rhs.h:23-37: deriv42, upwinded deriv42adv, ko_deriv42),
+     * FP64 only and not in the fused-unzip stepper. */
+    int fd_order;
+    /* Gauge / eta variant of the generated equations (BSSN_GR/src/rhs.cpp:
+     * 226-246): DGB_GAUGE_ETA_CONST (0, the default build's
+     * bssneqs_eta_const_standard_gauge.cpp) is the one built; the others
+     * (USE_ETA_FUNC, USE_ROCHESTER_GAUGE builds) are refused with
+     * DGB_ERR_UNSUPPORTED at dgb_plan_create. */
+    int gauge;
 } dgb_bssn_params;
+#define DGB_GAUGE_ETA_CONST 0           /* standard gauge, constant eta */
+#define DGB_GAUGE_ETA_FUNC 1            /* standard gauge, eta function (USE_ETA_FUNC) */
+#define DGB_GAUGE_ROCHESTER_ETA_CONST 2 /* USE_ROCHESTER_GAUGE */
+#define DGB_GAUGE_ROCHESTER_ETA_FUNC 3  /* USE_ROCHESTER_GAUGE + USE_ETA_FUNC */
 
 typedef struct dgb_plan dgb_plan;
 
@@ -128,11 +145,16 @@ dgb_status dgb_bssnrhs_block_host(double *const *rhs, const double *const *u,
  * slices, 64 MiB, held on every device that loads the library until exit),
  * so a block may span at most DGB_NOALLOC_MAX_TILES tiles of 6^3 interior
  * points (a cube of at most 42^3 padded points); larger blocks are rejected
- * with DGB_ERR_INVALID.  FP64 only, same results as dgb_bssn_rhs.  The first
- * call on a device looks up the workspace's device address; make that first
- * call before any stream capture.  All calls share the workspace: calls
- * that overlap on the GPU (other streams, other threads) race on it.  The
- * launch is asynchronous on `stream`. */
+ * with DGB_ERR_INVALID.  Interior and domain-boundary blocks (bflag != 0:
+ * at least 13 points per side, bflag <= 63).  FP64 and the 6th-order
+ * binding only (fd_order 4 and the other gauges are refused with
+ * DGB_ERR_UNSUPPORTED); same results as dgb_bssn_rhs.  The first call on a
+ * device looks up the workspace's device address and keeps it for the life
+ * of the process; make that first call before any stream capture, and do
+ * not call this entry after cudaDeviceReset on that device (the kept address
+ * belongs to the context the reset destroyed).  All calls share the
+ * workspace: calls that overlap on the GPU (other streams, other threads)
+ * race on it.  The launch is asynchronous on `stream`. */
 #define DGB_NOALLOC_MAX_TILES 239
 dgb_status dgb_bssnrhs_block_noalloc(double *const *rhs, const double *const *u,
                                      uint64_t offset, const double *ptmin, const double *ptmax,
@@ -356,7 +378,8 @@ dgb_status dgb_remesh_wavelets(const double *const *unzipped, const uint32_t *va
  * an earlier group.  Padded point p copies zipped node copy_src[p]
  * (0xFFFFFFFF: not a copy), or, for the rows interp_dst[r], takes
  * interp_ref[r]; zipped node d reads padded point zip_src[d].  A maintainer
- * builds the operator once per mesh from ot::Mesh's maps. */
+ * builds the operator once per mesh from ot::Mesh's maps: its element-to-node
+ * map and hanging-node parents (include/mesh.h:1152-1161) and its block list. */
 typedef struct dgb_unzip_plan dgb_unzip_plan;
 dgb_status dgb_unzip_plan_create(uint64_t ndof, uint64_t unzipped_size, const uint32_t *copy_src,
                                  uint64_t ninterp, const uint64_t *interp_dst,

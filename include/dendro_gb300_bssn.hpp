@@ -1,7 +1,13 @@
 /*
- * dendro_gb300_bssn.hpp — the reference's own C++ entry points for the BSSN
- * right-hand side, re-exported over the C ABI (dendro_gb300.h), so that a
- * solver written against Dendro-5's bssnRHS / bssnrhs links unchanged.
+ * dendro_gb300_bssn.hpp — the reference's C++ entry points for the BSSN
+ * right-hand side over the C ABI (dendro_gb300.h): bssnRHS and bssnrhs with
+ * the reference's array, block and offset arguments, plus what the library
+ * needs that the reference keeps in globals (the bssn:: parameters as a
+ * dgb_bssn_params, the octree-to-domain map, a plan cache and the
+ * precision).  A solver's call site changes by those arguments (the branch
+ * INTEGRATION.md shows); the stencil binding is chosen by
+ * dgb_bssn_params::fd_order: 4 for the BSSN_GR solver
+ * (BSSN_GR/include/rhs.h:23-37), 6 for the QuadGrav 6th-order binding.
  *
  * Header-only and templated on the caller's block type, so it compiles in
  * the reference's build against ot::Block (include/block.h) without this
@@ -47,12 +53,16 @@ dgb_block_desc describe_block(const Block &blk, const Point &pt_min, const Point
     return d;
 }
 
-/* The bssn:: globals the RHS reads (BSSN_GR/include/parameters.h). */
+/* The bssn:: globals the RHS reads (BSSN_GR/include/parameters.h), and the
+ * stencil binding of the solver being replaced: fd_order 4 for BSSN_GR's own
+ * (deriv42, upwinded deriv42adv), 6 for QuadGrav's (deriv64). */
 inline dgb_bssn_params params(const unsigned lambda[4], const double lambda_f[2],
                               double eta_const, double eta_r0, double eta_damping_exp,
-                              double ko_sigma, double chi_floor)
+                              double ko_sigma, double chi_floor, int fd_order)
 {
-    dgb_bssn_params p;
+    dgb_bssn_params p{};
+    p.fd_order = fd_order;
+    p.gauge = DGB_GAUGE_ETA_CONST;
     for (int i = 0; i < 4; i++) p.lambda[i] = (double)lambda[i];
     p.lambda_f[0] = lambda_f[0];
     p.lambda_f[1] = lambda_f[1];

@@ -144,3 +144,46 @@ def test_argument_checks_without_device(dgb):
     assert L.dgb_host_free(None) == 0
     foreign = np.zeros(4)
     assert L.dgb_host_free(C.c_void_p(foreign.ctypes.data)) == INVALID
+
+
+def _noalloc_call(dgb, sz=(13, 13, 13), bflag=0, pmin=(0.0, 0.0, 0.0), pmax=(1.2, 1.2, 1.2),
+                  prm=None, null_field=False, null_arg=False):
+    """dgb_bssnrhs_block_noalloc on placeholder (never dereferenced) pointers:
+    every case here is rejected by the entry's argument checks, which run
+    before any CUDA call."""
+    import ctypes as C
+    fake = [C.c_void_p(0x1000 + 8 * v) for v in range(24)]
+    if null_field:
+        fake[5] = C.c_void_p(0)
+    arr = (C.c_void_p * 24)(*fake)
+    ptrs = C.cast(arr, dgb.PtrArr)
+    prm = prm or dgb.default_params(0.1)
+    st = dgb.lib().dgb_bssnrhs_block_noalloc(
+        None if null_arg else ptrs, ptrs, 0, (C.c_double * 3)(*pmin), (C.c_double * 3)(*pmax),
+        (C.c_uint32 * 3)(*sz), bflag, C.byref(prm), None)
+    return st, dgb.lib().dgb_last_error().decode()
+
+
+@pytest.mark.parametrize("case,status,text", [
+    (dict(null_arg=True), 1, "null argument"),
+    (dict(null_field=True), 1, "null field pointer"),
+    (dict(sz=(6, 13, 13)), 1, "[7, 4096]"),
+    (dict(sz=(13, 13, 5000)), 1, "[7, 4096]"),
+    (dict(bflag=64), 1, "beyond the six faces"),
+    (dict(bflag=1, sz=(11, 13, 13)), 1, "at least 13"),
+    (dict(pmax=(1.2, -1.0, 1.2)), 1, "ptmax must exceed ptmin"),
+    (dict(sz=(61, 61, 61)), 1, "fixed workspace"),
+])
+def test_noalloc_argument_checks(dgb, case, status, text):
+    st, msg = _noalloc_call(dgb, **case)
+    assert st == status and text in msg, (st, msg)
+
+
+def test_noalloc_refuses_other_bindings(dgb):
+    p = dgb.default_params(0.1, fd_order=4)
+    st, msg = _noalloc_call(dgb, prm=p)
+    assert st == 8 and "6th-order" in msg
+    p = dgb.default_params(0.1)
+    p.gauge = 1
+    st, msg = _noalloc_call(dgb, prm=p)
+    assert st == 8 and "gauge" in msg

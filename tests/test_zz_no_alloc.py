@@ -3,8 +3,9 @@ cannot call cudaMalloc (a pre-reserved device-memory pool, a runtime that owns
 the allocator, or a step loop that must not synchronise the device): through
 the C ABI, on two calls in a row, it gives the same right-hand side as the
 plan-based entry point dgb_bssn_rhs, within the FP64 tolerance of the other
-parity tests, and it rejects blocks larger than its fixed workspace.
-Collected last (file name) so that a stop-at-first-failure run has already
+parity tests, on interior and domain-boundary blocks (its argument checks,
+which run before any CUDA call, are tested without a device in
+tests/test_abi.py).  Collected last (file name) so that a stop-at-first-failure run has already
 run every other test."""
 import ctypes as C
 
@@ -56,13 +57,29 @@ def test_noalloc_matches_plan_entry_twice(dgb, gpu):
         plan.close()
 
 
-def test_noalloc_rejects_blocks_beyond_workspace(dgb, gpu):
+def test_noalloc_boundary_blocks_match_plan_entry(dgb, gpu):
+    """Domain-boundary blocks (one-sided closures and the outgoing-radiation
+    condition on every face class), with the padding beyond the flagged faces
+    left as NaN as an unzip leaves it: the no-alloc entry gives the plan
+    entry's right-hand side."""
+    from test_oracle import boundary_blocks, poison_outside
     torch = gpu
-    allb = dgb.synth_blocks(2, SEED2)
-    blocks = repack(dgb, allb, sample_uneven(allb, (0, 0, 0, 1)))  # one 61^3 block
-    n = dgb.unzipped_size(blocks)
-    du = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(24)]
-    dr = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(24)]
-    st = _noalloc(dgb, dr, du, blocks[0], dgb.default_params(0.1))
-    assert st == 1  # DGB_ERR_INVALID
-    assert b"fixed workspace" in dgb.lib().dgb_last_error()
+    blocks = boundary_blocks(dgb)
+    u = host_fields(dgb, blocks, SEED2)
+    poison_outside(blocks, u)
+    n = len(u[0])
+    prm = dgb.default_params(0.1)
+    du = [torch.from_numpy(a).cuda() for a in u]
+    want_d = [torch.full((n,), 3.0, dtype=torch.float64, device="cuda") for _ in range(24)]
+    plan = dgb.Plan(blocks, prm)
+    plan.rhs_device([t.data_ptr() for t in want_d], [t.data_ptr() for t in du])
+    got_d = [torch.full((n,), 3.0, dtype=torch.float64, device="cuda") for _ in range(24)]
+    for b in blocks:
+        dgb.check(_noalloc(dgb, got_d, du, b, prm), "dgb_bssnrhs_block_noalloc")
+    torch.cuda.synchronize()
+    got = [t.cpu().numpy() for t in got_d]
+    want = [t.cpu().numpy() for t in want_d]
+    mask = interior_mask(blocks, n)
+    err = normwise(got, want, mask)
+    assert np.all(err <= FP64_TOL), dict(zip(dgb.VAR_NAMES, err))
+    plan.close()
