@@ -8,6 +8,12 @@ data + 1e-6 noise; one step = one bssnRHS evaluation (6th-order
 derivatives, algebra, KO sigma = 0.1) over all blocks in ONE persistent
 launch.  Units = interior points x 24 variables per step.
 
+The default line also carries `rk4_step`: the metric's full RK4 step
+(4 x unzip -> RHS -> zip -> stage update, one CUDA graph, fused stepper) on
+the level-10 octree with the reference's block decomposition, in FP64 and in
+mixed precision, each with its own ms_per_step, value, roofline and clocks
+(--no-rk4-step skips it).
+
 Arms:
   --impl ours (default)   the CUDA library through its C ABI.  `value`:
                           device-resident fields; `e2e`: host arrays through
@@ -329,6 +335,9 @@ def main():
                     help="e2e of the host-array entries with pageable numpy arrays (through "
                          "the library's staging copy) instead of dgb_host_alloc memory")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-rk4-step", action="store_true",
+                    help="uneven20k: skip the rk4_step sub-object (the full RK4 step on the "
+                         "level-10 octree, FP64 and mixed)")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the tile schedule by timing (always on for octree_rk4)")
     ap.add_argument("--no-autotune", action="store_true",
@@ -457,6 +466,15 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu, _ = run_cpu_baseline(dgb, blocks, seed, sigma)
 
+    rk4 = None
+    if args.workload == "uneven20k" and not args.no_rk4_step and not MAX_BLOCKS:
+        # the metric's full RK4 step, FP64 and mixed, on every rank's own GPU
+        torch.cuda.empty_cache()
+        rk4 = rk4_step_subobject(dgb, torch, dev)
+        if world > 1:
+            for q in ("fp64", "mixed"):
+                rk4[q]["ms_per_step"] = replica_max_ms(rk4[q]["ms_per_step"], world, dev)
+
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": "grid-pts*vars/s", "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -466,6 +484,8 @@ def main():
                "config": dict(wl, tile=plan.tile(prec)),
                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                "gpu_launches": args.steps, "impl": "ours"}
+        if rk4 is not None:
+            out["rk4_step"] = rk4
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -733,25 +753,123 @@ def cpu_rk4_baseline(dgb, seed, sigma, steps=1):
                       f"(OpenMP), zip, stage updates"}, vals
 
 
+OCTREE_SIGMA, OCTREE_SEED = 0.4, 20261203 + 3
+
+
+def octree_workload(dgb, mesh, fine_radius, t_mesh):
+    n_int = sum((b.sz[0] - 6) * (b.sz[1] - 6) * (b.sz[2] - 6) for b in mesh.blocks)
+    return n_int, {
+        "workload": f"octree_rk4: 2:1-balanced octree on [-32,32]^3, level 10 within "
+                    f"r<{fine_radius} of each puncture, coarsening to level 4; "
+                    f"{mesh.num_leaves} leaves, {mesh.nblocks} blocks (the reference's block "
+                    f"decomposition), {mesh.ndof} independent nodes",
+        "step": "one RK4 step = 4 x (unzip -> bssnRHS+KO+BCs -> zip -> stage update), "
+                "one CUDA graph (fused stepper: the RHS gathers the unzip and writes the zip)",
+        "units": "independent nodes x 24 vars per RK4 step", "ko_sigma": OCTREE_SIGMA,
+        "dt": 0.25 * 64.0 / (2 ** 10 * 6), "cfl": 0.25, "padded_points": mesh.nunzipped,
+        "interior_points": n_int, "mesh_build_s": round(t_mesh, 2),
+        "l2": "fields (6.6 GB zipped, 18 GB unzipped per set) larger than L2"}
+
+
+def measure_octree_step(dgb, torch, dev, mesh, prec, steps, warmup, stepper="fused",
+                        autotune=True, world=1, host=None):
+    """The full RK4 step on the octree (one CUDA graph) at one precision:
+    optional per-class tile autotune, warm-up, `steps` timed steps with CUDA
+    events and the clock sampler.  Returns (measurement dict, stepper,
+    unzip plan, device state, its pointers, the host state)."""
+    sh_dev = dev
+    op = mesh.operator()
+    plan = dgb.Plan(mesh.blocks, dgb.default_params(OCTREE_SIGMA))
+    out = {}
+    if autotune:  # tile caps per block-size class (interiors 7, 13, 25, 49)
+        tu = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(24)]
+        tr = [torch.zeros_like(tu[0]) for _ in range(24)]
+        plan.synth_fill_device([t.data_ptr() for t in tu], OCTREE_SEED, 1e-6)
+        t0 = time.perf_counter()
+        plan.autotune([t.data_ptr() for t in tr], [t.data_ptr() for t in tu], prec)
+        out["autotune_s"] = round(time.perf_counter() - t0, 1)
+        out["tile"] = plan.tile(prec)
+        out["class_tiles"] = [[list(sz), face, list(cap)] for sz, face, cap in plan.class_tiles(prec)]
+        del tu, tr
+        torch.cuda.empty_cache()
+    uz = dgb.UnzipPlan(op, mesh.ndof)
+    st = dgb.Stepper(plan, uz, prec, fused=stepper == "fused")
+    out["stepper"] = ("fused unzip -> RHS (gather from the zipped state, no unzipped set)"
+                      if stepper == "fused" else "unzip -> RHS -> zip")
+    out["stepper_device_gb"] = round(st.device_bytes / 1e9, 3)
+    if host is None:
+        host = [np.empty(mesh.ndof) for _ in range(24)]
+        dgb.synth_fill_points(mesh.dof_coords(), host, OCTREE_SEED, 1e-6)
+    ds = [torch.from_numpy(a).to(sh_dev) for a in host]
+    ptrs = [t.data_ptr() for t in ds]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    dt = 0.25 * 64.0 / (2 ** 10 * 6)
+    st.step(ptrs, dt, nsteps=warmup, stream=sh)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = ClockSampler(dev.index or 0)
+    clk.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    st.step(ptrs, dt, nsteps=steps, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    out["clocks"] = clk.stop()
+    out["ms_raw"] = e0.elapsed_time(e1) / steps
+    out["plan"] = plan
+    return out, st, uz, ds, ptrs, host
+
+
+def octree_roofline(dgb, n_int, ms):
+    fp64_gflops, _ = dgb.measure_fp64_peak()
+    achieved = 4 * n_int * FLOP_PER_POINT / (ms * 1e-3) / 1e9
+    return {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
+            "frac": achieved / fp64_gflops, "traffic": None,
+            "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
+            "flop_per_point": FLOP_PER_POINT,
+            "note": "4 RHS evaluations per step over all block interior points; unzip, zip "
+                    "and the stage updates are not counted"}
+
+
+def rk4_step_subobject(dgb, torch, dev, steps=3, warmup=2):
+    """The metric's full RK4 step on the octree, FP64 and mixed (fused
+    stepper, per-class autotune), for the default bench line."""
+    t0 = time.perf_counter()
+    mesh = dgb.Mesh(octree_params(dgb, 1.0))
+    n_int, wl = octree_workload(dgb, mesh, 1.0, time.perf_counter() - t0)
+    units = mesh.ndof * 24
+    res = {"config": wl, "steps": steps, "warmup": warmup}
+    host = None
+    for name, prec in (("fp64", dgb.PREC_FP64), ("mixed", dgb.PREC_MIXED)):
+        out, st, uz, ds, ptrs, host = measure_octree_step(dgb, torch, dev, mesh, prec, steps,
+                                                          warmup, host=host)
+        ms = out.pop("ms_raw")
+        out.pop("plan").close()
+        st.close()
+        uz.close()
+        del ds
+        torch.cuda.empty_cache()
+        res[name] = dict(out, ms_per_step=ms, value=units / (ms * 1e-3),
+                         unit="grid-pts*vars/s (independent nodes x 24 vars per RK4 step)",
+                         roofline=octree_roofline(dgb, n_int, ms),
+                         gpu_launches=4 * (mesh.nlevels + 3) * steps)
+    res["mixed_speedup"] = res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"]
+    mesh.close()
+    return res
+
+
 def main_octree(args, dgb, rank, world, local):
-    sigma, seed = 0.4, 20261203 + 3
+    sigma, seed = OCTREE_SIGMA, OCTREE_SEED
     t0 = time.perf_counter()
     mesh = dgb.Mesh(octree_params(dgb, args.fine_radius))
-    t_mesh = time.perf_counter() - t0
-    n_int = sum((b.sz[0] - 6) * (b.sz[1] - 6) * (b.sz[2] - 6) for b in mesh.blocks)
+    n_int, wl = octree_workload(dgb, mesh, args.fine_radius, time.perf_counter() - t0)
     units = mesh.ndof * 24
-    dx_min = 64.0 / (2 ** 10 * 6)
-    dt = 0.25 * dx_min
-    wl = {"workload": f"octree_rk4: 2:1-balanced octree on [-32,32]^3, level 10 within "
-                      f"r<{args.fine_radius} of each puncture, coarsening to level 4; "
-                      f"{mesh.num_leaves} leaves, {mesh.nblocks} blocks, "
-                      f"{mesh.ndof} independent nodes",
-          "step": "one RK4 step = 4 x (unzip -> bssnRHS+KO+BCs -> zip -> stage update), "
-                  "one CUDA graph (fused stepper: the RHS gathers the unzip and writes the zip)",
-          "units": "independent nodes x 24 vars per RK4 step", "ko_sigma": sigma,
-          "dt": dt, "cfl": 0.25, "padded_points": mesh.nunzipped, "interior_points": n_int,
-          "mesh_build_s": round(t_mesh, 2), "precision": args.precision,
-          "l2": "fields (6.6 GB zipped, 18 GB unzipped per set) larger than L2"}
+    dt = wl["dt"]
+    wl["precision"] = args.precision
     if args.impl == "reference":
         if rank != 0:
             return
@@ -774,55 +892,17 @@ def main_octree(args, dgb, rank, world, local):
     torch.cuda.set_device(dev)
     dgb.init(local)
     prec = dgb.PREC_MIXED if args.precision == "mixed" else dgb.PREC_FP64
-    op = mesh.operator()
-    plan = dgb.Plan(mesh.blocks, dgb.default_params(sigma))
-    if not args.no_autotune:  # tile caps per block-size class (interiors 7, 13, 25, 49)
-        tu = [torch.zeros(mesh.nunzipped, dtype=torch.float64, device=dev) for _ in range(24)]
-        tr = [torch.zeros_like(tu[0]) for _ in range(24)]
-        plan.synth_fill_device([t.data_ptr() for t in tu], seed, 1e-6)
-        t0 = time.perf_counter()
-        plan.autotune([t.data_ptr() for t in tr], [t.data_ptr() for t in tu], prec)
-        wl["autotune_s"] = round(time.perf_counter() - t0, 1)
-        wl["tile"] = plan.tile(prec)
-        wl["class_tiles"] = [[list(sz), face, list(cap)] for sz, face, cap in plan.class_tiles(prec)]
-        del tu, tr
-        torch.cuda.empty_cache()
-    uz = dgb.UnzipPlan(op, mesh.ndof)
-    st = dgb.Stepper(plan, uz, prec, fused=args.stepper == "fused")
-    wl["stepper"] = ("fused unzip -> RHS (gather from the zipped state, no unzipped set)"
-                     if args.stepper == "fused" else "unzip -> RHS -> zip")
-    wl["stepper_device_gb"] = round(st.device_bytes / 1e9, 3)
-    xyz = mesh.dof_coords()
-    host = [np.empty(mesh.ndof) for _ in range(24)]
-    dgb.synth_fill_points(xyz, host, seed, 1e-6)
-    ds = [torch.from_numpy(a).to(dev) for a in host]
-    ptrs = [t.data_ptr() for t in ds]
+    out, st, uz, ds, ptrs, host = measure_octree_step(
+        dgb, torch, dev, mesh, prec, args.steps, args.warmup, stepper=args.stepper,
+        autotune=not args.no_autotune, world=world)
+    clocks = out.pop("clocks")
+    plan = out.pop("plan")
+    ms = replica_max_ms(out.pop("ms_raw"), world, dev)
+    wl.update(out)
+    value = replica_value(units, world, ms)
+    roof = octree_roofline(dgb, n_int, ms)
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
-    st.step(ptrs, dt, nsteps=args.warmup, stream=sh)
-    torch.cuda.synchronize(dev)
-    if world > 1:
-        torch.distributed.barrier()
-    clk = ClockSampler(local)
-    clk.start()
-    time.sleep(0.3)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    st.step(ptrs, dt, nsteps=args.steps, stream=sh)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    clocks = clk.stop()
-    ms = replica_max_ms(e0.elapsed_time(e1) / args.steps, world, dev)
-    value = replica_value(units, world, ms)
-    fp64_gflops, _ = dgb.measure_fp64_peak()
-    achieved = 4 * n_int * FLOP_PER_POINT / (ms * 1e-3) / 1e9
-    roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
-            "frac": achieved / fp64_gflops, "traffic": None,
-            "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
-            "flop_per_point": FLOP_PER_POINT,
-            "note": "4 RHS evaluations per step over all block interior points; unzip, zip "
-                    "and the stage updates are not counted"}
     e2e = None
     if not args.no_e2e:
         k = max(1, min(args.steps, 3))
@@ -859,6 +939,7 @@ def main_octree(args, dgb, rank, world, local):
                           "impl": "ours"}))
     st.close()
     uz.close()
+    plan.close()
     if world > 1:
         torch.distributed.destroy_process_group()
 
