@@ -69,7 +69,9 @@ __device__ __forceinline__ void b4_item(const RhsArgs &args, const WorkItem &w, 
     const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
     const int px = ex + 6, py = ey + 6, pz = ez + 6;
     const int npad = px * py * pz;
+    const DivBy dpx(px), dpy(py);
     const int P = ex * ey * ez;
+    const DivBy dex(ex), dey(ey);
     const int sy = px, sz = px * py;
     const uint64_t rbase = blk.offset + (uint64_t)w.o[0]
                          + (uint64_t)nx * ((uint64_t)w.o[1] + (uint64_t)ny * w.o[2]);
@@ -91,7 +93,8 @@ __device__ __forceinline__ void b4_item(const RhsArgs &args, const WorkItem &w, 
     if (tid < 6) s_cnt[tid] = 0;
     __syncthreads();
     for (int p = tid; p < P; p += kB4Threads) {
-        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        int ti, tj, tk;
+        split3(p, dex, dey, ti, tj, tk);
         const uint64_t gi = blk.offset + (uint64_t)(w.o[0] + ti + 3)
                           + (uint64_t)nx * ((uint64_t)(w.o[1] + tj + 3) + (uint64_t)ny * (w.o[2] + tk + 3));
 #pragma unroll
@@ -103,7 +106,8 @@ __device__ __forceinline__ void b4_item(const RhsArgs &args, const WorkItem &w, 
         }
     }
     auto tile_pos = [&](int p, int d, int *ti_, int *tj_, int *tk_) {
-        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        int ti, tj, tk;
+        split3(p, dex, dey, ti, tj, tk);
         *ti_ = ti; *tj_ = tj; *tk_ = tk;
         return (d == 0 ? w.o[0] + ti : d == 1 ? w.o[1] + tj : w.o[2] + tk) + 3;
     };
@@ -159,7 +163,8 @@ __device__ __forceinline__ void b4_item(const RhsArgs &args, const WorkItem &w, 
     auto issue_load = [&](int v, double *dst) {
         const double *src = args.u[v] + rbase;
         for (int q = tid; q < npad; q += kB4Threads) {
-            const int i = q % px, r = q / px, j = r % py, k = r / py;
+            int i, j, k;
+            split3(q, dpx, dpy, i, j, k);
             cp_async8(dst + q, src + i + (uint64_t)nx * (j + (uint64_t)ny * k));
         }
         cp_async_commit();
@@ -184,7 +189,8 @@ __device__ __forceinline__ void b4_item(const RhsArgs &args, const WorkItem &w, 
         const bool want_grad = bflag != 0 || !((v >= 9 && v <= 11) || (v >= 18 && v <= 23));
         if (q2 < 0) {
             for (int p = tid; p < P; p += kB4Threads) {
-                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(p, dex, dey, ti, tj, tk);
                 const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
                 const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                 if (want_grad) {
@@ -199,15 +205,18 @@ __device__ __forceinline__ void b4_item(const RhsArgs &args, const WorkItem &w, 
             double *S2 = S + (size_t)(DGB_NUM_GRAD + 6 * q2) * G::PMAX;
             // (1a) d_x on x in tile and (y in tile +- 2, z in tile) or (y in tile, z halo of 2)
             const int by = ey + 4;
+            const DivBy dby(by);
             const int nA = ex * by * ez, nB = ex * ey * 4;
             for (int q = tid; q < nA + nB; q += kB4Threads) {
                 int ti, tj, tk;  // box coordinates: tj in [0, ey+4), tk in [0, ez+4)
                 if (q < nA) {
-                    ti = q % ex; const int r = q / ex; tj = r % by; tk = r / by + 2;
+                    split3(q, dex, dby, ti, tj, tk);
+                    tk += 2;
                 } else {
                     const int q3 = q - nA;
-                    ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 2;
-                    const int kk = r / ey;  // 0..3
+                    int kk;  // 0..3
+                    split3(q3, dex, dey, ti, tj, kk);
+                    tj += 2;
                     tk = kk < 2 ? kk : ez + kk;
                 }
                 const double *c = F + (ti + 3) + sy * (tj + 1) + sz * (tk + 1);
@@ -216,13 +225,15 @@ __device__ __forceinline__ void b4_item(const RhsArgs &args, const WorkItem &w, 
             // (1b) d_y on x, y in tile, z in tile +- 2
             const int nC = ex * ey * (ez + 4);
             for (int q = tid; q < nC; q += kB4Threads) {
-                const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(q, dex, dey, ti, tj, tk);
                 const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 1);
                 dyb[q] = d1_42_at(c, sy, w.o[1] + tj + 3, ny, lo[1], hi[1], ax[1]);
             }
             // (1c) pointwise: d_z, xx, yy, zz, KO
             for (int p = tid; p < P; p += kB4Threads) {
-                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(p, dex, dey, ti, tj, tk);
                 const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
                 const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                 Sg[2 * G::PMAX + p] = d1_42_at(c, sz, pos[2], nz, lo[2], hi[2], ax[2]);
@@ -234,7 +245,8 @@ __device__ __forceinline__ void b4_item(const RhsArgs &args, const WorkItem &w, 
             advection(F, Sa);  // ends with a barrier: the boxes are complete
             // (2) mixed from the boxes; d_x, d_y at the tile points
             for (int p = tid; p < P; p += kB4Threads) {
-                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(p, dex, dey, ti, tj, tk);
                 const int pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
                 const double *cx = dxb + ti + ex * ((tj + 2) + by * (tk + 2));
                 const double *cy = dyb + ti + ex * (tj + ey * (tk + 2));
@@ -275,12 +287,14 @@ __device__ __forceinline__ void b4_points(const RhsArgs &args, const WorkItem &w
     const int nx = blk.sz[0], ny = blk.sz[1], nz = blk.sz[2];
     const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
     const int P = ex * ey * ez;
+    const DivBy dex(ex), dey(ey);
     const uint32_t bflag = blk.bflag;
     const bool lo[3] = {(bflag & 1u) != 0, (bflag & 4u) != 0, (bflag & 16u) != 0};
     const bool hi[3] = {(bflag & 2u) != 0, (bflag & 8u) != 0, (bflag & 32u) != 0};
     const AlgPrm aprm{args.prm.l1, args.prm.l2, args.prm.l3, args.prm.l4, args.prm.lf0, args.prm.lf1};
     for (int p = tid; p < P; p += kB4Threads) {
-        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        int ti, tj, tk;
+        split3(p, dex, dey, ti, tj, tk);
         const int i = w.o[0] + ti + 3, j = w.o[1] + tj + 3, k = w.o[2] + tk + 3;
         const uint64_t gi = blk.offset + (uint64_t)i + (uint64_t)nx * ((uint64_t)j + (uint64_t)ny * k);
         const double x = __dadd_rn(blk.pmin[0], __dmul_rn((double)i, blk.h[0]));

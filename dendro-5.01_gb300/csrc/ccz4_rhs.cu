@@ -34,6 +34,7 @@
 #include "exact_mul.cuh"
 #include "fp32split.cuh"
 #include "stencil42.cuh"
+#include "tile_index.cuh"
 
 namespace dgb {
 namespace {
@@ -194,7 +195,9 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
     const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
     const int px = ex + 6, py = ey + 6, pz = ez + 6;
     const int npad = px * py * pz;
+    const DivBy dpx(px), dpy(py);
     const int P = ex * ey * ez;
+    const DivBy dex(ex), dey(ey);
     const int sy = px, sz = px * py;
     const uint64_t rbase = blk.offset + (uint64_t)w.o[0]
                          + (uint64_t)nx * ((uint64_t)w.o[1] + (uint64_t)ny * w.o[2]);
@@ -212,7 +215,8 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
     if (tid < 6) s_cnt[tid] = 0;
     __syncthreads();
     for (int p = tid; p < P; p += kC4Threads) {
-        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        int ti, tj, tk;
+        split3(p, dex, dey, ti, tj, tk);
         const uint64_t gi = blk.offset + (uint64_t)(w.o[0] + ti + 3)
                           + (uint64_t)nx * ((uint64_t)(w.o[1] + tj + 3) + (uint64_t)ny * (w.o[2] + tk + 3));
 #pragma unroll
@@ -225,7 +229,8 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
     }
     const int st3[3] = {1, sy, sz};
     auto tile_pos = [&](int p, int d, int *ti_, int *tj_, int *tk_) {
-        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        int ti, tj, tk;
+        split3(p, dex, dey, ti, tj, tk);
         *ti_ = ti; *tj_ = tj; *tk_ = tk;
         return (d == 0 ? w.o[0] + ti : d == 1 ? w.o[1] + tj : w.o[2] + tk) + 3;
     };
@@ -268,7 +273,8 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
     auto issue_load = [&](int v, double *dst) {
         const double *src = args.u[v] + rbase;
         for (int q = tid; q < npad; q += kC4Threads) {
-            const int i = q % px, r = q / px, j = r % py, k = r / py;
+            int i, j, k;
+            split3(q, dpx, dpy, i, j, k);
             c4_cp_async8(dst + q, src + i + (uint64_t)nx * (j + (uint64_t)ny * k));
         }
         c4_commit();
@@ -352,7 +358,8 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
             };
             if (q2 < 0) {
                 for (int p = tid; p < P; p += kC4Threads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                     if (want_grad) {
@@ -366,15 +373,18 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
             } else {
                 double *S2 = S + (size_t)(DGB_CCZ4_D20 + 6 * q2) * G::PMAX;
                 const int by = ey + 4;
+                const DivBy dby(by);
                 const int nA = ex * by * ez, nB = ex * ey * 4;
                 for (int q = tid; q < nA + nB; q += kC4Threads) {
                     int ti, tj, tk;
                     if (q < nA) {
-                        ti = q % ex; const int r = q / ex; tj = r % by; tk = r / by + 2;
+                        split3(q, dex, dby, ti, tj, tk);
+                        tk += 2;
                     } else {
                         const int q3 = q - nA;
-                        ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 2;
-                        const int kk = r / ey;
+                        int kk;
+                        split3(q3, dex, dey, ti, tj, kk);
+                        tj += 2;
                         tk = kk < 2 ? kk : ez + kk;
                     }
                     const int off = (ti + 3) + sy * (tj + 1) + sz * (tk + 1);
@@ -385,14 +395,16 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                 }
                 const int nC = ex * ey * (ez + 4);
                 for (int q = tid; q < nC; q += kC4Threads) {
-                    const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(q, dex, dey, ti, tj, tk);
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 1);
                     const FP2 h = N1(fhi + off, flo + off, sy);
                     dys[q] = h.s;
                     dye[q] = h.e;
                 }
                 for (int p = tid; p < P; p += kC4Threads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                     Sg[2 * G::PMAX + p] = to64(N1(fhi + off, flo + off, sz), f12[2]);
@@ -411,7 +423,8 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
                 const FC fxy = split_const(ax[0].c12 * ax[1].c12), fxz = split_const(ax[0].c12 * ax[2].c12),
                          fyz = split_const(ax[1].c12 * ax[2].c12);
                 for (int p = tid; p < P; p += kC4Threads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const int bxi = ti + ex * ((tj + 2) + by * (tk + 2));
                     const int byi = ti + ex * (tj + ey * (tk + 2));
                     Sg[p] = to64(FP2{dxs[bxi], dxe[bxi]}, f12[0]);
@@ -423,7 +436,8 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
             }
         } else if (q2 < 0) {
             for (int p = tid; p < P; p += kC4Threads) {
-                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(p, dex, dey, ti, tj, tk);
                 const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
                 const int st[3] = {1, sy, sz};
                 const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
@@ -443,15 +457,18 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
             double *S2 = S + (size_t)(DGB_CCZ4_D20 + 6 * q2) * G::PMAX;
             // (1a) d_x on x in tile and (y in tile +- 2, z in tile) or (y in tile, z halo of 2)
             const int by = ey + 4;
+            const DivBy dby(by);
             const int nA = ex * by * ez, nB = ex * ey * 4;
             for (int q = tid; q < nA + nB; q += kC4Threads) {
                 int ti, tj, tk;  // box coordinates: tj in [0, ey+4), tk in [0, ez+4)
                 if (q < nA) {
-                    ti = q % ex; const int r = q / ex; tj = r % by; tk = r / by + 2;
+                    split3(q, dex, dby, ti, tj, tk);
+                    tk += 2;
                 } else {
                     const int q3 = q - nA;
-                    ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 2;
-                    const int kk = r / ey;  // 0..3
+                    int kk;  // 0..3
+                    split3(q3, dex, dey, ti, tj, kk);
+                    tj += 2;
                     tk = kk < 2 ? kk : ez + kk;
                 }
                 const double *c = F + (ti + 3) + sy * (tj + 1) + sz * (tk + 1);
@@ -460,13 +477,15 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
             // (1b) d_y on x, y in tile, z in tile +- 2
             const int nC = ex * ey * (ez + 4);
             for (int q = tid; q < nC; q += kC4Threads) {
-                const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(q, dex, dey, ti, tj, tk);
                 const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 1);
                 dyb[q] = d1_42_at(c, sy, w.o[1] + tj + 3, ny, lo[1], hi[1], ax[1]);
             }
             // (1c) pointwise: d_z, xx, yy, zz, advective, KO
             for (int p = tid; p < P; p += kC4Threads) {
-                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(p, dex, dey, ti, tj, tk);
                 const int pos[3] = {w.o[0] + ti + 3, w.o[1] + tj + 3, w.o[2] + tk + 3};
                 const int st[3] = {1, sy, sz};
                 const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
@@ -486,7 +505,8 @@ __device__ __forceinline__ void c4_item(const C4Args &args, const WorkItem &w, c
             __syncthreads();
             // (2) mixed from the boxes; d_x, d_y at the tile points
             for (int p = tid; p < P; p += kC4Threads) {
-                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(p, dex, dey, ti, tj, tk);
                 const int pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
                 const double *cx = dxb + ti + ex * ((tj + 2) + by * (tk + 2));
                 const double *cy = dyb + ti + ex * (tj + ey * (tk + 2));
@@ -512,13 +532,15 @@ __device__ __forceinline__ void c4_points(const C4Args &args, const WorkItem &w,
     const int nx = blk.sz[0], ny = blk.sz[1], nz = blk.sz[2];
     const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
     const int P = ex * ey * ez;
+    const DivBy dex(ex), dey(ey);
     const uint32_t bflag = blk.bflag;
     const bool lo[3] = {(bflag & 1u) != 0, (bflag & 4u) != 0, (bflag & 16u) != 0};
     const bool hi[3] = {(bflag & 2u) != 0, (bflag & 8u) != 0, (bflag & 32u) != 0};
     const C4AlgPrm aprm{args.prm.l1, args.prm.l2, args.prm.l3, args.prm.l4, args.prm.lf0,
                         args.prm.lf1, args.prm.k1, args.prm.k2, args.prm.p};
     for (int p = tid; p < P; p += kC4Threads) {
-        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        int ti, tj, tk;
+        split3(p, dex, dey, ti, tj, tk);
         const int i = w.o[0] + ti + 3, j = w.o[1] + tj + 3, k = w.o[2] + tk + 3;
         const uint64_t gi = blk.offset + (uint64_t)i + (uint64_t)nx * ((uint64_t)j + (uint64_t)ny * k);
         // coordinates and radius with the reference's roundings (rhs.cpp:147-160)

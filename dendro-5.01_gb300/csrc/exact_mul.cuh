@@ -44,15 +44,6 @@ DGB_XM_HD double dgb_bitsd(uint64_t b)
 #endif
 }
 
-DGB_XM_HD int dgb_clz64(uint64_t v)
-{
-#if defined(__CUDA_ARCH__)
-    return __clzll((long long)v);
-#else
-    return v ? __builtin_clzll(v) : 64;
-#endif
-}
-
 // The hardware multiply for the rare inputs (subnormal, huge, non-finite),
 // out of line on the device: inlined behind the exponent test, the compiler
 // may turn the branch into a select and issue the DMUL on every call, which
@@ -117,26 +108,37 @@ DGB_XM_HD double dgb_mul2(double x)
     return dgb_bitsd(b + (1ull << 52));
 }
 
-// RN(C * x) for a compile-time constant 2 <= C < 1024.
+// bit length of a constant: 2^(L-1) <= C < 2^L
+constexpr int dgb_bitlen(uint32_t c) { return c ? 1 + dgb_bitlen(c >> 1) : 0; }
+
+// RN(C * x) for a compile-time constant 2 <= C < 1024, with L = bitlen(C).
+// The significand product p = m * C (m in [2^52, 2^53)) lies in
+// [2^(51+L), 2^(53+L)); doubling it when it is below 2^(52+L) puts every
+// product in [2^(52+L), 2^(53+L)), so the return to 53 bits is one fixed
+// shift by L.  Round-half-even is an add before the shift: the dropped bits
+// plus 2^(L-1) - 1 plus the kept lsb carry into the kept bits exactly when
+// they exceed half, or equal it with the lsb odd.  The result's bits are
+// the input's sign and exponent plus (shift - 1) << 52 plus the rounded
+// significand, whose implicit bit (or its carry to 2^53) lifts the exponent
+// by the remaining one (or two).  All shifts are by constants: about 20
+// integer instructions, no count-leading-zeros, no variable 64-bit shifts.
 template <uint32_t C>
 DGB_XM_HD double dgb_mul_const(double x)
 {
     static_assert(C >= 2 && C < 1024, "small integer constants only");
+    constexpr int L = dgb_bitlen(C);
     const uint64_t b = dgb_dbits(x);
     const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
-    if (e == 0u || e >= 0x7FFu - 10u) {
+    if (e - 1u >= 0x7FFu - 11u) {        // e == 0 (wraps) or e >= 0x7FF - 10
         if ((b << 1) == 0ull) return x;  // C * (+-0) = +-0
         return DGB_XM_SLOW(C, x);
     }
     const uint64_t m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
-    const uint64_t p = m * (uint64_t)C;           // exact, < 2^63
-    const int sh = 11 - dgb_clz64(p);             // bits beyond 53 (0..10)
-    uint64_t q = p >> sh;
-    const uint64_t rem = p & ((1ull << sh) - 1ull);
-    const uint64_t half = (1ull << sh) >> 1;      // 0 when sh == 0
-    q += (uint64_t)((rem > half) | ((rem == half) & (sh != 0) & (uint32_t)(q & 1u)));
-    const uint64_t carry = q >> 53;               // rounding reached 2^53
-    q >>= carry;
-    const uint64_t ex = (uint64_t)(e + (uint32_t)sh + (uint32_t)carry) << 52;
-    return dgb_bitsd((b & 0x8000000000000000ull) | ex | (q & 0x000FFFFFFFFFFFFFull));
+    const uint64_t p = m * (uint64_t)C;  // exact, < 2^63
+    const bool big = p >= (1ull << (52 + L));
+    const uint64_t pn = big ? p : p << 1;
+    const uint64_t t = pn + ((1ull << (L - 1)) - 1ull) + ((pn >> L) & 1ull);
+    const uint64_t q = t >> L;           // in [2^52, 2^53]
+    const uint64_t se = (b & 0xFFF0000000000000ull) + ((uint64_t)(big ? L - 1 : L - 2) << 52);
+    return dgb_bitsd(se + q);
 }

@@ -25,6 +25,7 @@
 #include "dgb_internal.h"
 #include "exact_mul.cuh"
 #include "stencil42.cuh"
+#include "tile_index.cuh"
 
 namespace dgb {
 namespace {
@@ -339,7 +340,9 @@ __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem 
     const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
     const int px = ex + 4, py = ey + 4, pz = ez + 4;
     const int npad = px * py * pz;
+    const DivBy dpx(px), dpy(py);
     const int P = ex * ey * ez;
+    const DivBy dex(ex), dey(ey);
     const int sy_ = px, sz_ = px * py;
     // staged region starts 2 points before the tile's first interior point
     const uint64_t rbase = blk.offset + (uint64_t)(w.o[0] + 1)
@@ -352,7 +355,8 @@ __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem 
     auto issue_load = [&](int q, double *dst) {
         const double *src = args.u[c_cfield[q]] + rbase;
         for (int e = tid; e < npad; e += kPcThreads) {
-            const int i = e % px, r = e / px, j = r % py, k = r / py;
+            int i, j, k;
+            split3(e, dpx, dpy, i, j, k);
             cp_async8(dst + e, src + i + (uint64_t)nx * (j + (uint64_t)ny * k));
         }
         cp_async_commit();
@@ -372,7 +376,8 @@ __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem 
         const int r2 = c_cd2[q];
         if (r2 < 0) {
             for (int p = tid; p < P; p += kPcThreads) {
-                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(p, dex, dey, ti, tj, tk);
                 const double *c = F + (ti + 2) + sy_ * (tj + 2) + sz_ * (tk + 2);
                 Sg[p] = d1_42_at(c, 1, w.o[0] + ti + 3, nx, lo[0], hi[0], ax[0]);
                 Sg[G::PMAX + p] = d1_42_at(c, sy_, w.o[1] + tj + 3, ny, lo[1], hi[1], ax[1]);
@@ -382,15 +387,18 @@ __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem 
             double *S2 = S + (size_t)(kGradSlots + 6 * r2) * G::PMAX;
             // d_x on x in tile and (y in tile +- 2, z in tile) or (y in tile, z in the z halo)
             const int by = ey + 4;
+            const DivBy dby(by);
             const int nA = ex * by * ez, nB = ex * ey * 4;
             for (int e = tid; e < nA + nB; e += kPcThreads) {
                 int ti, tj, tk;
                 if (e < nA) {
-                    ti = e % ex; const int r = e / ex; tj = r % by; tk = r / by + 2;
+                    split3(e, dex, dby, ti, tj, tk);
+                    tk += 2;
                 } else {
                     const int e3 = e - nA;
-                    ti = e3 % ex; const int r = e3 / ex; tj = r % ey + 2;
-                    const int kk = r / ey;  // 0..3
+                    int kk;  // 0..3
+                    split3(e3, dex, dey, ti, tj, kk);
+                    tj += 2;
                     tk = kk < 2 ? kk : ez + kk;
                 }
                 const double *c = F + (ti + 2) + sy_ * tj + sz_ * tk;
@@ -399,12 +407,14 @@ __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem 
             // d_y on x, y in tile, z in tile +- 2
             const int nC = ex * ey * pz;
             for (int e = tid; e < nC; e += kPcThreads) {
-                const int ti = e % ex, r = e / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(e, dex, dey, ti, tj, tk);
                 const double *c = F + (ti + 2) + sy_ * (tj + 2) + sz_ * tk;
                 dyb[e] = d1_42_at(c, sy_, w.o[1] + tj + 3, ny, lo[1], hi[1], ax[1]);
             }
             for (int p = tid; p < P; p += kPcThreads) {
-                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(p, dex, dey, ti, tj, tk);
                 const int pi = w.o[0] + ti + 3, pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
                 const double *c = F + (ti + 2) + sy_ * (tj + 2) + sz_ * (tk + 2);
                 Sg[2 * G::PMAX + p] = d1_42_at(c, sz_, pk, nz, lo[2], hi[2], ax[2]);
@@ -414,7 +424,8 @@ __device__ __forceinline__ void physcon_item(const PcArgs &args, const WorkItem 
             }
             __syncthreads();
             for (int p = tid; p < P; p += kPcThreads) {
-                const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                int ti, tj, tk;
+                split3(p, dex, dey, ti, tj, tk);
                 const int pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
                 const double *cx = dxb + ti + ex * ((tj + 2) + by * (tk + 2));
                 const double *cy = dyb + ti + ex * (tj + ey * (tk + 2));
@@ -440,8 +451,10 @@ __device__ __forceinline__ void physcon_points(const PcArgs &args, const WorkIte
     const int nx = blk.sz[0], ny = blk.sz[1];
     const int ex = w.e[0], ey = w.e[1], ez = w.e[2];
     const int P = ex * ey * ez;
+    const DivBy dex(ex), dey(ey);
     for (int p = tid; p < P; p += kPcThreads) {
-        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        int ti, tj, tk;
+        split3(p, dex, dey, ti, tj, tk);
         const int i = w.o[0] + ti + 3, j = w.o[1] + tj + 3, k = w.o[2] + tk + 3;
         const uint64_t gi = blk.offset + (uint64_t)i + (uint64_t)nx * ((uint64_t)j + (uint64_t)ny * k);
         // x = pmin + i h with the reference's two roundings (physcon.cpp:64-69)

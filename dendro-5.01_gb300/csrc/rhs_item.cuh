@@ -43,6 +43,7 @@
 #include "dgb_internal.h"
 #include "exact_mul.cuh"
 #include "fp32split.cuh"
+#include "tile_index.cuh"
 
 namespace dgb {
 namespace {
@@ -324,6 +325,7 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
     const int px = ex + 6, py = ey + 6, pz = ez + 6;
     const int npad = px * py * pz;
     const int P = ex * ey * ez;
+    const DivBy dex(ex), dey(ey), dbx(ey + 6), dpx(px), dpy(py);
     // region start in padded block coordinates = interior origin
     const uint64_t rbase = blk.offset + (uint64_t)w.o[0]
                          + (uint64_t)nx * ((uint64_t)w.o[1] + (uint64_t)ny * w.o[2]);
@@ -349,7 +351,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
     if (GATHER) {
         const uint32_t *gm = args.gmap + rbase;
         for (int q = tid; q < npad; q += kThreads) {
-            const int i = q % px, r = q / px, j = r % py, k = r / py;
+            int i, j, k;
+            split3(q, dpx, dpy, i, j, k);
             gidx[q] = __ldg(gm + i + (uint64_t)nx * (j + (uint64_t)ny * k));
         }
         __syncthreads();
@@ -360,7 +363,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
         } else {
             const double *src = args.u[v] + rbase;
             for (int q = tid; q < npad; q += kThreads) {
-                const int i = q % px, r = q / px, j = r % py, k = r / py;
+                int i, j, k;
+                split3(q, dpx, dpy, i, j, k);
                 cp_async8(dst + q, src + i + (uint64_t)nx * (j + (uint64_t)ny * k));
             }
         }
@@ -385,7 +389,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
             // ---------------- domain-boundary block: closures, FP64 in both precisions
             if (q2 < 0) {
                 for (int p = tid; p < P; p += kThreads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const int pi = w.o[0] + ti + 3, pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
                     const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                     Sg[p] = d1_at(c, 1, pi, nx, blo[0], bhi[0], ax[0]);
@@ -402,11 +407,13 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 for (int q = tid; q < nA + nB; q += kThreads) {
                     int ti, tj, tk;
                     if (q < nA) {
-                        ti = q % ex; const int r = q / ex; tj = r % bx_y; tk = r / bx_y + 3;
+                        split3(q, dex, dbx, ti, tj, tk);
+                        tk += 3;
                     } else {
                         const int q3 = q - nA;
-                        ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 3;
-                        const int kk = r / ey;
+                        int kk;  // 0..5
+                        split3(q3, dex, dey, ti, tj, kk);
+                        tj += 3;
                         tk = kk < 3 ? kk : ez + kk;
                     }
                     const double *c = F + (ti + 3) + sy * tj + sz * tk;
@@ -414,12 +421,14 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 }
                 const int nC = ex * ey * pz;
                 for (int q = tid; q < nC; q += kThreads) {
-                    const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(q, dex, dey, ti, tj, tk);
                     const double *c = F + (ti + 3) + sy * (tj + 3) + sz * tk;
                     dyb[q] = d1_at(c, sy, w.o[1] + tj + 3, ny, blo[1], bhi[1], ax[1]);
                 }
                 for (int p = tid; p < P; p += kThreads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const int pi = w.o[0] + ti + 3, pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
                     const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                     Sg[2 * G::PMAX + p] = d1_at(c, sz, pk, nz, blo[2], bhi[2], ax[2]);
@@ -432,7 +441,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 }
                 __syncthreads();
                 for (int p = tid; p < P; p += kThreads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const int pj = w.o[1] + tj + 3, pk = w.o[2] + tk + 3;
                     const double *cx = dxb + ti + ex * ((tj + 3) + bx_y * (tk + 3));
                     const double *cy = dyb + ti + ex * (tj + ey * (tk + 3));
@@ -446,7 +456,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
         } else if constexpr (!MIXED) {
             if (q2 < 0) {
                 for (int p = tid; p < P; p += kThreads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                     Sg[p] = d1_64(c, 1, c60[0]);
                     Sg[G::PMAX + p] = d1_64(c, sy, c60[1]);
@@ -461,11 +472,13 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 for (int q = tid; q < nA + nB; q += kThreads) {
                     int ti, tj, tk;  // box coords: tj in [0,ey+6), tk in [0,ez+6)
                     if (q < nA) {
-                        ti = q % ex; const int r = q / ex; tj = r % bx_y; tk = r / bx_y + 3;
+                        split3(q, dex, dbx, ti, tj, tk);
+                        tk += 3;
                     } else {
                         const int q3 = q - nA;
-                        ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 3;
-                        const int kk = r / ey;  // 0..5
+                        int kk;  // 0..5
+                        split3(q3, dex, dey, ti, tj, kk);
+                        tj += 3;
                         tk = kk < 3 ? kk : ez + kk;
                     }
                     const double *c = F + (ti + 3) + sy * tj + sz * tk;
@@ -474,13 +487,15 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 // (1b) d_y on x,y in tile, z extended
                 const int nC = ex * ey * pz;
                 for (int q = tid; q < nC; q += kThreads) {
-                    const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(q, dex, dey, ti, tj, tk);
                     const double *c = F + (ti + 3) + sy * (tj + 3) + sz * tk;
                     dyb[q] = d1_64(c, sy, c60[1]);
                 }
                 // (1c) pointwise: d_z, xx, yy, zz, KO
                 for (int p = tid; p < P; p += kThreads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const double *c = F + (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                     Sg[2 * G::PMAX + p] = d1_64(c, sz, c60[2]);
                     S2[0 * G::PMAX + p] = d2_64(c, 1, c180[0]);
@@ -491,7 +506,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 __syncthreads();
                 // (2) mixed from the boxes; d_x, d_y at tile points
                 for (int p = tid; p < P; p += kThreads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const double *cx = dxb + ti + ex * ((tj + 3) + bx_y * (tk + 3));
                     const double *cy = dyb + ti + ex * (tj + ey * (tk + 3));
                     Sg[p] = cx[0];
@@ -537,7 +553,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
             };
             if (q2 < 0) {
                 for (int p = tid; p < P; p += kThreads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                     Sg[p] = fp2_widen(mulfc(N1(off, 1), f60[0]));
                     Sg[G::PMAX + p] = fp2_widen(mulfc(N1(off, sy), f60[1]));
@@ -552,11 +569,13 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 for (int q = tid; q < nA + nB; q += kThreads) {
                     int ti, tj, tk;
                     if (q < nA) {
-                        ti = q % ex; const int r = q / ex; tj = r % bx_y; tk = r / bx_y + 3;
+                        split3(q, dex, dbx, ti, tj, tk);
+                        tk += 3;
                     } else {
                         const int q3 = q - nA;
-                        ti = q3 % ex; const int r = q3 / ex; tj = r % ey + 3;
-                        const int kk = r / ey;
+                        int kk;  // 0..5
+                        split3(q3, dex, dey, ti, tj, kk);
+                        tj += 3;
                         tk = kk < 3 ? kk : ez + kk;
                     }
                     const FP2 h = N1((ti + 3) + sy * tj + sz * tk, 1);
@@ -567,13 +586,15 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 // (1b) y-numerators, z extended
                 const int nC = ex * ey * pz;
                 for (int q = tid; q < nC; q += kThreads) {
-                    const int ti = q % ex, r = q / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(q, dex, dey, ti, tj, tk);
                     const FP2 h = N1((ti + 3) + sy * (tj + 3) + sz * tk, sy);
                     dys[q] = h.s;
                     dye[q] = h.e;
                 }
                 for (int p = tid; p < P; p += kThreads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const int off = (ti + 3) + sy * (tj + 3) + sz * (tk + 3);
                     Sg[2 * G::PMAX + p] = fp2_widen(mulfc(N1(off, sz), f60[2]));
                     S2[0 * G::PMAX + p] = fp2_widen(mulfc(N2(off, 1), f180[0]));
@@ -587,7 +608,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 const FC fxy = split_const(c60[0] * c60[1]), fxz = split_const(c60[0] * c60[2]),
                          fyz = split_const(c60[1] * c60[2]);
                 for (int p = tid; p < P; p += kThreads) {
-                    const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+                    int ti, tj, tk;
+                    split3(p, dex, dey, ti, tj, tk);
                     const int bxi = ti + ex * ((tj + 3) + bx_y * (tk + 3));
                     const int byi = ti + ex * (tj + ey * (tk + 3));
                     Sg[p] = fp2_widen(mulfc(FP2{dxs[bxi], dxe[bxi]}, f60[0]));
@@ -609,7 +631,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
 
     // ------------------------------------------------------------ phase A
     for (int p = tid; p < P; p += kThreads) {
-        const int ti = p % ex, r = p / ex, tj = r % ey, tk = r / ey;
+        int ti, tj, tk;
+        split3(p, dex, dey, ti, tj, tk);
         const int i = w.o[0] + ti + 3, j = w.o[1] + tj + 3, k = w.o[2] + tk + 3;
         const uint64_t gi = blk.offset + (uint64_t)i + (uint64_t)nx * ((uint64_t)j + (uint64_t)ny * k);
         // coordinates and radius with the reference's roundings (rhs.cpp:210-219)

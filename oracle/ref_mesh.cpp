@@ -159,7 +159,7 @@ int refmesh_zip_owner(int64_t *owner)
     if (!g_mesh) return 1;
     const std::vector<unsigned int> &cg = g_mesh->getE2NMapping();
     const std::vector<unsigned int> &dg = g_mesh->getE2NMapping_DG();
-    const size_t npe = (size_t)(g_order ? 0 : 0) + cg.size() / g_mesh->getAllElements().size();
+    const size_t npe = cg.size() / g_mesh->getAllElements().size();
     for (size_t i = 0; i < g_mesh->getDegOfFreedom(); i++) owner[i] = -1;
     for (size_t e = g_mesh->getElementLocalBegin(); e < g_mesh->getElementLocalEnd(); e++)
         for (size_t k = 0; k < npe; k++)
