@@ -111,12 +111,21 @@ def test_rk4_step_matches_oracle(dgb, gpu, oracle, small_mesh, nsteps):
     want = z0
     for _ in range(nsteps):
         want = oracle_step(dgb, oracle, m, op, want, dt, sigma)
+    # Bar on the increment over the steps, relative to its largest value.
+    # Measured worst cases on a GB300: 5.0e-12 after one step, 1.3e-12 after
+    # two, 2.2e-13 after ten, all in the diagonal of gt (4-5e-12; chi 8e-13,
+    # every other field <= 2e-13).  Those are the fields the constraint
+    # closure rescales: gt by det^(-1/3), which the GPU takes as one
+    # reciprocal cube root (within an ulp) where the oracle, like the
+    # reference, takes 1 / pow(det, 1/3); an ulp of gt_ii ~ 1 is a few 1e-12
+    # of its one-step increment.  The other fields differ only by the RHS's
+    # own 1e-14-level differences.
     for v in range(24):
         inc_w = want[v] - z0[v]
         inc_g = got[v] - z0[v]
         scale = max(np.abs(inc_w).max(), 1e-300)
         err = np.abs(inc_g - inc_w).max() / scale
-        assert err <= 1e-10, (dgb.VAR_NAMES[v], err)
+        assert err <= 2e-11, (dgb.VAR_NAMES[v], err)
     st.close()
     uz.close()
 
