@@ -457,9 +457,10 @@ def main():
                "h2d_bytes_per_step": 24 * n * 8, "d2h_bytes_per_step": 24 * npts * 8,
                "ms_per_step": e2e_s * 1e3, "host_arrays": kind,
                "path": "dgb_bssn_rhs_host (reference calling convention, host arrays): chunked "
-                       "pipeline, uploads (from the caller's arrays when page-locked, else "
-                       "through pinned staging) and downloads overlapping the kernel, interior "
-                       "points written back by host threads"}
+                       "pipeline overlapping the kernel; uploads from the caller's arrays when "
+                       "page-locked (interior points then downloaded and written back by host "
+                       "threads) or through pinned staging (interior points then stored by the "
+                       "kernel into page-locked outputs, else downloaded and written back)"}
         del hu, hr
 
     cpu = None
@@ -573,9 +574,8 @@ def main_ccz4(args, dgb, rank, world, local):
         e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
                "h2d_bytes_per_step": 25 * n * 8, "d2h_bytes_per_step": 25 * npts * 8,
                "ms_per_step": e2e_s * 1e3, "host_arrays": kind,
-               "path": "dgb_ccz4_rhs_host (host arrays): chunked pipeline, uploads (from the "
-                       "caller's arrays when page-locked, else through pinned staging) and "
-                       "downloads overlapping the kernel, interior points written back"}
+               "path": "dgb_ccz4_rhs_host (host arrays): chunked pipeline overlapping the "
+                       "kernel, the upload and output paths of dgb_bssn_rhs_host"}
         del hu, hr
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -697,10 +697,9 @@ def main_constraints(args, dgb, rank, world, local):
         e2e = {"value": npts / e2e_s, "unit": "grid-pts/s",
                "h2d_bytes_per_step": 24 * n * 8, "d2h_bytes_per_step": 6 * npts * 8,
                "ms_per_step": e2e_s * 1e3, "host_arrays": kind,
-               "path": "dgb_physical_constraints_host (host arrays): chunked pipeline, uploads "
-                       "(from the caller's arrays when page-locked, else through pinned "
-                       "staging), interior rows packed on the device and downloaded, written "
-                       "back by host threads"}
+               "path": "dgb_physical_constraints_host (host arrays): chunked pipeline "
+                       "overlapping the kernel, the upload and output paths of "
+                       "dgb_bssn_rhs_host"}
         del hu, hc
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -768,7 +767,8 @@ def octree_workload(dgb, mesh, fine_radius, t_mesh):
         "units": "independent nodes x 24 vars per RK4 step", "ko_sigma": OCTREE_SIGMA,
         "dt": 0.25 * 64.0 / (2 ** 10 * 6), "cfl": 0.25, "padded_points": mesh.nunzipped,
         "interior_points": n_int, "mesh_build_s": round(t_mesh, 2),
-        "l2": "fields (6.6 GB zipped, 18 GB unzipped per set) larger than L2"}
+        "l2": f"fields ({24 * 8 * mesh.ndof / 1e9:.1f} GB zipped, "
+              f"{24 * 8 * mesh.nunzipped / 1e9:.1f} GB unzipped per set) larger than L2"}
 
 
 def measure_octree_step(dgb, torch, dev, mesh, prec, steps, warmup, stepper="fused",

@@ -1085,9 +1085,12 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
 // runs the kernel of one chunk.
 template <class Compute>
 dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *u, int nv,
-                          Compute compute, int nv_out, bool direct)
+                          Compute compute, int nv_out, bool direct, bool out_direct)
 {
-    // nv fields in, nv_out fields out; direct: upload from the caller's arrays
+    // nv fields in, nv_out fields out; direct: upload from the caller's arrays;
+    // out_direct: the kernel stores the right-hand side's interior points
+    // straight into the caller's page-locked arrays (no pack, download or
+    // host scatter)
     HostPipe *h = p->pipe;
     const long nch = (long)h->members.size();
     const size_t slot = (size_t)NV4 * h->slot_pts;
@@ -1104,10 +1107,12 @@ dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *
             double *du[NV4], *dr[NV4];
             ptrs(0, c, du);
             ptrs(1, c, dr);
+            if (out_direct)  // the sub-plan's offsets are relative to the chunk start
+                for (int v = 0; v < nv_out; v++) dr[v] = rhs[v] + h->start[c];
             dgb_status s = compute(h->sub[c], dr, (const double *const *)du, h->s_comp);
             if (s != DGB_OK) return s;
             const size_t nr = h->row_ptr[c + 1] - h->row_ptr[c];
-            if (nr) {
+            if (nr && !out_direct) {
                 DGB_CUDA(pack_rows_launch(dr[0], h->slot_pts, h->d_packed + (size_t)(c % 3) * pslot,
                                           h->islot, h->d_rows + h->row_ptr[c], nr, nv_out,
                                           h->s_comp));
@@ -1117,7 +1122,7 @@ dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *
         if (d >= 0 && d < nch) {  // download chunk d's packed interior once computed
             DGB_CUDA(cudaStreamWaitEvent(h->s_d2h, h->ev_comp[d], 0));
             const double *pk = h->d_packed + (size_t)(d % 3) * pslot;
-            for (int v = 0; v < nv_out && h->ispan[d]; v++)
+            for (int v = 0; v < nv_out && h->ispan[d] && !out_direct; v++)
                 DGB_CUDA(cudaMemcpyAsync(h->h_out[d % 2] + (size_t)v * h->islot,
                                          pk + (size_t)v * h->islot, h->ispan[d] * sizeof(double),
                                          cudaMemcpyDeviceToHost, h->s_d2h));
@@ -1139,7 +1144,7 @@ dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *
             }
             DGB_CUDA(cudaEventRecord(h->ev_h2d[a], h->s_h2d));
         }
-        if (e >= 0 && e < nch) {  // scatter chunk e's interior rows back
+        if (e >= 0 && e < nch && !out_direct) {  // scatter chunk e's interior rows back
             DGB_CUDA(cudaEventSynchronize(h->ev_d2h[e]));
             host_scatter_rows(rhs, h->h_out[e % 2], h->islot, nv_out,
                               h->rows.data() + h->row_ptr[e], h->row_ptr[e + 1] - h->row_ptr[e],
@@ -1149,9 +1154,10 @@ dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *
     return DGB_OK;
 }
 
-// Whether every input field lies inside dgb_host_alloc memory over the
-// pipeline's extent, so that the upload can read the caller's arrays.
-bool inputs_page_locked(const HostPipe *h, const double *const *u, int nv)
+// Whether every field lies inside dgb_host_alloc memory over the pipeline's
+// extent: inputs so that the upload can read the caller's arrays, outputs
+// so that the kernel can store into them.
+bool fields_page_locked(const HostPipe *h, const double *const *u, int nv)
 {
     if (h->members.empty()) return false;
     uint64_t lo = UINT64_MAX, hi = 0;
@@ -1194,11 +1200,23 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
 {
     if (nv_out < 0) nv_out = nv;
     HostPipe *h = p->pipe;
-    const bool locked = inputs_page_locked(h, u, nv);
+    const bool locked = fields_page_locked(h, u, nv);
     const int key = nv * 64 + nv_out;
     const bool direct = locked && choose_direct(h, key);
+    // Outputs in dgb_host_alloc memory while the inputs go through the
+    // staging: the kernel stores the interior points into the caller's arrays
+    // over the host link as it runs, which leaves the host thread only the
+    // gather (gather and scatter together take longer per chunk than the
+    // kernel; the stores to host memory cost the kernel about 8 %).  With
+    // direct uploads the host thread has time for the scatter and the
+    // download path is faster.  DGB_HOST_DOWNLOAD=copy|store fixes it.
+    const char *dl = getenv("DGB_HOST_DOWNLOAD");
+    const bool out_locked = fields_page_locked(h, (const double *const *)rhs, nv_out);
+    const bool out_direct = out_locked && (dl && !strcmp(dl, "store")   ? true
+                                           : dl && !strcmp(dl, "copy") ? false
+                                                                       : !direct);
     const auto t0 = std::chrono::steady_clock::now();
-    const dgb_status s = run_pipe_steps(p, rhs, u, nv, compute, nv_out, direct);
+    const dgb_status s = run_pipe_steps(p, rhs, u, nv, compute, nv_out, direct, out_direct);
     if (s != DGB_OK) {
         cudaStreamSynchronize(h->s_h2d);
         cudaStreamSynchronize(h->s_comp);

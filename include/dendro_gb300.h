@@ -110,18 +110,22 @@ dgb_status dgb_bssn_rhs(dgb_plan *plan, double *const *rhs, const double *const 
                         int precision, void *stream);
 
 /* Same call with HOST arrays (the reference's calling convention): copies the
- * fields in, computes, copies the interior of rhs out, synchronously.
- * Fields that lie in memory from dgb_host_alloc are uploaded straight from
- * the caller's arrays; others go through the library's pinned staging. */
+ * fields in, computes, writes the interior of rhs back, synchronously; the
+ * padding of rhs is left untouched.  Fields that lie in memory from
+ * dgb_host_alloc may be uploaded straight from the caller's arrays; others go
+ * through the library's pinned staging.  When the upload goes through the
+ * staging and rhs lies in dgb_host_alloc memory, the kernel stores the
+ * interior points into rhs over the host link as it runs; otherwise they are
+ * downloaded and written back by host threads. */
 dgb_status dgb_bssn_rhs_host(dgb_plan *plan, double *const *rhs, const double *const *u,
                              int precision);
 
 /* Page-locked host memory for the caller's unzipped field arrays (the
  * reference allocates them with new[] in Mesh::createUnZippedVector,
  * include/mesh.tcc:245-262).  The host-array entries (dgb_bssn_rhs_host,
- * dgb_ccz4_rhs_host, dgb_physical_constraints_host) upload input fields that
- * lie entirely inside one such allocation without the host-side staging
- * copy, which halves the host memory traffic of the upload.  Thread-safe. */
+ * dgb_ccz4_rhs_host, dgb_physical_constraints_host) may upload input fields
+ * that lie entirely inside one such allocation without the host-side staging
+ * copy, and store into outputs that do (see dgb_bssn_rhs_host).  Thread-safe. */
 dgb_status dgb_host_alloc(size_t bytes, void **ptr);
 dgb_status dgb_host_free(void *ptr);
 

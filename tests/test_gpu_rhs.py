@@ -152,6 +152,37 @@ def test_rhs_host_pipeline_pinned_inputs(dgb, gpu, all_pinned, monkeypatch):
     plan.close()
 
 
+@pytest.mark.parametrize("upload,download", [("direct", "store"), ("staged", "copy"),
+                                              ("direct", "copy"), ("staged", "store")])
+def test_rhs_host_pipeline_output_paths(dgb, gpu, upload, download, monkeypatch):
+    """Page-locked inputs and outputs with each upload mode and each output
+    path (the kernel storing into the caller's arrays, or download + host
+    scatter): the device entry's bits, padding untouched, FP64 and mixed."""
+    torch = gpu
+    monkeypatch.setenv("DGB_HOST_CHUNK_PTS", "30000")
+    monkeypatch.setenv("DGB_HOST_UPLOAD", upload)
+    monkeypatch.setenv("DGB_HOST_DOWNLOAD", download)
+    allb = dgb.synth_blocks(2, SEED2)
+    blocks = repack(dgb, allb, sample_uneven(allb, (6, 3, 2, 0)))
+    u = host_fields(dgb, blocks, SEED2)
+    n = len(u[0])
+    plan = dgb.Plan(blocks, dgb.default_params(0.1))
+    pu = []
+    for v in range(24):
+        a = dgb.host_array(n)
+        a[:] = u[v]
+        pu.append(a)
+    for prec in (dgb.PREC_FP64, dgb.PREC_MIXED):
+        dev = run_device(dgb, torch, plan, u, rhs_init=[np.full(n, 7.0)] * 24, precision=prec)
+        host = [dgb.host_array(n) for _ in range(24)]
+        for a in host:
+            a[:] = 7.0
+        plan.rhs_host(host, pu, prec)
+        for v in range(24):
+            assert np.array_equal(dev[v], host[v]), (prec, v)
+    plan.close()
+
+
 def test_block_entry_matches_oracle(dgb, gpu, oracle):
     """dgb_bssnrhs_block_host: the bssnrhs(...) drop-in for one block at an offset."""
     allb = dgb.synth_blocks(2, SEED2)
