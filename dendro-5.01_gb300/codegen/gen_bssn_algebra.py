@@ -164,11 +164,22 @@ def generate(upwind=False):
     da = [dsc("alpha", d) for d in range(3)]
     dK = [dsc("K", d) for d in range(3)]
 
-    e.comment("first-kind Christoffels C1_kij (dendro.py:368-387)")
+    e.comment("first-kind Christoffels C1_kij = (d_j g_ki + d_i g_kj - d_k g_ij) / 2 "
+              "(dendro.py:368-387), the coinciding-index forms reduced; halving is exact")
     C1 = [[[None] * 3 for _ in range(3)] for _ in range(3)]
     for k in range(3):
         for (i, j) in PAIRS:
-            nm = e.let(f"C1_{k}{i}{j}", f"0.5 * ({dg(k, i, j)} + {dg(k, j, i)} - {dg(i, j, k)})")
+            if i == j == k:
+                expr = f"dgb_mul_pow2<-1>({dg(k, k, k)})"
+            elif i == j:  # d_i g_ki - d_k g_ii / 2
+                expr = f"{dg(k, i, i)} - 0.5 * {dg(i, i, k)}"
+            elif k == i:  # d_j g_kk / 2
+                expr = f"dgb_mul_pow2<-1>({dg(k, k, j)})"
+            elif k == j:  # d_i g_kk / 2
+                expr = f"dgb_mul_pow2<-1>({dg(k, k, i)})"
+            else:
+                expr = f"dgb_mul_pow2<-1>({dg(k, i, j)} + {dg(k, j, i)} - {dg(i, j, k)})"
+            nm = e.let(f"C1_{k}{i}{j}", expr)
             C1[k][i][j] = C1[k][j][i] = nm
     e.comment("second-kind Christoffels C2^k_ij = ig^kl C1_lij (dendro.py:390-410)")
     C2 = [[[None] * 3 for _ in range(3)] for _ in range(3)]
@@ -206,11 +217,26 @@ def generate(upwind=False):
     e.let("rphi_g", "half_ichi * (trchi - CalGtdchi)")
     e.let("q_ichi2", "0.25 * ichi * ichi")
 
-    e.comment("Ricci tensor R_ij = Rt_ij + Rphi_ij (dendro.py:470-527)")
+    e.comment("Ricci tensor R_ij = Rt_ij + Rphi_ij (dendro.py:470-527); on the diagonal the")
+    e.comment("two halves of each symmetrised term are equal and are evaluated once")
     R = [[None] * 3 for _ in range(3)]
     for (i, j) in PAIRS:
         t1 = symcontract([[dd(gtname[SYM[i][j]], l, m) for m in range(3)] for l in range(3)])
         e.let(f"t1_{i}{j}", t1)
+        c2d = sum_terms([f"{C2[k][j][i]} * {dchi[k]}" for k in range(3)])
+        e.let(f"Rphi_{i}{j}", f"half_ichi * ({ddchi[i][j]} - ({c2d})) - q_ichi2 * {dchi[i]} * {dchi[j]}"
+              f" + {g[i][j]} * rphi_g")
+        if i == j:
+            # t2 / 2, t3 / 2 and t4 = 2 A + B of the general form below
+            e.let(f"h2_{i}{j}", sum_terms([f"{g[k][i]} * {dvec('Gt', k, i)}" for k in range(3)]))
+            e.let(f"h3_{i}{j}", sum_terms([f"{CalGt[k]} * {C1[i][i][k]}" for k in range(3)]))
+            e.let(f"t4a_{i}{j}", sum_terms([f"{C2U[k][i][m]} * {C1[i][k][m]}"
+                                            for k in range(3) for m in range(3)]))
+            e.let(f"t4b_{i}{j}", sum_terms([f"{C2[k][i][m]} * {C1U[k][m][i]}"
+                                            for k in range(3) for m in range(3)]))
+            R[i][j] = e.let(f"R_{i}{j}", f"-0.5 * t1_{i}{j} + h2_{i}{j} + h3_{i}{j} + "
+                                         f"(2.0 * t4a_{i}{j} + t4b_{i}{j}) + Rphi_{i}{j}")
+            continue
         t2 = sum_terms([f"{g[k][i]} * {dvec('Gt', k, j)}" for k in range(3)]
                        + [f"{g[k][j]} * {dvec('Gt', k, i)}" for k in range(3)])
         e.let(f"t2_{i}{j}", t2)
@@ -220,9 +246,6 @@ def generate(upwind=False):
                        + [f"{C2U[k][j][m]} * {C1[i][k][m]}" for k in range(3) for m in range(3)]
                        + [f"{C2[k][i][m]} * {C1U[k][m][j]}" for k in range(3) for m in range(3)])
         e.let(f"t4_{i}{j}", t4)
-        c2d = sum_terms([f"{C2[k][j][i]} * {dchi[k]}" for k in range(3)])
-        e.let(f"Rphi_{i}{j}", f"half_ichi * ({ddchi[i][j]} - ({c2d})) - q_ichi2 * {dchi[i]} * {dchi[j]}"
-              f" + {g[i][j]} * rphi_g")
         R[i][j] = R[j][i] = e.let(f"R_{i}{j}",
                                   f"-0.5 * t1_{i}{j} + 0.5 * t2_{i}{j} + 0.5 * t3_{i}{j} + t4_{i}{j} + Rphi_{i}{j}")
 
@@ -329,6 +352,7 @@ HEADER = """// GENERATED by codegen/gen_bssn_algebra.py -- do not edit by hand.
 // Per-point BSSN right-hand side (eta constant, standard gauge) of the
 // reference's CodeGen/bssn.py:36-96, evaluated stage by stage.
 #pragma once
+#include "exact_mul.cuh"
 
 #define DGB_NUM_GRAD {ng}
 #define DGB_NUM_D2 {nd2}
@@ -350,6 +374,7 @@ HEADER_UPWIND = """// GENERATED by codegen/gen_bssn_algebra.py --upwind -- do no
 // (BSSN_GR/include/rhs.h:23-37): the advection terms beta^j ad(j, f) are read
 // from slot {adv} + v (the kernel's sums of upwinded derivatives).
 #pragma once
+#include "exact_mul.cuh"
 
 #define DGB_B42_ADV0 {adv}
 #define DGB_B42_NUM_SLOTS {ns}

@@ -119,11 +119,23 @@ def generate():
     dK = [dsc("K", d) for d in range(3)]
     dth = [dsc("theta_z4", d) for d in range(3)]
 
-    e.comment("Christoffels of the conformal metric (dendro_ccz4.py:447-500)")
+    e.comment("Christoffels of the conformal metric (dendro_ccz4.py:447-500); first kind")
+    e.comment("C1_kij = (d_j g_ki + d_i g_kj - d_k g_ij) / 2 with the coinciding-index forms")
+    e.comment("reduced; halving is exact")
     C1 = [[[None] * 3 for _ in range(3)] for _ in range(3)]
     for k in range(3):
         for (i, j) in PAIRS:
-            nm = e.let(f"C1_{k}{i}{j}", f"0.5 * ({dg(k, i, j)} + {dg(k, j, i)} - {dg(i, j, k)})")
+            if i == j == k:
+                expr = f"dgb_mul_pow2<-1>({dg(k, k, k)})"
+            elif i == j:  # d_i g_ki - d_k g_ii / 2
+                expr = f"{dg(k, i, i)} - 0.5 * {dg(i, i, k)}"
+            elif k == i:  # d_j g_kk / 2
+                expr = f"dgb_mul_pow2<-1>({dg(k, k, j)})"
+            elif k == j:  # d_i g_kk / 2
+                expr = f"dgb_mul_pow2<-1>({dg(k, k, i)})"
+            else:
+                expr = f"dgb_mul_pow2<-1>({dg(k, i, j)} + {dg(k, j, i)} - {dg(i, j, k)})"
+            nm = e.let(f"C1_{k}{i}{j}", expr)
             C1[k][i][j] = C1[k][j][i] = nm
     C2 = [[[None] * 3 for _ in range(3)] for _ in range(3)]
     for k in range(3):
@@ -159,11 +171,26 @@ def generate():
     e.let("Rtemp", f"hp * (({symcontract(Yp)}) - ({sum_terms([f'{Gh[m]} * {dpsi[m]}' for m in range(3)])}))")
     gG = [e.let(f"gG{i}", sum_terms([f"{GmC[k]} * {g[k][i]}" for k in range(3)])) for i in range(3)]
 
-    e.comment("R_DZ for the trace-free operator: Rt + R_DZ_psi_TF (dendro_ccz4.py:548-589)")
+    e.comment("R_DZ for the trace-free operator: Rt + R_DZ_psi_TF (dendro_ccz4.py:548-589);")
+    e.comment("on the diagonal the two halves of each symmetrised term are evaluated once")
     RTF = [[None] * 3 for _ in range(3)]
     for (i, j) in PAIRS:
         t1 = symcontract([[dd(gtname[SYM[i][j]], l, m) for m in range(3)] for l in range(3)])
         e.let(f"t1_{i}{j}", t1)
+        c2p = sum_terms([f"{C2[k][i][j]} * {dpsi[k]}" for k in range(3)])
+        e.let(f"RpsiTF_{i}{j}", f"-hp * ({ddpsi[i][j]} - ({c2p})) + cpp2 * {dpsi[i]} * {dpsi[j]}"
+              f" - hp * ({gG[i]} * {dpsi[j]} + {gG[j]} * {dpsi[i]})")
+        if i == j:
+            # t2 / 2, t3 / 2 and t4 = 2 A + B of the general form below
+            e.let(f"h2_{i}{j}", sum_terms([f"{g[k][i]} * {dvec('Gh', k, i)}" for k in range(3)]))
+            e.let(f"h3_{i}{j}", sum_terms([f"{Gh[k]} * {C1[i][i][k]}" for k in range(3)]))
+            e.let(f"t4a_{i}{j}", sum_terms([f"{C2U[k][i][m]} * {C1[i][k][m]}"
+                                            for k in range(3) for m in range(3)]))
+            e.let(f"t4b_{i}{j}", sum_terms([f"{C2[k][i][m]} * {C1U[k][m][i]}"
+                                            for k in range(3) for m in range(3)]))
+            RTF[i][j] = e.let(f"RTF_{i}{j}", f"-0.5 * t1_{i}{j} + h2_{i}{j} + h3_{i}{j} + "
+                                             f"(2.0 * t4a_{i}{j} + t4b_{i}{j}) + RpsiTF_{i}{j}")
+            continue
         t2 = sum_terms([f"{g[k][i]} * {dvec('Gh', k, j)}" for k in range(3)]
                        + [f"{g[k][j]} * {dvec('Gh', k, i)}" for k in range(3)])
         e.let(f"t2_{i}{j}", t2)
@@ -173,9 +200,6 @@ def generate():
                        + [f"{C2U[k][j][m]} * {C1[i][k][m]}" for k in range(3) for m in range(3)]
                        + [f"{C2[k][i][m]} * {C1U[k][m][j]}" for k in range(3) for m in range(3)])
         e.let(f"t4_{i}{j}", t4)
-        c2p = sum_terms([f"{C2[k][i][j]} * {dpsi[k]}" for k in range(3)])
-        e.let(f"RpsiTF_{i}{j}", f"-hp * ({ddpsi[i][j]} - ({c2p})) + cpp2 * {dpsi[i]} * {dpsi[j]}"
-              f" - hp * ({gG[i]} * {dpsi[j]} + {gG[j]} * {dpsi[i]})")
         RTF[i][j] = RTF[j][i] = e.let(
             f"RTF_{i}{j}", f"-0.5 * t1_{i}{j} + 0.5 * t2_{i}{j} + 0.5 * t3_{i}{j} + t4_{i}{j}"
                            f" + RpsiTF_{i}{j}")
@@ -286,6 +310,7 @@ HEADER = """// GENERATED by codegen/gen_ccz4_algebra.py -- do not edit by hand.
 // Per-point CCZ4 right-hand side of the reference's
 // GR/rhs_scripts/ccz4/ccz4.py:52-117, evaluated stage by stage.
 #pragma once
+#include "exact_mul.cuh"
 
 #define DGB_CCZ4_NUM_GRAD {ng}
 #define DGB_CCZ4_ADV0 {a0}

@@ -375,13 +375,12 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
     issue_load(0, fb0);
     for (int v = 0; v < NV; v++) {
         double *F = (v & 1) ? fb1 : fb0;
-        if (v + 1 < NV) {
-            issue_load(v + 1, (v & 1) ? fb0 : fb1);
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
+        cp_async_wait<0>();
+        // one barrier per field: field v is staged and visible, and every
+        // thread is done with field v-1 (its buffer, the boxes); the next
+        // field's load then goes into field v-1's buffer
         __syncthreads();
+        if (v + 1 < NV) issue_load(v + 1, (v & 1) ? fb0 : fb1);
         const int q2 = c_d2index[v];
         double *Sg = S + (size_t)(3 * v) * G::PMAX;
         double *Sko = S + (size_t)(DGB_NUM_DERIV + v) * G::PMAX;
@@ -626,8 +625,8 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 }
             }
         }
-        __syncthreads();  // buffer F and the boxes are reused
     }
+    __syncthreads();
 
     // ------------------------------------------------------------ phase A
     for (int p = tid; p < P; p += kThreads) {
