@@ -240,7 +240,7 @@ def generate(upwind=False):
         t2 = sum_terms([f"{g[k][i]} * {dvec('Gt', k, j)}" for k in range(3)]
                        + [f"{g[k][j]} * {dvec('Gt', k, i)}" for k in range(3)])
         e.let(f"t2_{i}{j}", t2)
-        t3 = sum_terms([f"{CalGt[k]} * ({C1[i][j][k]} + {C1[j][i][k]})" for k in range(3)])
+        t3 = sum_terms([f"{CalGt[k]} * {dg(i, j, k)}" for k in range(3)])  # C1_ijk + C1_jik = d_k g_ij
         e.let(f"t3_{i}{j}", t3)
         t4 = sum_terms([f"{C2U[k][i][m]} * {C1[j][k][m]}" for k in range(3) for m in range(3)]
                        + [f"{C2U[k][j][m]} * {C1[i][k][m]}" for k in range(3) for m in range(3)]

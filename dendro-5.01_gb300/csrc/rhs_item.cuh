@@ -253,6 +253,11 @@ struct AlgIOw {
 // Gather mode (fused unzip): the fields are the zipped state and the
 // interpolated-point buffer, read through the padded point's gather index;
 // the RHS at a padded point goes to its zipped node when the point owns it.
+// The algebra's results are stored unconditionally (into the KO slot each
+// one has just consumed) and copied to the owned node afterwards: a store
+// behind a branch would split the algebra into other basic blocks than in
+// the plain kernel, where the compiler may contract other multiply-adds,
+// and the fused step would no longer give the unfused step's bits.
 __device__ __forceinline__ const double *gather_src(const RhsArgs &a, int v, uint32_t g)
 {
     return g < a.ndof ? a.u[v] + g : a.ib[v] + (g - a.ndof);
@@ -260,7 +265,7 @@ __device__ __forceinline__ const double *gather_src(const RhsArgs &a, int v, uin
 
 struct AlgIOg {
     const RhsArgs *a;
-    const double *S;
+    double *S;
     int pmax, p;
     uint32_t g, o;  // gather index and owned zipped node (0xFFFFFFFF: none) of the point
     double sigma;
@@ -268,8 +273,13 @@ struct AlgIOg {
     __device__ __forceinline__ double d(int s) const { return S[(size_t)s * pmax + p]; }
     __device__ __forceinline__ void out(int v, double x) const
     {
-        const double r = __dadd_rn(x, __dmul_rn(sigma, S[(size_t)(DGB_NUM_DERIV + v) * pmax + p]));
-        if (o != 0xFFFFFFFFu) a->rhs[v][o] = r;
+        double *ko = S + (size_t)(DGB_NUM_DERIV + v) * pmax + p;
+        *ko = __dadd_rn(x, __dmul_rn(sigma, *ko));
+    }
+    __device__ __forceinline__ void flush() const
+    {
+        if (o == 0xFFFFFFFFu) return;
+        for (int v = 0; v < NV; v++) a->rhs[v][o] = S[(size_t)(DGB_NUM_DERIV + v) * pmax + p];
     }
 };
 
@@ -672,6 +682,7 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
             AlgIOg io{&args, S, G::PMAX, p, __ldg(args.gmap + gi), __ldg(args.zmap + gi),
                       args.prm.sigma};
             dgb_bssn_algebra(io, aprm, eta);
+            io.flush();
         } else {
             AlgIOw io{args.u, args.rhs, S, G::PMAX, p, gi, args.prm.sigma};
             dgb_bssn_algebra(io, aprm, eta);
