@@ -165,20 +165,20 @@ def generate(upwind=False):
     dK = [dsc("K", d) for d in range(3)]
 
     e.comment("first-kind Christoffels C1_kij = (d_j g_ki + d_i g_kj - d_k g_ij) / 2 "
-              "(dendro.py:368-387), the coinciding-index forms reduced; halving is exact")
+              "(dendro.py:368-387), the coinciding-index forms reduced")
     C1 = [[[None] * 3 for _ in range(3)] for _ in range(3)]
     for k in range(3):
         for (i, j) in PAIRS:
             if i == j == k:
-                expr = f"dgb_mul_pow2<-1>({dg(k, k, k)})"
+                expr = f"0.5 * {dg(k, k, k)}"
             elif i == j:  # d_i g_ki - d_k g_ii / 2
                 expr = f"{dg(k, i, i)} - 0.5 * {dg(i, i, k)}"
             elif k == i:  # d_j g_kk / 2
-                expr = f"dgb_mul_pow2<-1>({dg(k, k, j)})"
+                expr = f"0.5 * {dg(k, k, j)}"
             elif k == j:  # d_i g_kk / 2
-                expr = f"dgb_mul_pow2<-1>({dg(k, k, i)})"
+                expr = f"0.5 * {dg(k, k, i)}"
             else:
-                expr = f"dgb_mul_pow2<-1>({dg(k, i, j)} + {dg(k, j, i)} - {dg(i, j, k)})"
+                expr = f"0.5 * ({dg(k, i, j)} + {dg(k, j, i)} - {dg(i, j, k)})"
             nm = e.let(f"C1_{k}{i}{j}", expr)
             C1[k][i][j] = C1[k][j][i] = nm
     e.comment("second-kind Christoffels C2^k_ij = ig^kl C1_lij (dendro.py:390-410)")
@@ -352,7 +352,6 @@ HEADER = """// GENERATED by codegen/gen_bssn_algebra.py -- do not edit by hand.
 // Per-point BSSN right-hand side (eta constant, standard gauge) of the
 // reference's CodeGen/bssn.py:36-96, evaluated stage by stage.
 #pragma once
-#include "exact_mul.cuh"
 
 #define DGB_NUM_GRAD {ng}
 #define DGB_NUM_D2 {nd2}
@@ -374,7 +373,6 @@ HEADER_UPWIND = """// GENERATED by codegen/gen_bssn_algebra.py --upwind -- do no
 // (BSSN_GR/include/rhs.h:23-37): the advection terms beta^j ad(j, f) are read
 // from slot {adv} + v (the kernel's sums of upwinded derivatives).
 #pragma once
-#include "exact_mul.cuh"
 
 #define DGB_B42_ADV0 {adv}
 #define DGB_B42_NUM_SLOTS {ns}

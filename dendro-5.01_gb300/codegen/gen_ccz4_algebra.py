@@ -121,20 +121,20 @@ def generate():
 
     e.comment("Christoffels of the conformal metric (dendro_ccz4.py:447-500); first kind")
     e.comment("C1_kij = (d_j g_ki + d_i g_kj - d_k g_ij) / 2 with the coinciding-index forms")
-    e.comment("reduced; halving is exact")
+    e.comment("reduced")
     C1 = [[[None] * 3 for _ in range(3)] for _ in range(3)]
     for k in range(3):
         for (i, j) in PAIRS:
             if i == j == k:
-                expr = f"dgb_mul_pow2<-1>({dg(k, k, k)})"
+                expr = f"0.5 * {dg(k, k, k)}"
             elif i == j:  # d_i g_ki - d_k g_ii / 2
                 expr = f"{dg(k, i, i)} - 0.5 * {dg(i, i, k)}"
             elif k == i:  # d_j g_kk / 2
-                expr = f"dgb_mul_pow2<-1>({dg(k, k, j)})"
+                expr = f"0.5 * {dg(k, k, j)}"
             elif k == j:  # d_i g_kk / 2
-                expr = f"dgb_mul_pow2<-1>({dg(k, k, i)})"
+                expr = f"0.5 * {dg(k, k, i)}"
             else:
-                expr = f"dgb_mul_pow2<-1>({dg(k, i, j)} + {dg(k, j, i)} - {dg(i, j, k)})"
+                expr = f"0.5 * ({dg(k, i, j)} + {dg(k, j, i)} - {dg(i, j, k)})"
             nm = e.let(f"C1_{k}{i}{j}", expr)
             C1[k][i][j] = C1[k][j][i] = nm
     C2 = [[[None] * 3 for _ in range(3)] for _ in range(3)]
@@ -310,7 +310,6 @@ HEADER = """// GENERATED by codegen/gen_ccz4_algebra.py -- do not edit by hand.
 // Per-point CCZ4 right-hand side of the reference's
 // GR/rhs_scripts/ccz4/ccz4.py:52-117, evaluated stage by stage.
 #pragma once
-#include "exact_mul.cuh"
 
 #define DGB_CCZ4_NUM_GRAD {ng}
 #define DGB_CCZ4_ADV0 {a0}
