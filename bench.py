@@ -48,6 +48,10 @@ METRIC = ("BSSN RK4 grid-pts×vars/s on 1 GB300 (FP64 vs mixed), % roofline, vs 
 # Algorithmic FP64 operations per interior point per RHS, 6th order with
 # the reference binding (centred advective, 7-point KO): 8,223.
 FLOP_PER_POINT = 8223.0
+# The BSSN_GR solver's 4th-order binding (same algebra; 72 first, 33 second,
+# 33 mixed, 72 upwinded advective, 72 KO stencils at the CCZ4 set's counts):
+# 72*8 + 33*10 + 33*16 + 72*10 + 72*14 + 4137 + 96 = 7,395.
+FLOP_PER_POINT_BSSN42 = 7395.0
 # CCZ4 (4th order, the reference's set: 75 first + 36 mixed + 36 second +
 # 75 upwind + 75 KO stencils, "reduced ops 4633" algebra, KO accumulate):
 # 75*8 + 36*16 + 36*10 + 75*10 + 75*14 + 4633 + 24*4 = 8,065.
@@ -241,10 +245,11 @@ def e2e_host_arrays(dgb, count, n, pageable):
     return [np.zeros(n) for _ in range(count)], "pageable"
 
 
-def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="bssn"):
+def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="bssn", order=6):
     """Times the oracle port of the reference CPU path on all host cores
-    (system "bssn": bssnrhs; "ccz4": ccz4rhs with its 25 variables), on
-    inputs from the oracle's own copy of the synthetic generator."""
+    (system "bssn": bssnrhs in the binding of `order`; "ccz4": ccz4rhs with
+    its 25 variables), on inputs from the oracle's own copy of the synthetic
+    generator."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from workloads import repack
     ora = timing_oracle()
@@ -259,7 +264,7 @@ def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="b
         prm = dgb.params_vector(dgb.default_params(sigma))
 
         def call(r, u, sub):
-            return ora.bssnrhs_blocks(r, u, sub, prm, cores)
+            return ora.bssnrhs_blocks(r, u, sub, prm, cores, order=order)
     # calibrate on a small sample, then size the sample to ~target_s
     frac = 1.0 / 400
     times = []
@@ -282,7 +287,7 @@ def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="b
     u1 = [np.zeros(dgb.unzipped_size(sub1)) for _ in range(nv)]
     ora.synth_fill(sub1, u1, seed, 1e-6)
     r1 = [np.zeros_like(u1[0]) for _ in range(nv)]
-    one_core = dict(bssn=lambda: ora.bssnrhs_blocks(r1, u1, sub1, prm, 1),
+    one_core = dict(bssn=lambda: ora.bssnrhs_blocks(r1, u1, sub1, prm, 1, order=order),
                     ccz4=lambda: ora.ccz4rhs_blocks(r1, u1, sub1, prm, True, 1))[system]
     t0 = time.perf_counter()
     assert one_core() == 0
@@ -298,7 +303,7 @@ def run_cpu_baseline(dgb, blocks, seed, sigma, target_s=12.0, steps=1, system="b
             "kind": "port", "value_1core": v1,
             "sample": f"{len(sub)} of {len(blocks)} blocks (stratified by size, "
                       f"{pts} interior points), FP64, OpenMP over blocks, "
-                      f"{'ccz4rhs' if system == 'ccz4' else 'bssnrhs'}; value_1core: "
+                      f"{'ccz4rhs' if system == 'ccz4' else f'bssnrhs (order {order})'}; value_1core: "
                       f"{len(sub1)} of those blocks on one thread"}, vals
 
 
@@ -309,6 +314,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--fd-order", type=int, default=6, choices=[6, 4],
+                    help="uneven20k / uniform512: 6 = the QuadGrav binding (default), "
+                         "4 = the BSSN_GR solver's binding (FP64)")
     ap.add_argument("--workload", default="uneven20k",
                     choices=["uneven20k", "uniform512", "octree_rk4", "drift", "ccz4_uneven20k",
                              "constraints_uneven20k", "wavelet_octree"])
@@ -362,6 +370,9 @@ def main():
         return main_constraints(args, dgb, rank, world, local)
     if args.workload == "wavelet_octree":
         return main_wavelets(args, dgb, rank, world, local)
+    if args.fd_order == 4 and args.precision != "fp64":
+        ap.error("--fd-order 4 runs in FP64 only")
+    flop_pt = FLOP_PER_POINT if args.fd_order == 6 else FLOP_PER_POINT_BSSN42
     blocks, seed, sigma = workload(dgb, args.workload,
                                    timing_oracle() if args.impl == "reference" else None)
     npts = interior_points(blocks)
@@ -370,7 +381,7 @@ def main():
                       + ("(14000x13^3, 4000x19^3, 1600x31^3, 400x61^3)" if len(blocks) == 20000
                          else "(first blocks of the uneven batch)") if args.workload == "uneven20k"
           else f"{args.workload}: 512 blocks 13^3, dx 0.05",
-          "interior_points": npts, "vars": 24, "fd_order": 6, "ko_sigma": sigma,
+          "interior_points": npts, "vars": 24, "fd_order": args.fd_order, "ko_sigma": sigma,
           "step": "one bssnRHS (+KO) over all blocks, one persistent launch",
           "l2": "inputs (37.8 GB of fields) larger than L2" if args.workload == "uneven20k"
           else "inputs larger than L2 not guaranteed (small workload)",
@@ -379,7 +390,8 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        base, vals = run_cpu_baseline(dgb, blocks, seed, sigma, steps=args.steps + args.warmup)
+        base, vals = run_cpu_baseline(dgb, blocks, seed, sigma, steps=args.steps + args.warmup,
+                                      order=args.fd_order)
         v = float(np.median(vals[args.warmup:])) if len(vals) > args.warmup else base["value"]
         ms = units / v * 1e3
         print(json.dumps({"metric": METRIC, "value": v, "unit": "grid-pts*vars/s", "n_gpus": 1,
@@ -400,7 +412,7 @@ def main():
     torch.cuda.set_device(dev)
     dgb.init(local)
     prec = dgb.PREC_MIXED if args.precision == "mixed" else dgb.PREC_FP64
-    plan = dgb.Plan(blocks, dgb.default_params(sigma))
+    plan = dgb.Plan(blocks, dgb.default_params(sigma, fd_order=args.fd_order))
     n = plan.unzipped
     du = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(24)]
     dr = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(24)]
@@ -437,13 +449,14 @@ def main():
     value = replica_value(units, world, ms)
 
     fp64_gflops, _ = dgb.measure_fp64_peak()
-    achieved = npts * FLOP_PER_POINT / (ms * 1e-3) / 1e9
+    achieved = npts * flop_pt / (ms * 1e-3) / 1e9
     roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_gflops, "unit": "GFLOP/s",
             "frac": achieved / fp64_gflops, "traffic": None,
             "peak_source": "FP64 FMA probe kernel run in this process (dgb_measure_fp64_peak)",
-            "flop_per_point": FLOP_PER_POINT,
+            "flop_per_point": flop_pt,
             "hbm_gbs_algorithmic": 24 * 8 * (n + npts) / (ms * 1e-3) / 1e9}
-    roof["traffic"] = measured_traffic(f"{args.workload}:{args.precision}", blocks)
+    roof["traffic"] = measured_traffic(f"{args.workload}:{args.precision}"
+                                       + ("" if args.fd_order == 6 else ":fd4"), blocks)
 
     e2e = None
     if not args.no_e2e:
@@ -465,10 +478,11 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu, _ = run_cpu_baseline(dgb, blocks, seed, sigma)
+        cpu, _ = run_cpu_baseline(dgb, blocks, seed, sigma, order=args.fd_order)
 
     rk4 = None
-    if args.workload == "uneven20k" and not args.no_rk4_step and not MAX_BLOCKS:
+    if (args.workload == "uneven20k" and not args.no_rk4_step and not MAX_BLOCKS
+            and args.fd_order == 6):
         # the metric's full RK4 step, FP64 and mixed, on every rank's own GPU
         torch.cuda.empty_cache()
         rk4 = rk4_step_subobject(dgb, torch, dev)
