@@ -61,7 +61,10 @@ struct dgb_plan {
         uint64_t gen = ~0ull;
         WorkItem *d = nullptr;
         uint32_t n = 0;
-    } rhs_items[2];  // the BSSN RHS's work items per precision
+    } rhs_items[2][8];  // the BSSN RHS's capped work items per precision and variant
+    // bumped whenever a work-item buffer is freed: a captured RK4 graph that
+    // may hold the old buffer's address is captured again
+    uint64_t items_gen = 0;
     unsigned int *d_queue = nullptr;
     double *d_scratch = nullptr;
     size_t scratch_doubles = 0;
@@ -243,7 +246,7 @@ TileShape clip(TileShape a, TileShape m)
 // block-size class where the autotuner chose a cap.
 dgb_status rhs_items(dgb_plan *p, int variant, int prec, const WorkItem **d, uint32_t *n)
 {
-    dgb_plan::ItemCache &c = p->rhs_items[prec];
+    dgb_plan::ItemCache &c = p->rhs_items[prec][variant];
     if (p->caps[prec].empty()) {
         dgb_status s = build_items(p, variant);
         *d = p->d_items[variant];
@@ -251,6 +254,7 @@ dgb_status rhs_items(dgb_plan *p, int variant, int prec, const WorkItem **d, uin
         return s;
     }
     if (c.variant != variant || c.gen != p->caps_gen[prec]) {
+        if (c.d) p->items_gen++;
         const TileShape m = kTileShapes[variant];
         std::vector<WorkItem> items;
         dgb_status s = make_items(
@@ -331,6 +335,8 @@ dgb_status run_rhs_on(dgb_plan *p, double *const *rhs, const double *const *u, i
 
 }  // namespace
 
+uint64_t dgb::plan_items_gen(const dgb_plan *p) { return p->items_gen; }
+
 dgb_status dgb::run_rhs_gather(dgb_plan *p, double *const *k, const double *const *z,
                                const double *const *ib, const uint32_t *gmap, const uint32_t *zmap,
                                uint32_t ndof, int precision, cudaStream_t st)
@@ -345,21 +351,27 @@ dgb_status dgb::run_rhs_gather(dgb_plan *p, double *const *k, const double *cons
         return DGB_ERR_UNSUPPORTED;
     }
     const int prec = precision == DGB_PREC_MIXED ? 1 : 0;
-    const int variant = p->variant[prec];
+    int variant = p->variant[prec];
+    for (int pass = 0; pass < 2; pass++) {
+        if (p->occupancy_g[variant][prec] == 0) {
+            // the workspace is sized for the plain kernels' residency: never exceed it
+            const int occ = rhs_max_ctas_per_sm_gather(variant, precision);
+            if (occ < 1) {
+                set_error("gather-mode RHS kernel cannot be resident");
+                return DGB_ERR_CUDA;
+            }
+            p->occupancy_g[variant][prec] = std::min(occ, p->occupancy[variant][prec]);
+        }
+        // a variant whose gather indices cost it resident CTAs runs as 8^3
+        // (the same bits: the tiling does not change any point's arithmetic)
+        if (variant == 0 || p->occupancy_g[variant][prec] >= p->occupancy[variant][prec]) break;
+        variant = 0;
+    }
     const WorkItem *items = nullptr;
     uint32_t nitems = 0;
     dgb_status s = rhs_items(p, variant, prec, &items, &nitems);
     if (s != DGB_OK) return s;
     if (nitems == 0) return DGB_OK;
-    if (p->occupancy_g[variant][prec] == 0) {
-        // the workspace is sized for the plain kernels' residency: never exceed it
-        const int occ = rhs_max_ctas_per_sm_gather(variant, precision);
-        if (occ < 1) {
-            set_error("gather-mode RHS kernel cannot be resident");
-            return DGB_ERR_CUDA;
-        }
-        p->occupancy_g[variant][prec] = std::min(occ, p->occupancy[variant][prec]);
-    }
     RhsArgs a{};
     for (int v = 0; v < NV; v++) {
         a.u[v] = z[v];
@@ -538,6 +550,7 @@ dgb_status dgb_plan_create(const dgb_block_desc *blocks, size_t nblk, const dgb_
             maxcta = std::max(maxcta, rhs_scratch_per_cta(v) * (size_t)p->occupancy[v][q]);
         }
     p->scratch_doubles = maxcta * (size_t)p->nsm;
+    if (p->occupancy[kDefaultVariantFp64][0] >= 2) p->variant[0] = kDefaultVariantFp64;
     cudaError_t e = cudaSuccess;
     if (nblk) {
         e = cudaMalloc(&p->d_blocks, nblk * sizeof(DevBlock));
@@ -562,7 +575,8 @@ dgb_status dgb_plan_destroy(dgb_plan *p)
     cudaFree(p->d_blocks);
     cudaFree(p->d_first);
     for (auto d : p->d_items) cudaFree(d);
-    for (int q = 0; q < 2; q++) cudaFree(p->rhs_items[q].d);
+    for (int q = 0; q < 2; q++)
+        for (int v = 0; v < 8; v++) cudaFree(p->rhs_items[q][v].d);
     cudaFree(p->d_queue);
     if (!p->borrowed_scratch) {
         cudaFree(p->d_scratch);

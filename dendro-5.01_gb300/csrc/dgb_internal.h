@@ -63,6 +63,7 @@ struct TileShape {
 // Compiled variants (index into kTileShapes).
 extern const TileShape kTileShapes[];
 extern const int kNumTileShapes;
+extern const int kDefaultVariantFp64;  // the plan's FP64 variant unless set or tuned
 
 size_t rhs_smem_bytes(int variant, int precision);
 int rhs_threads(int variant);
@@ -75,6 +76,8 @@ cudaError_t rhs_launch_gather(int variant, int precision, const RhsArgs &args, i
                               cudaStream_t stream);
 int rhs_max_ctas_per_sm_gather(int variant, int precision);
 // the gather-mode RHS over a plan (dgb_api.cu)
+// changes whenever a work-item buffer of the plan is freed (see dgb_rk4_step)
+uint64_t plan_items_gen(const dgb_plan *p);
 dgb_status run_rhs_gather(dgb_plan *p, double *const *k, const double *const *z,
                           const double *const *ib, const uint32_t *gmap, const uint32_t *zmap,
                           uint32_t ndof, int precision, cudaStream_t st);

@@ -96,16 +96,29 @@ __device__ __forceinline__ void physcon_point(const PcIO &io, double x, double y
     ig[4] = (g[1] * g[2] - g[0] * g[4]) / det;
     ig[5] = (g[0] * g[3] - g[1] * g[1]) / det;
 
-    // C1[k][(i,j)] = 0.5 (d_j g_ki + d_i g_kj - d_k g_ij), C2 = ig . C1
+    // C1[k][(i,j)] = 0.5 (d_j g_ki + d_i g_kj - d_k g_ij), reduced where indices
+    // coincide (d_k g_kk / 2, d_i g_ki - d_k g_ii / 2, d_j g_kk / 2); C2 = ig . C1
     double C1[3][6], C2[3][6];
 #pragma unroll
     for (int k = 0; k < 3; k++)
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
-            for (int j = i; j < 3; j++)
-                C1[k][sy(i, j)] = 0.5 * (io.grad(Q_G + sy(k, i), j) + io.grad(Q_G + sy(k, j), i)
-                                         - io.grad(Q_G + sy(i, j), k));
+            for (int j = i; j < 3; j++) {
+                double c;
+                if (i == j && j == k)
+                    c = 0.5 * io.grad(Q_G + sy(k, k), k);
+                else if (i == j)
+                    c = io.grad(Q_G + sy(k, i), i) - 0.5 * io.grad(Q_G + sy(i, i), k);
+                else if (k == i)
+                    c = 0.5 * io.grad(Q_G + sy(k, k), j);
+                else if (k == j)
+                    c = 0.5 * io.grad(Q_G + sy(k, k), i);
+                else
+                    c = 0.5 * (io.grad(Q_G + sy(k, i), j) + io.grad(Q_G + sy(k, j), i)
+                               - io.grad(Q_G + sy(i, j), k));
+                C1[k][sy(i, j)] = c;
+            }
 #pragma unroll
     for (int k = 0; k < 3; k++)
 #pragma unroll
@@ -131,34 +144,66 @@ __device__ __forceinline__ void physcon_point(const PcIO &io, double x, double y
             trchi += ig[sy(k, l)] * (io.dd(0, sy(k, l)) - 1.5 * ichi * dchi[k] * dchi[l]);
     const double CalGtdchi = CalGt[0] * dchi[0] + CalGt[1] * dchi[1] + CalGt[2] * dchi[2];
 
-    // Ricci tensor (CodeGen/dendro.py:470-532)
+    // Ricci tensor (CodeGen/dendro.py:470-532).  The quadratic term contracts
+    // the raised Christoffels C2U[k][i][m] = ig^lm C2^k_li and C1U[k][m][j] =
+    // ig^ml C1_klj once instead of ig^lm inside a triple sum per component;
+    // C1_ijk + C1_jik = d_k g_ij; on the diagonal the two halves of each
+    // symmetrised term are equal and are evaluated once.
+    double C2U[3][3][3], C1U[3][3][3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int m = 0; m < 3; m++) {
+                C2U[k][i][m] = ig[sy(0, m)] * C2[k][sy(0, i)] + ig[sy(1, m)] * C2[k][sy(1, i)]
+                             + ig[sy(2, m)] * C2[k][sy(2, i)];
+                C1U[k][i][m] = ig[sy(i, 0)] * C1[k][sy(0, m)] + ig[sy(i, 1)] * C1[k][sy(1, m)]
+                             + ig[sy(i, 2)] * C1[k][sy(2, m)];
+            }
     double R[6];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = i; j < 3; j++) {
-            double t1 = 0.0, t2 = 0.0, t3 = 0.0, t4 = 0.0, c2d = 0.0;
+            double t1 = 0.0, c2d = 0.0;
 #pragma unroll
             for (int m = 0; m < 6; m++) t1 += wpair(m) * ig[m] * io.dd(1 + sy(i, j), m);
 #pragma unroll
-            for (int k = 0; k < 3; k++)
-                t2 += g[sy(k, i)] * io.grad(Q_GT + k, j) + g[sy(k, j)] * io.grad(Q_GT + k, i);
-#pragma unroll
-            for (int k = 0; k < 3; k++) t3 += CalGt[k] * (C1[i][sy(j, k)] + C1[j][sy(i, k)]);
-#pragma unroll
-            for (int k = 0; k < 3; k++)
-#pragma unroll
-                for (int l = 0; l < 3; l++)
-#pragma unroll
-                    for (int m = 0; m < 3; m++)
-                        t4 += ig[sy(l, m)] * (C2[k][sy(l, i)] * C1[j][sy(k, m)]
-                                              + C2[k][sy(l, j)] * C1[i][sy(k, m)]
-                                              + C2[k][sy(i, m)] * C1[k][sy(l, j)]);
-#pragma unroll
             for (int k = 0; k < 3; k++) c2d += C2[k][sy(i, j)] * dchi[k];
             const double xR = 0.5 * ichi * (io.dd(0, sy(i, j)) - c2d) - 0.25 * ichi * ichi * dchi[i] * dchi[j];
-            R[sy(i, j)] = -0.5 * t1 + 0.5 * t2 + 0.5 * t3 + t4 + xR
-                        + 0.5 * ichi * g[sy(i, j)] * (trchi - CalGtdchi);
+            double rt;
+            if (i == j) {
+                double h2 = 0.0, h3 = 0.0, t4a = 0.0, t4b = 0.0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    h2 += g[sy(k, i)] * io.grad(Q_GT + k, i);
+                    h3 += CalGt[k] * C1[i][sy(i, k)];
+                }
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+#pragma unroll
+                    for (int m = 0; m < 3; m++) {
+                        t4a += C2U[k][i][m] * C1[i][sy(k, m)];
+                        t4b += C2[k][sy(i, m)] * C1U[k][m][i];
+                    }
+                rt = -0.5 * t1 + h2 + h3 + (2.0 * t4a + t4b);
+            } else {
+                double t2 = 0.0, t3 = 0.0, t4 = 0.0;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    t2 += g[sy(k, i)] * io.grad(Q_GT + k, j) + g[sy(k, j)] * io.grad(Q_GT + k, i);
+                    t3 += CalGt[k] * io.grad(Q_G + sy(i, j), k);
+                }
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+#pragma unroll
+                    for (int m = 0; m < 3; m++)
+                        t4 += C2U[k][i][m] * C1[j][sy(k, m)] + C2U[k][j][m] * C1[i][sy(k, m)]
+                            + C2[k][sy(i, m)] * C1U[k][m][j];
+                rt = -0.5 * t1 + 0.5 * t2 + 0.5 * t3 + t4;
+            }
+            R[sy(i, j)] = rt + xR + 0.5 * ichi * g[sy(i, j)] * (trchi - CalGtdchi);
         }
 
     // Hamiltonian (CodeGen/constraints.py:158)

@@ -66,6 +66,7 @@ cudaError_t launch_any(int variant, bool mixed, const RhsArgs &a, int grid, cuda
     case 2: return mixed ? launch_variant<8, 8, 4, true, GATHER>(a, grid, st) : launch_variant<8, 8, 4, false, GATHER>(a, grid, st);
     case 3: return mixed ? launch_variant<16, 8, 4, true, GATHER>(a, grid, st) : launch_variant<16, 8, 4, false, GATHER>(a, grid, st);
     case 4: return mixed ? launch_variant<6, 6, 6, true, GATHER>(a, grid, st) : launch_variant<6, 6, 6, false, GATHER>(a, grid, st);
+    case 5: return mixed ? launch_variant<8, 8, 16, true, GATHER>(a, grid, st) : launch_variant<8, 8, 16, false, GATHER>(a, grid, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -79,6 +80,7 @@ cudaError_t configure_any(int variant, bool mixed)
     case 2: return mixed ? configure_variant<8, 8, 4, true, GATHER>() : configure_variant<8, 8, 4, false, GATHER>();
     case 3: return mixed ? configure_variant<16, 8, 4, true, GATHER>() : configure_variant<16, 8, 4, false, GATHER>();
     case 4: return mixed ? configure_variant<6, 6, 6, true, GATHER>() : configure_variant<6, 6, 6, false, GATHER>();
+    case 5: return mixed ? configure_variant<8, 8, 16, true, GATHER>() : configure_variant<8, 8, 16, false, GATHER>();
     default: return cudaErrorInvalidValue;
     }
 }
@@ -92,6 +94,7 @@ int occupancy_any(int variant, bool mixed)
     case 2: return mixed ? occupancy_variant<8, 8, 4, true, GATHER>() : occupancy_variant<8, 8, 4, false, GATHER>();
     case 3: return mixed ? occupancy_variant<16, 8, 4, true, GATHER>() : occupancy_variant<16, 8, 4, false, GATHER>();
     case 4: return mixed ? occupancy_variant<6, 6, 6, true, GATHER>() : occupancy_variant<6, 6, 6, false, GATHER>();
+    case 5: return mixed ? occupancy_variant<8, 8, 16, true, GATHER>() : occupancy_variant<8, 8, 16, false, GATHER>();
     default: return 0;
     }
 }

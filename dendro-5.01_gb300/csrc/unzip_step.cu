@@ -296,6 +296,7 @@ struct dgb_stepper {
     cudaGraphExec_t exec = nullptr;
     const double *key_state[NV] = {};
     double key_dt = 0.0, key_floor = 0.0;
+    uint64_t key_items = 0;  // plan_items_gen of the plan(s) at capture
 };
 
 namespace {
@@ -714,7 +715,9 @@ dgb_status dgb_rk4_step(dgb_stepper *s, double *const *state, double dt, double 
     }
     for (int v = 0; v < NV; v++)
         if (!state[v]) return DGB_ERR_INVALID;
-    bool same = s->exec && s->key_dt == dt && s->key_floor == chi_floor;
+    // the graph holds the plans' work-item addresses: capture again when one was freed
+    const uint64_t items = plan_items_gen(s->plan);
+    bool same = s->exec && s->key_dt == dt && s->key_floor == chi_floor && s->key_items == items;
     for (int v = 0; same && v < NV; v++) same = s->key_state[v] == state[v];
     if (!same) {
         if (s->exec) {
@@ -743,6 +746,7 @@ dgb_status dgb_rk4_step(dgb_stepper *s, double *const *state, double dt, double 
         for (int v = 0; v < NV; v++) s->key_state[v] = state[v];
         s->key_dt = dt;
         s->key_floor = chi_floor;
+        s->key_items = items;
     }
     cudaStream_t caller = (cudaStream_t)stream;
     DGB_CUDA(cudaEventRecord(s->ev_in, caller));
