@@ -305,7 +305,11 @@ struct Smem {
     static constexpr size_t base = MIXED
         ? (2 * G::FBUF * 8 + 2 * G::FBUF * 4 + 2 * (G::DXB + G::DYB) * 4)
         : (2 * G::FBUF * 8 + (G::DXB + G::DYB) * 8);
-    static constexpr size_t bytes = base + (GATHER ? G::FBUF * 4 : 0);
+    // the gather indices are staged only where two CTAs per SM still fit
+    // (228 KB per SM, 1 KB of it reserved per CTA); deeper tiles read them
+    // from global memory (L1-resident) once per field instead
+    static constexpr bool gidx_smem = GATHER && 2 * (base + G::FBUF * 4 + 1024) <= 228 * 1024;
+    static constexpr size_t bytes = base + (gidx_smem ? G::FBUF * 4 : 0);
 };
 
 // One work item (a tile of one block): phase D then phase A.  S is this
@@ -357,8 +361,9 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
     }
 
     // gather mode: the staged region's gather indices, loaded once per item
+    constexpr bool kGidxSmem = Smem<TX, TY, TZ, MIXED, GATHER>::gidx_smem;
     uint32_t *gidx = reinterpret_cast<uint32_t *>(smem_raw + Smem<TX, TY, TZ, MIXED>::base);
-    if (GATHER) {
+    if (GATHER && kGidxSmem) {
         const uint32_t *gm = args.gmap + rbase;
         for (int q = tid; q < npad; q += kThreads) {
             int i, j, k;
@@ -368,8 +373,15 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
         __syncthreads();
     }
     auto issue_load = [&](int v, double *dst) {
-        if (GATHER) {
+        if (GATHER && kGidxSmem) {
             for (int q = tid; q < npad; q += kThreads) cp_async8(dst + q, gather_src(args, v, gidx[q]));
+        } else if (GATHER) {
+            const uint32_t *gm = args.gmap + rbase;
+            for (int q = tid; q < npad; q += kThreads) {
+                int i, j, k;
+                split3(q, dpx, dpy, i, j, k);
+                cp_async8(dst + q, gather_src(args, v, __ldg(gm + i + (uint64_t)nx * (j + (uint64_t)ny * k))));
+            }
         } else {
             const double *src = args.u[v] + rbase;
             for (int q = tid; q < npad; q += kThreads) {
