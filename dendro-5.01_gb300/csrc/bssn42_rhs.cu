@@ -49,6 +49,8 @@ struct B4Geo {
     // points, the three upwinded derivatives of the current field; then per
     // direction the tile points ordered by the sign of the shift (uint16)
     static constexpr size_t bytes = (size_t)(2 * FBUF + DXB + DYB + 6 * PMAX) * 8 + 3 * PMAX * 2;
+    // DivBy (tile_index.cuh) splits indices q < FBUF by extents < 32 exactly
+    static_assert(FBUF < (1 << 13) && TX + 6 < 32 && TY + 6 < 32 && TZ + 6 < 32, "tile too large for DivBy");
 };
 
 template <int TX, int TY, int TZ, bool BDY>

@@ -130,6 +130,8 @@ struct C4Geo {
     static constexpr size_t bytes = (size_t)(2 * FBUF + DXB + DYB + 3 * PMAX) * 8 + 3 * PMAX * 2;
     // + hi/lo planes of the staged field and the s + e pair boxes (floats)
     static constexpr size_t bytes_mixed = bytes + (size_t)(2 * FBUF + 2 * DXB + 2 * DYB) * 4;
+    // DivBy (tile_index.cuh) splits indices q < FBUF by extents < 32 exactly
+    static_assert(FBUF < (1 << 13) && TX + 6 < 32 && TY + 6 < 32 && TZ + 6 < 32, "tile too large for DivBy");
 };
 
 struct C4AlgPrm {

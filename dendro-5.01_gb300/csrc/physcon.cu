@@ -365,6 +365,8 @@ struct PcGeo {
     static constexpr int DYB = TX * TY * PZ;
     static constexpr int PMAX = TX * TY * TZ;
     static constexpr size_t bytes = (size_t)(2 * FBUF + DXB + DYB) * 8;
+    // DivBy (tile_index.cuh) splits indices q < FBUF by extents < 32 exactly
+    static_assert(FBUF < (1 << 13) && TX + 6 < 32 && TY + 6 < 32 && TZ + 6 < 32, "tile too large for DivBy");
 };
 
 // Phase D of a work item.  BDY: the block touches a domain face.  Interior

@@ -294,6 +294,8 @@ struct Geo {
     static constexpr int DXB = TX * PY * PZ;         // d_x box (cross region)
     static constexpr int DYB = TX * TY * PZ;         // d_y box
     static constexpr int PMAX = TX * TY * TZ;
+    // DivBy (tile_index.cuh) splits indices q < FBUF by extents < 32 exactly
+    static_assert(FBUF < (1 << 13) && PX < 32 && PY < 32 && PZ < 32, "tile too large for DivBy");
 };
 
 template <int TX, int TY, int TZ, bool MIXED, bool GATHER = false>
