@@ -203,7 +203,7 @@ def test_ccz4_host_pipeline_many_chunks(dgb, gpu, precision, pinned, monkeypatch
         for v in range(25):
             pu[v][:] = u[v]
         u = pu
-    for rep in range(3 if pinned else 2):  # pinned: direct, direct, staged upload
+    for rep in range(4 if pinned else 2):  # pinned: direct x3, then staged upload
         host = [np.full(n, 7.0) for _ in range(25)]
         plan.ccz4_rhs_host(prm, host, u, prec)
         for v in range(25):

@@ -182,7 +182,7 @@ def test_constraints_host_pipeline_many_chunks(dgb, gpu, pinned, monkeypatch):
         for v in range(24):
             pu[v][:] = u[v]
         u = pu
-    for rep in range(3 if pinned else 2):  # pinned: direct, direct, staged upload
+    for rep in range(4 if pinned else 2):  # pinned: direct x3, then staged upload
         host = [dgb.host_array(n) if pinned else np.empty(n) for _ in range(6)]
         for h in host:
             h[:] = 7.0

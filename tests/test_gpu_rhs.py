@@ -125,8 +125,8 @@ def test_rhs_host_pipeline_many_chunks(dgb, gpu, precision, monkeypatch):
 @pytest.mark.parametrize("all_pinned", [True, False])
 def test_rhs_host_pipeline_pinned_inputs(dgb, gpu, all_pinned, monkeypatch):
     """Fields in dgb_host_alloc memory (all 24 pinned) are uploaded straight
-    from the caller's arrays on the first two calls and through the staging on
-    the third (the plan times both modes); with one field pageable every call
+    from the caller's arrays on the first three calls and through the staging
+    on the fourth (the plan times both modes); with one field pageable every call
     goes through the staging: the same bits as the device entry each time,
     padding untouched."""
     torch = gpu
@@ -142,7 +142,7 @@ def test_rhs_host_pipeline_pinned_inputs(dgb, gpu, all_pinned, monkeypatch):
         a = dgb.host_array(n) if (all_pinned or v != 5) else np.empty(n)
         a[:] = u[v]
         pu.append(a)
-    for rep in range(3):  # direct (warm-up), direct, then through the staging
+    for rep in range(4):  # direct (two warm-ups), direct, then through the staging
         host = [dgb.host_array(n) for _ in range(24)]
         for a in host:
             a[:] = 7.0
