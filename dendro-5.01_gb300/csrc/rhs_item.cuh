@@ -489,31 +489,33 @@ __device__ __forceinline__ void rhs_item(const RhsArgs &args, const WorkItem &w,
                 }
             } else {
                 double *S2 = S + (size_t)(DGB_NUM_GRAD + 6 * q2) * G::PMAX;
-                // (1a) d_x on the cross region: x in tile, (y ext, z tile) or (y tile, z ext)
+                // (1a) d_x on the cross region: x in tile, (y ext, z tile) or (y tile, z ext),
+                // and (1b) d_y on x, y in tile, z extended, in one pass: every item is one
+                // first-derivative stencil, so the threads share the two boxes evenly
                 const int bx_y = ey + 6;  // d_x box rows
                 const int nA = ex * bx_y * ez, nB = ex * ey * 6;
-                for (int q = tid; q < nA + nB; q += kThreads) {
-                    int ti, tj, tk;  // box coords: tj in [0,ey+6), tk in [0,ez+6)
-                    if (q < nA) {
-                        split3(q, dex, dbx, ti, tj, tk);
-                        tk += 3;
-                    } else {
-                        const int q3 = q - nA;
-                        int kk;  // 0..5
-                        split3(q3, dex, dey, ti, tj, kk);
-                        tj += 3;
-                        tk = kk < 3 ? kk : ez + kk;
-                    }
-                    const double *c = F + (ti + 3) + sy * tj + sz * tk;
-                    dxb[ti + ex * (tj + bx_y * tk)] = d1_64(c, 1, c60[0]);
-                }
-                // (1b) d_y on x,y in tile, z extended
                 const int nC = ex * ey * pz;
-                for (int q = tid; q < nC; q += kThreads) {
-                    int ti, tj, tk;
-                    split3(q, dex, dey, ti, tj, tk);
-                    const double *c = F + (ti + 3) + sy * (tj + 3) + sz * tk;
-                    dyb[q] = d1_64(c, sy, c60[1]);
+                for (int q = tid; q < nA + nB + nC; q += kThreads) {
+                    int ti, tj, tk;  // box coords: tj in [0,ey+6), tk in [0,ez+6)
+                    if (q < nA + nB) {
+                        if (q < nA) {
+                            split3(q, dex, dbx, ti, tj, tk);
+                            tk += 3;
+                        } else {
+                            const int q3 = q - nA;
+                            int kk;  // 0..5
+                            split3(q3, dex, dey, ti, tj, kk);
+                            tj += 3;
+                            tk = kk < 3 ? kk : ez + kk;
+                        }
+                        const double *c = F + (ti + 3) + sy * tj + sz * tk;
+                        dxb[ti + ex * (tj + bx_y * tk)] = d1_64(c, 1, c60[0]);
+                    } else {
+                        const int qc = q - nA - nB;
+                        split3(qc, dex, dey, ti, tj, tk);
+                        const double *c = F + (ti + 3) + sy * (tj + 3) + sz * tk;
+                        dyb[qc] = d1_64(c, sy, c60[1]);
+                    }
                 }
                 // (1c) pointwise: d_z, xx, yy, zz, KO
                 for (int p = tid; p < P; p += kThreads) {
