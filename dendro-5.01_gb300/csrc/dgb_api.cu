@@ -126,7 +126,12 @@ struct HostPipe {
         uint64_t calls = 0;
     };
     std::map<int, UploadStats> upload;
-    cudaStream_t s_h2d = nullptr, s_comp = nullptr, s_d2h = nullptr;
+    // two compute streams, even and odd chunks: the next chunk's kernel fills
+    // the SMs the current one's last work items leave idle.  Odd chunks run
+    // on their own derivative workspaces (the parent's serve the even ones).
+    cudaStream_t s_h2d = nullptr, s_comp[2] = {nullptr, nullptr}, s_d2h = nullptr;
+    double *d_scratch_odd = nullptr, *d_scratch4_odd = nullptr;
+    size_t scratch4_odd_doubles = 0;
     std::vector<cudaEvent_t> ev_h2d, ev_comp, ev_d2h;
 };
 
@@ -137,6 +142,8 @@ void destroy_pipe(HostPipe *h)
     cudaFree(h->d_slots);
     cudaFree(h->d_rows);
     cudaFree(h->d_packed);
+    cudaFree(h->d_scratch_odd);
+    cudaFree(h->d_scratch4_odd);
     for (int q = 0; q < 2; q++) {
         cudaFreeHost(h->h_in[q]);
         cudaFreeHost(h->h_out[q]);
@@ -145,7 +152,8 @@ void destroy_pipe(HostPipe *h)
     for (auto e : h->ev_comp) if (e) cudaEventDestroy(e);
     for (auto e : h->ev_d2h) if (e) cudaEventDestroy(e);
     if (h->s_h2d) cudaStreamDestroy(h->s_h2d);
-    if (h->s_comp) cudaStreamDestroy(h->s_comp);
+    for (int q = 0; q < 2; q++)
+        if (h->s_comp[q]) cudaStreamDestroy(h->s_comp[q]);
     if (h->s_d2h) cudaStreamDestroy(h->s_d2h);
     delete h;
 }
@@ -1014,13 +1022,17 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
         return (uint64_t)d.sz[0] * d.sz[1] * d.sz[2];
     };
     for (size_t q = 0; q < order.size();) {
+        // the first two chunks a quarter and a half of the others: the GPU
+        // waits only for the first, short upload before its first kernel
+        const size_t k = h->members.size();
+        const uint64_t cap = k == 0 ? chunk_pts / 4 : k == 1 ? chunk_pts / 2 : chunk_pts;
         const uint64_t s0 = p->blocks[order[q]].offset;
         uint64_t end = s0 + npts(order[q]);
         std::vector<uint32_t> mem{order[q]};
         size_t r = q + 1;
         while (r < order.size()) {
             const uint64_t e2 = std::max(end, p->blocks[order[r]].offset + npts(order[r]));
-            if (e2 - s0 > chunk_pts) break;
+            if (e2 - s0 > cap) break;
             end = e2;
             mem.push_back(order[r]);
             r++;
@@ -1031,8 +1043,12 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
         h->members.push_back(std::move(mem));
         q = r;
     }
-    // one sub-plan per chunk, offsets relative to the chunk start, sharing
-    // the parent's derivative workspace (chunks run one after another)
+    // one sub-plan per chunk, offsets relative to the chunk start; even
+    // chunks share the parent's derivative workspace, odd chunks a second one
+    // (consecutive chunks may run at the same time, chunks two apart never:
+    // each compute stream runs its chunks in order)
+    if (h->members.size() > 1)
+        DGB_CUDA(cudaMalloc(&h->d_scratch_odd, p->scratch_doubles * sizeof(double)));
     for (size_t c = 0; c < h->members.size(); c++) {
         std::vector<dgb_block_desc> d;
         for (uint32_t b : h->members[c]) {
@@ -1045,7 +1061,7 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
         if (s != DGB_OK) return s;
         h->sub.push_back(sp);
         cudaFree(sp->d_scratch);
-        sp->d_scratch = p->d_scratch;
+        sp->d_scratch = (c & 1) ? h->d_scratch_odd : p->d_scratch;
         sp->borrowed_scratch = true;
         for (int q = 0; q < 2; q++) sp->variant[q] = p->variant[q];
     }
@@ -1081,7 +1097,7 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
         DGB_CUDA(cudaMallocHost(&h->h_out[q], std::max<size_t>(pslot, 1) * sizeof(double)));
     }
     DGB_CUDA(cudaStreamCreateWithFlags(&h->s_h2d, cudaStreamNonBlocking));
-    DGB_CUDA(cudaStreamCreateWithFlags(&h->s_comp, cudaStreamNonBlocking));
+    for (int q = 0; q < 2; q++) DGB_CUDA(cudaStreamCreateWithFlags(&h->s_comp[q], cudaStreamNonBlocking));
     DGB_CUDA(cudaStreamCreateWithFlags(&h->s_d2h, cudaStreamNonBlocking));
     const size_t nch = h->members.size();
     h->ev_h2d.resize(nch);
@@ -1099,14 +1115,16 @@ dgb_status build_pipe_into(dgb_plan *p, HostPipe *h)
 // runs the kernel of one chunk.
 template <class Compute>
 dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *u, int nv,
-                          Compute compute, int nv_out, bool direct, bool out_direct)
+                          Compute compute, int nv_out, bool direct, bool out_direct, bool out_last)
 {
     // nv fields in, nv_out fields out; direct: upload from the caller's arrays;
     // out_direct: the kernel stores the right-hand side's interior points
     // straight into the caller's page-locked arrays (no pack, download or
-    // host scatter)
+    // host scatter); out_last: the last chunk does, so that no download and
+    // scatter trail the last kernel
     HostPipe *h = p->pipe;
     const long nch = (long)h->members.size();
+    auto od = [&](long c) { return out_direct || (out_last && c == nch - 1); };
     const size_t slot = (size_t)NV4 * h->slot_pts;
     const size_t pslot = (size_t)NV4 * h->islot;
     auto ptrs = [&](int kind, long c, double **out) {  // kind 0: u slot, 1: rhs slot
@@ -1116,27 +1134,27 @@ dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *
     for (long step = 0; step < nch + 3; step++) {
         const long c = step - 1, d = step - 2, a = step, e = step - 3;
         if (c >= 0 && c < nch) {  // compute chunk c once its upload is done
-            DGB_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_h2d[c], 0));
-            if (c >= 3) DGB_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_d2h[c - 3], 0));
+            cudaStream_t sc = h->s_comp[c & 1];
+            DGB_CUDA(cudaStreamWaitEvent(sc, h->ev_h2d[c], 0));
+            if (c >= 3) DGB_CUDA(cudaStreamWaitEvent(sc, h->ev_d2h[c - 3], 0));
             double *du[NV4], *dr[NV4];
             ptrs(0, c, du);
             ptrs(1, c, dr);
-            if (out_direct)  // the sub-plan's offsets are relative to the chunk start
+            if (od(c))  // the sub-plan's offsets are relative to the chunk start
                 for (int v = 0; v < nv_out; v++) dr[v] = rhs[v] + h->start[c];
-            dgb_status s = compute(h->sub[c], dr, (const double *const *)du, h->s_comp);
+            dgb_status s = compute(h->sub[c], dr, (const double *const *)du, sc);
             if (s != DGB_OK) return s;
             const size_t nr = h->row_ptr[c + 1] - h->row_ptr[c];
-            if (nr && !out_direct) {
+            if (nr && !od(c)) {
                 DGB_CUDA(pack_rows_launch(dr[0], h->slot_pts, h->d_packed + (size_t)(c % 3) * pslot,
-                                          h->islot, h->d_rows + h->row_ptr[c], nr, nv_out,
-                                          h->s_comp));
+                                          h->islot, h->d_rows + h->row_ptr[c], nr, nv_out, sc));
             }
-            DGB_CUDA(cudaEventRecord(h->ev_comp[c], h->s_comp));
+            DGB_CUDA(cudaEventRecord(h->ev_comp[c], sc));
         }
         if (d >= 0 && d < nch) {  // download chunk d's packed interior once computed
             DGB_CUDA(cudaStreamWaitEvent(h->s_d2h, h->ev_comp[d], 0));
             const double *pk = h->d_packed + (size_t)(d % 3) * pslot;
-            for (int v = 0; v < nv_out && h->ispan[d] && !out_direct; v++)
+            for (int v = 0; v < nv_out && h->ispan[d] && !od(d); v++)
                 DGB_CUDA(cudaMemcpyAsync(h->h_out[d % 2] + (size_t)v * h->islot,
                                          pk + (size_t)v * h->islot, h->ispan[d] * sizeof(double),
                                          cudaMemcpyDeviceToHost, h->s_d2h));
@@ -1158,7 +1176,7 @@ dgb_status run_pipe_steps(dgb_plan *p, double *const *rhs, const double *const *
             }
             DGB_CUDA(cudaEventRecord(h->ev_h2d[a], h->s_h2d));
         }
-        if (e >= 0 && e < nch && !out_direct) {  // scatter chunk e's interior rows back
+        if (e >= 0 && e < nch && !od(e)) {  // scatter chunk e's interior rows back
             DGB_CUDA(cudaEventSynchronize(h->ev_d2h[e]));
             host_scatter_rows(rhs, h->h_out[e % 2], h->islot, nv_out,
                               h->rows.data() + h->row_ptr[e], h->row_ptr[e + 1] - h->row_ptr[e],
@@ -1207,6 +1225,15 @@ bool choose_direct(HostPipe *h, int key)
     return (st.calls % 8 == 7) ? !best : best;
 }
 
+// every stream of the pipeline idle
+void sync_pipe(HostPipe *h)
+{
+    cudaStreamSynchronize(h->s_h2d);
+    cudaStreamSynchronize(h->s_comp[0]);
+    cudaStreamSynchronize(h->s_comp[1]);
+    cudaStreamSynchronize(h->s_d2h);
+}
+
 // run_pipe_steps in the chosen upload mode, timed for the mode choice; on an
 // error, a wait for the copies still in flight, so that no transfer touches
 // the caller's arrays after the call returns.
@@ -1232,19 +1259,16 @@ dgb_status run_pipe(dgb_plan *p, double *const *rhs, const double *const *u, int
                                            : dl && !strcmp(dl, "copy") ? false
                                                                        : !direct);
     const auto t0 = std::chrono::steady_clock::now();
-    const dgb_status s = run_pipe_steps(p, rhs, u, nv, compute, nv_out, direct, out_direct);
+    const bool out_last = out_locked && !(dl && !strcmp(dl, "copy"));
+    const dgb_status s = run_pipe_steps(p, rhs, u, nv, compute, nv_out, direct, out_direct, out_last);
     if (s != DGB_OK) {
-        cudaStreamSynchronize(h->s_h2d);
-        cudaStreamSynchronize(h->s_comp);
-        cudaStreamSynchronize(h->s_d2h);
+        sync_pipe(h);
         return s;
     }
     if (locked) {
         HostPipe::UploadStats &st = h->upload[key];
         if (st.calls >= 2) {  // the whole call, to its last download
-            cudaStreamSynchronize(h->s_h2d);
-            cudaStreamSynchronize(h->s_comp);
-            cudaStreamSynchronize(h->s_d2h);
+            sync_pipe(h);
             st.ms[direct ? 1 : 0] = std::chrono::duration<double, std::milli>(
                                         std::chrono::steady_clock::now() - t0).count();
         }
@@ -1285,12 +1309,33 @@ dgb_status ensure_pipe(dgb_plan *p)
     return DGB_OK;
 }
 
+// The parent's 4th-order / CCZ4 workspace for the even chunks, a copy of its
+// size for the odd ones (consecutive chunks may overlap on the GPU).
+dgb_status pipe_scratch4(dgb_plan *p)
+{
+    HostPipe *h = p->pipe;
+    if (h->sub.size() > 1 && h->scratch4_odd_doubles < p->scratch4_doubles) {
+        cudaFree(h->d_scratch4_odd);
+        h->d_scratch4_odd = nullptr;
+        h->scratch4_odd_doubles = 0;
+        DGB_CUDA(cudaMalloc(&h->d_scratch4_odd, p->scratch4_doubles * sizeof(double)));
+        h->scratch4_odd_doubles = p->scratch4_doubles;
+    }
+    for (size_t c = 0; c < h->sub.size(); c++) {
+        h->sub[c]->d_scratch4 = (c & 1) ? h->d_scratch4_odd : p->d_scratch4;
+        h->sub[c]->scratch4_doubles = p->scratch4_doubles;
+    }
+    return DGB_OK;
+}
+
 // whatever happened, nothing may still be copying into the staging buffers
 dgb_status finish_pipe(dgb_plan *p, dgb_status s, const char *what)
 {
     HostPipe *h = p->pipe;
     cudaError_t e1 = cudaStreamSynchronize(h->s_h2d);
-    cudaError_t e2 = cudaStreamSynchronize(h->s_comp);
+    cudaError_t e2 = cudaStreamSynchronize(h->s_comp[0]);
+    const cudaError_t e2b = cudaStreamSynchronize(h->s_comp[1]);
+    if (e2 == cudaSuccess) e2 = e2b;
     cudaError_t e3 = cudaStreamSynchronize(h->s_d2h);
     if (s != DGB_OK) return s;
     if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
@@ -1325,16 +1370,13 @@ dgb_status dgb_bssn_rhs_host(dgb_plan *p, double *const *rhs, const double *cons
         set_error("dgb_bssn_rhs_host: fd_order 4 runs in FP64 only");
         return DGB_ERR_UNSUPPORTED;
     }
-    // fd_order 4: the chunks run one after another on the parent's workspace
+    // fd_order 4: the chunks run on the parent's 4th-order workspace and its odd copy
     dgb_status s = p->prm.fd_order == 4 ? b4_workspace(p) : DGB_OK;
     if (s == DGB_OK) s = ensure_pipe(p);
+    if (s == DGB_OK && p->prm.fd_order == 4) s = pipe_scratch4(p);
     if (s != DGB_OK) return s;
     if (p->prm.fd_order == 4)
-        for (dgb_plan *sp : p->pipe->sub) {
-            sp->d_scratch4 = p->d_scratch4;
-            sp->scratch4_doubles = p->scratch4_doubles;
-            sp->b4_occupancy = p->b4_occupancy;
-        }
+        for (dgb_plan *sp : p->pipe->sub) sp->b4_occupancy = p->b4_occupancy;
     const int variant = p->variant[precision == DGB_PREC_MIXED ? 1 : 0];
     s = run_pipe(p, rhs, u, NV,
                  [&](dgb_plan *sp, double *const *dr, const double *const *du, cudaStream_t st) {
@@ -1360,16 +1402,13 @@ dgb_status dgb_ccz4_rhs_host(dgb_plan *p, const dgb_ccz4_params *prm, double *co
         return DGB_ERR_INVALID;
     }
     if (p->blocks.empty()) return DGB_OK;
-    // the chunks run one after another on the parent's CCZ4 workspace
+    // the chunks run on the parent's CCZ4 workspace and its odd copy
     dgb_status s = c4_workspace(p, precision);
     if (s == DGB_OK) s = ensure_pipe(p);
+    if (s == DGB_OK) s = pipe_scratch4(p);
     if (s != DGB_OK) return s;
     const int pq = precision == DGB_PREC_MIXED ? 1 : 0;
-    for (dgb_plan *sp : p->pipe->sub) {
-        sp->d_scratch4 = p->d_scratch4;
-        sp->scratch4_doubles = p->scratch4_doubles;
-        sp->c4_occupancy[pq] = p->c4_occupancy[pq];
-    }
+    for (dgb_plan *sp : p->pipe->sub) sp->c4_occupancy[pq] = p->c4_occupancy[pq];
     s = run_pipe(p, rhs, u, NV4,
                  [&](dgb_plan *sp, double *const *dr, const double *const *du, cudaStream_t st) {
                      return dgb_ccz4_rhs(sp, prm, dr, du, precision, st);

@@ -116,7 +116,10 @@ dgb_status dgb_bssn_rhs(dgb_plan *plan, double *const *rhs, const double *const 
  * through the library's pinned staging.  When the upload goes through the
  * staging and rhs lies in dgb_host_alloc memory, the kernel stores the
  * interior points into rhs over the host link as it runs; otherwise they are
- * downloaded and written back by host threads. */
+ * downloaded and written back by host threads (except the last chunk's, which
+ * the kernel stores when rhs lies in dgb_host_alloc memory).  The first call
+ * builds the plan's pipeline: device slots for three chunks of fields each
+ * way and a second derivative workspace for overlapping chunk kernels. */
 dgb_status dgb_bssn_rhs_host(dgb_plan *plan, double *const *rhs, const double *const *u,
                              int precision);
 
