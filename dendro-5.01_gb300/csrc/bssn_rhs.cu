@@ -8,8 +8,11 @@ namespace dgb {
 // boxes' z extension per interior point; at 100 KB of shared memory it still
 // fits 2 CTAs per SM in FP64 (not in mixed precision, nor with the gather
 // indices of the fused stepper) and is the FP64 default (2 % faster than 8^3
-// on the uneven batch, bit-identical).
-const TileShape kTileShapes[] = {{8, 8, 8}, {7, 7, 7}, {8, 8, 4}, {16, 8, 4}, {6, 6, 6}, {8, 8, 16}};
+// on the uneven batch, bit-identical).  7x13x13 and 9x9x13 (variants 6, 7,
+// about 105 and 99 KB in FP64) cover the 13^3 and 25^3 interiors of the
+// octree's 19^3 and 31^3 blocks in 2 and 16 or 18 tiles instead of 4 and 32.
+const TileShape kTileShapes[] = {{8, 8, 8}, {7, 7, 7}, {8, 8, 4},  {16, 8, 4},
+                                 {6, 6, 6}, {8, 8, 16}, {7, 13, 13}, {9, 9, 13}};
 const int kNumTileShapes = sizeof(kTileShapes) / sizeof(kTileShapes[0]);
 const int kDefaultVariantFp64 = 5;
 
