@@ -61,7 +61,7 @@ struct dgb_plan {
         uint64_t gen = ~0ull;
         WorkItem *d = nullptr;
         uint32_t n = 0;
-    } rhs_items[2][8];  // the BSSN RHS's capped work items per precision and variant
+    } rhs_items[2][kMaxTileShapes];  // the BSSN RHS's capped work items per precision and variant
     // bumped whenever a work-item buffer is freed: a captured RK4 graph that
     // may hold the old buffer's address is captured again
     uint64_t items_gen = 0;
@@ -584,7 +584,7 @@ dgb_status dgb_plan_destroy(dgb_plan *p)
     cudaFree(p->d_first);
     for (auto d : p->d_items) cudaFree(d);
     for (int q = 0; q < 2; q++)
-        for (int v = 0; v < 8; v++) cudaFree(p->rhs_items[q][v].d);
+        for (int v = 0; v < kMaxTileShapes; v++) cudaFree(p->rhs_items[q][v].d);
     cudaFree(p->d_queue);
     if (!p->borrowed_scratch) {
         cudaFree(p->d_scratch);

@@ -63,6 +63,7 @@ struct TileShape {
 // Compiled variants (index into kTileShapes).
 extern const TileShape kTileShapes[];
 extern const int kNumTileShapes;
+constexpr int kMaxTileShapes = 10;  // capacity of the per-variant caches
 extern const int kDefaultVariantFp64;  // the plan's FP64 variant unless set or tuned
 
 size_t rhs_smem_bytes(int variant, int precision);

@@ -69,6 +69,7 @@ cudaError_t launch_any(int variant, bool mixed, const RhsArgs &a, int grid, cuda
     case 5: return mixed ? launch_variant<8, 8, 16, true, GATHER>(a, grid, st) : launch_variant<8, 8, 16, false, GATHER>(a, grid, st);
     case 6: return mixed ? launch_variant<7, 13, 13, true, GATHER>(a, grid, st) : launch_variant<7, 13, 13, false, GATHER>(a, grid, st);
     case 7: return mixed ? launch_variant<9, 9, 13, true, GATHER>(a, grid, st) : launch_variant<9, 9, 13, false, GATHER>(a, grid, st);
+    case 8: return mixed ? launch_variant<7, 7, 13, true, GATHER>(a, grid, st) : launch_variant<7, 7, 13, false, GATHER>(a, grid, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -85,6 +86,7 @@ cudaError_t configure_any(int variant, bool mixed)
     case 5: return mixed ? configure_variant<8, 8, 16, true, GATHER>() : configure_variant<8, 8, 16, false, GATHER>();
     case 6: return mixed ? configure_variant<7, 13, 13, true, GATHER>() : configure_variant<7, 13, 13, false, GATHER>();
     case 7: return mixed ? configure_variant<9, 9, 13, true, GATHER>() : configure_variant<9, 9, 13, false, GATHER>();
+    case 8: return mixed ? configure_variant<7, 7, 13, true, GATHER>() : configure_variant<7, 7, 13, false, GATHER>();
     default: return cudaErrorInvalidValue;
     }
 }
@@ -101,6 +103,7 @@ int occupancy_any(int variant, bool mixed)
     case 5: return mixed ? occupancy_variant<8, 8, 16, true, GATHER>() : occupancy_variant<8, 8, 16, false, GATHER>();
     case 6: return mixed ? occupancy_variant<7, 13, 13, true, GATHER>() : occupancy_variant<7, 13, 13, false, GATHER>();
     case 7: return mixed ? occupancy_variant<9, 9, 13, true, GATHER>() : occupancy_variant<9, 9, 13, false, GATHER>();
+    case 8: return mixed ? occupancy_variant<7, 7, 13, true, GATHER>() : occupancy_variant<7, 7, 13, false, GATHER>();
     default: return 0;
     }
 }
