@@ -223,15 +223,15 @@ def time_host_entry(call, steps):
     four warm-up calls (the first builds the plan's pipeline and staging; with
     page-locked inputs the plan warms and times the direct upload on the
     first three and times the staging on the fourth, then keeps the faster),
-    then the median of min(max(steps, 3), 5) timed calls."""
-    for _ in range(4):
-        call()
+    then the median of min(max(steps, 3), 5) timed calls.  Also returns every
+    call's milliseconds, warm-ups first (the spread between calls and boxes
+    is the host's upload rate)."""
     ts = []
-    for _ in range(min(max(steps, 3), 5)):
+    for _ in range(4 + min(max(steps, 3), 5)):
         t0 = time.perf_counter()
         call()
         ts.append(time.perf_counter() - t0)
-    return float(np.median(ts))
+    return float(np.median(ts[4:])), [round(t * 1e3, 1) for t in ts]
 
 
 def e2e_host_arrays(dgb, count, n, pageable):
@@ -467,10 +467,10 @@ def main():
         hu, kind = e2e_host_arrays(dgb, 24, n, args.e2e_pageable)
         dgb.synth_fill_host(blocks, hu, seed, 1e-6)
         hr, _ = e2e_host_arrays(dgb, 24, n, args.e2e_pageable)
-        e2e_s = time_host_entry(lambda: plan.rhs_host(hr, hu, prec), args.steps)
+        e2e_s, calls_ms = time_host_entry(lambda: plan.rhs_host(hr, hu, prec), args.steps)
         e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
                "h2d_bytes_per_step": 24 * n * 8, "d2h_bytes_per_step": 24 * npts * 8,
-               "ms_per_step": e2e_s * 1e3, "host_arrays": kind,
+               "ms_per_step": e2e_s * 1e3, "host_arrays": kind, "calls_ms": calls_ms,
                "path": "dgb_bssn_rhs_host (reference calling convention, host arrays): chunked "
                        "pipeline overlapping the kernel; uploads from the caller's arrays when "
                        "page-locked (interior points then downloaded and written back by host "
@@ -586,10 +586,10 @@ def main_ccz4(args, dgb, rank, world, local):
         hu, kind = e2e_host_arrays(dgb, 25, n, args.e2e_pageable)
         dgb.synth_fill_host(blocks, hu, seed, 1e-6)
         hr, _ = e2e_host_arrays(dgb, 25, n, args.e2e_pageable)
-        e2e_s = time_host_entry(lambda: plan.ccz4_rhs_host(prm, hr, hu, prec), args.steps)
+        e2e_s, calls_ms = time_host_entry(lambda: plan.ccz4_rhs_host(prm, hr, hu, prec), args.steps)
         e2e = {"value": units / e2e_s, "unit": "grid-pts*vars/s",
                "h2d_bytes_per_step": 25 * n * 8, "d2h_bytes_per_step": 25 * npts * 8,
-               "ms_per_step": e2e_s * 1e3, "host_arrays": kind,
+               "ms_per_step": e2e_s * 1e3, "host_arrays": kind, "calls_ms": calls_ms,
                "path": "dgb_ccz4_rhs_host (host arrays): chunked pipeline overlapping the "
                        "kernel, the upload and output paths of dgb_bssn_rhs_host"}
         del hu, hr
@@ -709,10 +709,10 @@ def main_constraints(args, dgb, rank, world, local):
         hu, kind = e2e_host_arrays(dgb, 24, n, args.e2e_pageable)
         dgb.synth_fill_host(blocks, hu, seed, 1e-6)
         hc, _ = e2e_host_arrays(dgb, 6, n, args.e2e_pageable)
-        e2e_s = time_host_entry(lambda: plan.physical_constraints_host(hc, hu), args.steps)
+        e2e_s, calls_ms = time_host_entry(lambda: plan.physical_constraints_host(hc, hu), args.steps)
         e2e = {"value": npts / e2e_s, "unit": "grid-pts/s",
                "h2d_bytes_per_step": 24 * n * 8, "d2h_bytes_per_step": 6 * npts * 8,
-               "ms_per_step": e2e_s * 1e3, "host_arrays": kind,
+               "ms_per_step": e2e_s * 1e3, "host_arrays": kind, "calls_ms": calls_ms,
                "path": "dgb_physical_constraints_host (host arrays): chunked pipeline "
                        "overlapping the kernel, the upload and output paths of "
                        "dgb_bssn_rhs_host"}
