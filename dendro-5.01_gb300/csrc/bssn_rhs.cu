@@ -8,15 +8,15 @@ namespace dgb {
 // boxes' z extension per interior point; at 100 KB of shared memory it still
 // fits 2 CTAs per SM in FP64 (not in mixed precision, nor with the gather
 // indices of the fused stepper); 2 % faster than 8^3 on the uneven batch.
-// 7x13x13 and 9x9x13 (variants 6, 7, about 105 and 99 KB in FP64) cover the
-// 13^3 and 25^3 interiors of the octree's 19^3 and 31^3 blocks in 2 and 16 or
-// 18 tiles instead of 4 and 32; 7x13x13 is the FP64 default (the autotuner's
-// choice for every block class of the uneven batch and of the octree, 1 %
-// faster than 8x8x16 on the former, 6 % on the latter's RK4 step).  7x7x13
-// (variant 8) is the deep tile that fits 2 CTAs per SM in mixed precision
-// (96 KB; the autotuner's choice on the octree).
-const TileShape kTileShapes[] = {{8, 8, 8},  {7, 7, 7},   {8, 8, 4}, {16, 8, 4}, {6, 6, 6},
-                                 {8, 8, 16}, {7, 13, 13}, {9, 9, 13}, {7, 7, 13}};
+// 7x13x13 (variant 6, 107 KB in FP64) covers the 13^3 and 25^3 interiors of the
+// octree's 19^3 and 31^3 blocks in 2 and 16 tiles instead of 4 and 32; it is
+// the FP64 default (the autotuner's choice for every block class of the uneven
+// batch and of the octree, 1 % faster than 8x8x16 on the former, 6 % on the
+// latter's RK4 step; a 9x9x13 variant was never chosen and was dropped).
+// 7x7x13 (variant 7) is the deep tile that fits 2 CTAs per SM in mixed
+// precision (96 KB; the autotuner's choice on the octree).
+const TileShape kTileShapes[] = {{8, 8, 8},  {7, 7, 7},   {8, 8, 4}, {16, 8, 4},
+                                 {6, 6, 6},  {8, 8, 16},  {7, 13, 13}, {7, 7, 13}};
 const int kNumTileShapes = sizeof(kTileShapes) / sizeof(kTileShapes[0]);
 static_assert(sizeof(kTileShapes) / sizeof(kTileShapes[0]) <= kMaxTileShapes, "too many tile shapes");
 const int kDefaultVariantFp64 = 6;

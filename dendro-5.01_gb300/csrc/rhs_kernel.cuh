@@ -68,8 +68,7 @@ cudaError_t launch_any(int variant, bool mixed, const RhsArgs &a, int grid, cuda
     case 4: return mixed ? launch_variant<6, 6, 6, true, GATHER>(a, grid, st) : launch_variant<6, 6, 6, false, GATHER>(a, grid, st);
     case 5: return mixed ? launch_variant<8, 8, 16, true, GATHER>(a, grid, st) : launch_variant<8, 8, 16, false, GATHER>(a, grid, st);
     case 6: return mixed ? launch_variant<7, 13, 13, true, GATHER>(a, grid, st) : launch_variant<7, 13, 13, false, GATHER>(a, grid, st);
-    case 7: return mixed ? launch_variant<9, 9, 13, true, GATHER>(a, grid, st) : launch_variant<9, 9, 13, false, GATHER>(a, grid, st);
-    case 8: return mixed ? launch_variant<7, 7, 13, true, GATHER>(a, grid, st) : launch_variant<7, 7, 13, false, GATHER>(a, grid, st);
+    case 7: return mixed ? launch_variant<7, 7, 13, true, GATHER>(a, grid, st) : launch_variant<7, 7, 13, false, GATHER>(a, grid, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -85,8 +84,7 @@ cudaError_t configure_any(int variant, bool mixed)
     case 4: return mixed ? configure_variant<6, 6, 6, true, GATHER>() : configure_variant<6, 6, 6, false, GATHER>();
     case 5: return mixed ? configure_variant<8, 8, 16, true, GATHER>() : configure_variant<8, 8, 16, false, GATHER>();
     case 6: return mixed ? configure_variant<7, 13, 13, true, GATHER>() : configure_variant<7, 13, 13, false, GATHER>();
-    case 7: return mixed ? configure_variant<9, 9, 13, true, GATHER>() : configure_variant<9, 9, 13, false, GATHER>();
-    case 8: return mixed ? configure_variant<7, 7, 13, true, GATHER>() : configure_variant<7, 7, 13, false, GATHER>();
+    case 7: return mixed ? configure_variant<7, 7, 13, true, GATHER>() : configure_variant<7, 7, 13, false, GATHER>();
     default: return cudaErrorInvalidValue;
     }
 }
@@ -102,8 +100,7 @@ int occupancy_any(int variant, bool mixed)
     case 4: return mixed ? occupancy_variant<6, 6, 6, true, GATHER>() : occupancy_variant<6, 6, 6, false, GATHER>();
     case 5: return mixed ? occupancy_variant<8, 8, 16, true, GATHER>() : occupancy_variant<8, 8, 16, false, GATHER>();
     case 6: return mixed ? occupancy_variant<7, 13, 13, true, GATHER>() : occupancy_variant<7, 13, 13, false, GATHER>();
-    case 7: return mixed ? occupancy_variant<9, 9, 13, true, GATHER>() : occupancy_variant<9, 9, 13, false, GATHER>();
-    case 8: return mixed ? occupancy_variant<7, 7, 13, true, GATHER>() : occupancy_variant<7, 7, 13, false, GATHER>();
+    case 7: return mixed ? occupancy_variant<7, 7, 13, true, GATHER>() : occupancy_variant<7, 7, 13, false, GATHER>();
     default: return 0;
     }
 }
